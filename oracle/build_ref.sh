@@ -1,0 +1,28 @@
+#!/bin/sh
+# Build the unmodified reference skid (N-BodyShop/skid v1.4.1) from its own
+# source files, where they lie, into oracle/_ref/.  Test infrastructure only:
+# the binaries are the oracle's reference leg and never part of the product.
+#
+#   oracle/_ref/skid       reference skid, as shipped
+#   oracle/_ref/skid_nsp   built by build_ref_nsp.sh (patched oracle for -nsp)
+#
+# The only missing dependency is SunRPC/tirpc XDR; oracle/xdr_shim provides
+# the handful of XDR routines the reference calls.  -ffp-contract=off keeps
+# a*b+c unfused on hosts whose gcc contracts to FMA by default (aarch64).
+#
+# Usage: sh oracle/build_ref.sh [reference-dir]   (default /root/reference)
+set -eu
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/kd.c" ]; then
+    echo "build_ref: no reference sources at $REF" >&2
+    exit 2
+fi
+mkdir -p "$OUT"
+CFLAGS="-O2 -ffp-contract=off -D_GNU_SOURCE -w -I$HERE/xdr_shim"
+gcc $CFLAGS -o "$OUT/skid" \
+    "$REF/main.c" "$REF/kd.c" "$REF/smooth1.c" "$REF/grav.c" \
+    "$REF/cosmo.c" "$REF/romberg.c" "$REF/runge.c" \
+    "$HERE/xdr_shim/xdr_shim.c" -lm
+echo "build_ref: built $OUT/skid"

@@ -1,0 +1,226 @@
+"""ORACLE -- TEST INFRASTRUCTURE ONLY.
+
+ctypes front end of the CPU restatement in skid_oracle.c.  Only the tests,
+``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this
+module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libskidoracle.so")
+SRC = os.path.join(HERE, "skid_oracle.c")
+REF_SKID = os.path.join(HERE, "_ref", "skid")
+
+FLT_MAX = float(np.finfo(np.float32).max)
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement (gcc, no FMA contraction)."""
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "skid_oracle.h"))):
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                               "-o", tmp, SRC, "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def build_reference(ref_dir: str = "/root/reference") -> str | None:
+    """Build the unmodified reference into oracle/_ref when its sources exist."""
+    if not os.path.exists(os.path.join(ref_dir, "kd.c")):
+        return None
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), ref_dir],
+                          stdout=subprocess.DEVNULL)
+    return REF_SKID
+
+
+class Params(C.Structure):
+    _fields_ = [("period", C.c_float * 3), ("center", C.c_float * 3), ("periodic", C.c_int),
+                ("nSmooth", C.c_int), ("fTau", C.c_float), ("fCvg", C.c_float),
+                ("fScoop", C.c_float), ("fStep", C.c_float), ("fDensMin", C.c_float),
+                ("fTempMax", C.c_float), ("fMassMax", C.c_float), ("bGasAndDark", C.c_int),
+                ("bGasOnly", C.c_int), ("bForceInitialCut", C.c_int),
+                ("bNoScatterCut", C.c_int), ("nMinMembers", C.c_int), ("nMaxMembers", C.c_int),
+                ("bNoUnbind", C.c_int), ("iSoftType", C.c_int), ("bEps", C.c_int),
+                ("fEps", C.c_float), ("G", C.c_float), ("Omega0", C.c_float),
+                ("Lambda", C.c_float), ("fQuintess", C.c_float), ("H0", C.c_float),
+                ("z", C.c_float), ("maxIter", C.c_int), ("verbose", C.c_int)]
+
+
+class Group(C.Structure):
+    _fields_ = [("nMembers", C.c_int), ("fMass", C.c_float), ("rel", C.c_float * 3),
+                ("rCenter", C.c_float * 3), ("rBound", C.c_float * 3), ("vcm", C.c_float * 3),
+                ("fRadius", C.c_float)]
+
+
+class Result(C.Structure):
+    _fields_ = [("nScatterInit", C.c_int), ("nExtraScat", C.c_int), ("nMove", C.c_int),
+                ("nIter", C.c_int), ("nGroupFoF", C.c_int), ("nUnbound", C.c_int),
+                ("nGroup", C.c_int), ("nScatFinal", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        f = C.POINTER(C.c_float)
+        d = C.POINTER(C.c_double)
+        i = C.POINTER(C.c_int)
+        u = C.POINTER(C.c_uint)
+        _lib.or_knn_ball2.argtypes = [C.c_int, f, C.c_int, f, f]
+        _lib.or_knn_ball2_brute.argtypes = [C.c_int, f, C.c_int, f, f]
+        _lib.or_density.argtypes = [C.c_int, f, f, f, f, d]
+        _lib.or_replica_mask.argtypes = [C.c_int, f, f, f, f, C.c_int, u]
+        _lib.or_field.argtypes = [C.c_int, f, f, f, u, C.c_int, f, f, d, u]
+        _lib.or_fof.argtypes = [C.c_int, f, f, C.c_float, i, i]
+        _lib.or_d2.argtypes = [f, f, f]
+        _lib.or_d2.restype = C.c_float
+        _lib.or_run.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_int, C.c_double,
+                                f, f, f, f, f, i, C.POINTER(Group), C.c_int, f, f, f,
+                                C.POINTER(Result)]
+    return _lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _up(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint))
+
+
+def _period(period):
+    if period is None:
+        return np.full(3, FLT_MAX, np.float32)
+    p = np.asarray(period, np.float32)
+    return np.full(3, p, np.float32) if p.ndim == 0 else p.copy()
+
+
+def knn_ball2(pos, k, period=None, brute=False):
+    pos = np.ascontiguousarray(pos, np.float32)
+    out = np.empty(len(pos), np.float32)
+    fn = lib().or_knn_ball2_brute if brute else lib().or_knn_ball2
+    rc = fn(len(pos), _fp(pos), int(k), _fp(_period(period)), _fp(out))
+    if rc:
+        raise ValueError("oracle knn failed")
+    return out
+
+
+def density(pos, mass, ball2, period=None):
+    pos = np.ascontiguousarray(pos, np.float32)
+    mass = np.ascontiguousarray(mass, np.float32)
+    ball2 = np.ascontiguousarray(ball2, np.float32)
+    out = np.empty(len(pos), np.float64)
+    lib().or_density(len(pos), _fp(pos), _fp(mass), _fp(ball2), _fp(_period(period)), _dp(out))
+    return out
+
+
+def replica_mask(pos, ball2, period=None, center=(0, 0, 0), periodic=True):
+    pos = np.ascontiguousarray(pos, np.float32)
+    ball2 = np.ascontiguousarray(ball2, np.float32)
+    out = np.empty(len(pos), np.uint32)
+    lib().or_replica_mask(len(pos), _fp(pos), _fp(ball2), _fp(_period(period)),
+                          _fp(np.asarray(center, np.float32)), int(periodic), _up(out))
+    return out
+
+
+def field(spos, smass, sball2, alive, mpos, period=None):
+    """Move field (minus the SPH density gradient) at mover positions, FP64."""
+    spos = np.ascontiguousarray(spos, np.float32)
+    smass = np.ascontiguousarray(smass, np.float32)
+    sball2 = np.ascontiguousarray(sball2, np.float32)
+    alive = np.ascontiguousarray(alive, np.uint32)
+    mpos = np.ascontiguousarray(mpos, np.float32)
+    acc = np.empty((len(mpos), 3), np.float64)
+    touched = np.empty(len(spos), np.uint32)
+    lib().or_field(len(spos), _fp(spos), _fp(smass), _fp(sball2), _up(alive), len(mpos),
+                   _fp(mpos), _fp(_period(period)), _dp(acc), _up(touched))
+    return acc, touched
+
+
+def fof(pos, tau, period=None, iorder=None):
+    pos = np.ascontiguousarray(pos, np.float32)
+    n = len(pos)
+    io = np.arange(n, dtype=np.int32) if iorder is None else np.ascontiguousarray(iorder, np.int32)
+    grp = np.empty(n, np.int32)
+    ng = lib().or_fof(n, _fp(pos), _fp(_period(period)), float(tau), _ip(io), _ip(grp))
+    return grp, ng
+
+
+def d2(q, c, period=None):
+    q = np.ascontiguousarray(q, np.float32)
+    c = np.ascontiguousarray(c, np.float32)
+    return float(lib().or_d2(_fp(q), _fp(c), _fp(_period(period))))
+
+
+def run(snap, flags, verbose=False, max_iter=0):
+    """Run the whole pipeline on a Snapshot with skid-style options (a
+    ``skid_gb300.options.Options``).  Returns a dict of arrays."""
+    from skid_gb300.options import Options
+    o = flags if isinstance(flags, Options) else Options.parse(flags)
+    p = Params()
+    for d in range(3):
+        p.period[d] = o.period[d]
+        p.center[d] = o.center[d]
+    p.periodic = int(o.periodic)
+    p.nSmooth = o.nSmooth
+    p.fTau, p.fCvg, p.fScoop, p.fStep = o.fTau, o.fCvg, o.fScoop, o.fStep
+    p.fDensMin, p.fTempMax, p.fMassMax = o.fDensMin, o.fTempMax, o.fMassMax
+    p.bGasAndDark, p.bGasOnly, p.bForceInitialCut = int(o.bGasAndDark), int(o.bGasOnly), int(o.bForceInitialCut)
+    p.bNoScatterCut = int(o.bNoScatterCut)
+    p.nMinMembers, p.nMaxMembers, p.bNoUnbind = o.nMembers, o.nMaxMembers, int(o.bNoUnbind)
+    p.iSoftType = o.iSoftType
+    p.bEps, p.fEps = int(o.bEps), o.fEps
+    p.G, p.Omega0, p.Lambda, p.fQuintess, p.H0, p.z = o.G, o.Omega0, o.Lambda, o.fQuintess, o.H0, o.z
+    p.maxIter = max_iter or o.maxIter
+    p.verbose = int(verbose)
+    n = snap.n
+    pos = np.ascontiguousarray(snap.pos, np.float32)
+    vel = np.ascontiguousarray(snap.vel, np.float32)
+    mass = np.ascontiguousarray(snap.mass, np.float32)
+    soft = np.ascontiguousarray(snap.soft, np.float32)
+    temp = np.ascontiguousarray(snap.temp, np.float32)
+    grp = np.empty(n, np.int32)
+    cap = n + 1
+    groups = (Group * cap)()
+    rho = np.empty(n, np.float32)
+    ball2 = np.empty(n, np.float32)
+    moved = np.empty((n, 3), np.float32)
+    res = Result()
+    rc = lib().or_run(C.byref(p), snap.n_gas, snap.n_dark, snap.n_star, snap.time,
+                      _fp(pos), _fp(vel), _fp(mass), _fp(soft), _fp(temp), _ip(grp), groups, cap,
+                      _fp(rho), _fp(ball2), _fp(moved), C.byref(res))
+    if rc:
+        raise ValueError(f"oracle run failed: {rc}")
+    ng = res.nGroup + 1
+    gr = {
+        "nMembers": np.array([groups[g].nMembers for g in range(ng)], np.int64),
+        "fMass": np.array([groups[g].fMass for g in range(ng)], np.float32),
+        "rCenter": np.array([list(groups[g].rCenter) for g in range(ng)], np.float32),
+        "vcm": np.array([list(groups[g].vcm) for g in range(ng)], np.float32),
+        "rBound": np.array([list(groups[g].rBound) for g in range(ng)], np.float32),
+        "fRadius": np.array([groups[g].fRadius for g in range(ng)], np.float32),
+    }
+    return {"grp": grp, "groups": gr, "rho": rho, "ball2": ball2, "moved": moved,
+            "nScatterInit": res.nScatterInit, "nExtraScat": res.nExtraScat,
+            "nMove": res.nMove, "nIter": res.nIter, "nGroupFoF": res.nGroupFoF,
+            "nUnbound": res.nUnbound, "nGroup": res.nGroup, "nScatFinal": res.nScatFinal}

@@ -1,0 +1,158 @@
+"""Seeded synthetic clustered particle sets (NFW halos + background).
+
+skid ships no benchmark data; the workloads are synthetic stand-ins shaped
+like the snapshots skid is run on: a periodic unit box centred on 0 (skid's
+``-p 1``), total mass 1 (mean density 1) and G = 1.
+
+Halo masses are log-uniform over ``dex`` decades and normalised so the halos
+hold ``halo_frac`` of the particles; r200 scales as M^(1/3) with the largest
+equal to ``r200_max``; concentrations are uniform in ``conc``; radii come from
+the inverse CDF of the truncated NFW enclosed mass mu(x) = ln(1+x) - x/(1+x),
+x <= c; directions are isotropic and centres uniform.  Halo particles get an
+isotropic Gaussian velocity of dispersion sqrt(G M / (2 r200)) about a bulk
+velocity; the background is uniform with small Gaussian velocities.  Dark
+softening is eps = 0.02 N^(-1/3).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from . import tipsy
+
+SEED_BASE = 0x5C1D
+
+
+@dataclasses.dataclass(frozen=True)
+class HaloSpec:
+    n: int                   # particles
+    n_halo: int              # number of halos
+    dex: float               # halo mass range in decades
+    conc: tuple              # concentration range
+    r200_max: float          # r200 of the most massive halo
+    halo_frac: float         # fraction of particles in halos
+    seed: int
+    gas_frac: float = 0.0    # fraction of particles that are gas (mixed runs)
+    gas_mass_ratio: float = 0.2
+    gas_temp: float = 1.0e4
+
+
+# The workloads.  Skid flags that go with each are in WORKLOAD_FLAGS.
+CONFIGS = {
+    0: HaloSpec(32768, 20, 1.5, (5.0, 15.0), 0.05, 0.60, SEED_BASE + 0),
+    1: HaloSpec(1 << 21, 800, 3.0, (4.0, 20.0), 0.02, 0.55, SEED_BASE + 1),
+    3: HaloSpec(1 << 20, 400, 3.0, (4.0, 20.0), 0.02, 0.55, SEED_BASE + 3),
+    4: HaloSpec(1 << 24, 6000, 3.5, (4.0, 20.0), 0.02, 0.50, SEED_BASE + 4, gas_frac=0.5),
+}
+
+
+def hubble_for(omega0: float) -> float:
+    """Self-consistent H0 for G=1, mean density 1: H0 = sqrt(8 pi / (3 Omega0))."""
+    return math.sqrt(8.0 * math.pi / (3.0 * omega0))
+
+
+def _nfw_x(u: np.ndarray, c: np.ndarray) -> np.ndarray:
+    """Solve mu(x) = u mu(c) for x in [0, c] by bisection (mu is increasing)."""
+    mu = lambda x: np.log1p(x) - x / (1.0 + x)
+    target = u * mu(c)
+    lo = np.zeros_like(u)
+    hi = np.array(c, dtype=np.float64, copy=True)
+    for _ in range(60):
+        mid = 0.5 * (lo + hi)
+        below = mu(mid) < target
+        lo = np.where(below, mid, lo)
+        hi = np.where(below, hi, mid)
+    return 0.5 * (lo + hi)
+
+
+def _wrap32(x: np.ndarray) -> np.ndarray:
+    """Wrap float64 coordinates into [-0.5, 0.5) and round to float32 in range."""
+    w = x - np.floor(x + 0.5)
+    f = w.astype(np.float32)
+    f[f >= np.float32(0.5)] = np.float32(-0.5)
+    f[f < np.float32(-0.5)] = np.float32(-0.5)
+    return f
+
+
+def make_halos(spec: HaloSpec):
+    """Return (pos, vel, mass, soft, temp, n_gas) in iOrder (gas first)."""
+    rng = np.random.default_rng(spec.seed)
+    n = spec.n
+    n_halo_p = int(round(spec.halo_frac * n))
+    # Halo masses and particle counts.
+    logm = rng.uniform(0.0, spec.dex, spec.n_halo)
+    m = 10.0 ** logm
+    counts = np.floor(n_halo_p * m / m.sum()).astype(np.int64)
+    rem = n_halo_p - counts.sum()
+    order = np.argsort(-(n_halo_p * m / m.sum() - counts))
+    counts[order[:rem]] += 1
+    r200 = spec.r200_max * (m / m.max()) ** (1.0 / 3.0)
+    conc = rng.uniform(spec.conc[0], spec.conc[1], spec.n_halo)
+    centres = rng.uniform(-0.5, 0.5, (spec.n_halo, 3))
+    bulk = rng.normal(0.0, 0.1, (spec.n_halo, 3))
+    hid = np.repeat(np.arange(spec.n_halo), counts)
+    u = rng.uniform(0.0, 1.0, n_halo_p)
+    x = _nfw_x(u, conc[hid])
+    r = x * (r200[hid] / conc[hid])
+    costh = rng.uniform(-1.0, 1.0, n_halo_p)
+    phi = rng.uniform(0.0, 2.0 * math.pi, n_halo_p)
+    sinth = np.sqrt(1.0 - costh * costh)
+    d = np.stack([sinth * np.cos(phi), sinth * np.sin(phi), costh], axis=1)
+    hpos = centres[hid] + r[:, None] * d
+    mhalo = counts.astype(np.float64) / n        # halo mass in units of total mass 1
+    sig = np.sqrt(mhalo / (2.0 * r200))
+    hvel = bulk[hid] + rng.normal(0.0, 1.0, (n_halo_p, 3)) * sig[hid][:, None]
+    nb = n - n_halo_p
+    bpos = rng.uniform(-0.5, 0.5, (nb, 3))
+    bvel = rng.normal(0.0, 0.05, (nb, 3))
+    pos = np.concatenate([hpos, bpos])
+    vel = np.concatenate([hvel, bvel])
+    perm = rng.permutation(n)
+    pos, vel = pos[perm], vel[perm]
+    n_gas = int(round(spec.gas_frac * n))
+    eps = 0.02 * n ** (-1.0 / 3.0)
+    mass = np.full(n, 1.0, np.float64)
+    mass[:n_gas] = spec.gas_mass_ratio
+    mass /= mass.sum()
+    temp = np.zeros(n, np.float32)
+    temp[:n_gas] = spec.gas_temp
+    return (_wrap32(pos), vel.astype(np.float32), mass.astype(np.float32),
+            np.full(n, eps, np.float32), temp, n_gas)
+
+
+def make_snapshot(spec: HaloSpec, time: float = 1.0) -> tipsy.Snapshot:
+    pos, vel, mass, soft, temp, n_gas = make_halos(spec)
+    n = len(mass)
+    return tipsy.Snapshot(time, n_gas, n - n_gas, 0, pos, vel, mass, soft, temp)
+
+
+def write_snapshot(path, snap: tipsy.Snapshot, standard: bool = False) -> None:
+    gas, dark, star = tipsy.snapshot_records(snap)
+    tipsy.write_tipsy(path, snap.time, gas, dark, star, standard=standard)
+
+
+def subvolume_specs(n_vol: int = 96, seed: int = SEED_BASE + 2, lo: int = 14, hi: int = 20):
+    """Uneven independent subvolumes: N log-uniform in [2^lo, 2^hi], halos
+    proportional to N, nSmooth from {32, 64, 128}, tau = 0.5 N^(-1/3)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_vol):
+        n = int(round(2.0 ** rng.uniform(lo, hi)))
+        n_halo = max(1, int(round(800 * n / (1 << 21))))
+        k = int(rng.choice([32, 64, 128]))
+        tau = 0.5 * n ** (-1.0 / 3.0)
+        spec = HaloSpec(n, n_halo, 3.0, (4.0, 20.0), 0.02, 0.55, seed * 1000 + i)
+        out.append((spec, k, tau))
+    return out
+
+
+# skid command-line flags for each workload (the reference's own flag names).
+WORKLOAD_FLAGS = {
+    0: ["-tau", "0.01", "-s", "64", "-m", "16", "-p", "1", "-H", f"{hubble_for(1.0):.6g}"],
+    1: ["-tau", "0.004", "-s", "64", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
+        "-H", f"{hubble_for(0.3):.6g}"],
+    3: ["-tau", "0.005", "-s", "64", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
+        "-H", f"{hubble_for(0.3):.6g}"],
+}
