@@ -1,0 +1,184 @@
+/*
+ * skid_gpu.h -- C ABI of libskidgpu, the GB300 (sm_103a) implementation of
+ * SKID's group-finding path (N-BodyShop/skid v1.4.1).
+ *
+ * The reference has no plugin or FFI layer: its driver main.c calls the
+ * internal API of kd.h:338-365 and smooth1.h:94-99 in a fixed order
+ * (main.c:347-485).  Each entry point below replaces one of those calls (or
+ * one step of main.c) and says which.  A host program (the `skid` CLI in
+ * skid_gb300/host, or Python through ctypes) makes the same sequence of calls
+ * and writes the same output files.
+ *
+ * Conventions
+ *  - Every call returns 0 on success or a negative SKID_E* code; nothing in
+ *    the library exits, asserts or prints (progress lines are the caller's).
+ *  - A context owns all device memory; host buffers are the caller's and are
+ *    copied (per-particle arrays are indexed by iOrder: gas, dark, star).
+ *  - Device-side failures (a bounded wait that ran out, a capacity overflow)
+ *    are latched in a device status word and returned by the next call that
+ *    synchronises; skid_last_error() repeats the first one.
+ *  - One context per host thread; calls on a context are serialised on its
+ *    own CUDA stream.  Contexts are independent.
+ *  - Positions are float32; FP64 appears only in per-group sums.
+ */
+#ifndef SKID_GPU_H
+#define SKID_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SKID_OK 0
+#define SKID_EINVAL -1      /* bad argument or call order                   */
+#define SKID_ENOMEM -2      /* device or host allocation failed             */
+#define SKID_ECUDA -3       /* CUDA runtime error                           */
+#define SKID_ETIMEOUT -4    /* a bounded device-side wait ran out           */
+#define SKID_EOVERFLOW -5   /* an internal capacity was exceeded            */
+#define SKID_ENODEV -6      /* no usable sm_103 device                      */
+#define SKID_ESTATE -7      /* call made in the wrong pipeline state        */
+
+#define SKID_SOFT_PLUMMER 1 /* kd.h:24 */
+#define SKID_SOFT_SPLINE 2  /* kd.h:25 */
+
+typedef struct skid_ctx skid_ctx;
+
+/* Box and smoothing parameters fixed for a context (kdInit, kd.c:46-82,
+ * and smInit, smooth1.c:8-29).  period[] is FLT_MAX when not periodic. */
+typedef struct skid_params {
+    float period[3];
+    float center[3];
+    int periodic;        /* -p given: periodic replica scatterers (main.c:279) */
+    int nSmooth;         /* -s (main.c:185-190) */
+    int device;          /* CUDA device ordinal */
+} skid_params;
+
+/* One group as written to .gtp / .stat (PGROUP, kd.h:45-55). */
+typedef struct skid_group {
+    int nMembers;
+    float fMass;
+    float rel[3];
+    float rCenter[3];
+    float rBound[3];
+    float vcm[3];
+    float fRadius;
+} skid_group;
+
+/* Device time per stage, milliseconds (CUDA events); the reference prints
+ * user CPU time per stage (main.c:486-494). */
+typedef struct skid_timings {
+    float density_ms, moving_ms, fof_ms, micro_ms, groups_ms, unbind_ms, toosmall_ms;
+    long long gather_launches;  /* move-field kernel launches so far */
+    long long kernel_launches;  /* all kernels launched so far */
+} skid_timings;
+
+/* kdInit (kd.c:46-82) + smInit (smooth1.c:8-29). */
+int skid_create(skid_ctx **pctx, const skid_params *par);
+
+/* kdFinish (kd.c:1842-1850) + smFinish (smooth1.c:32-38). */
+int skid_destroy(skid_ctx *ctx);
+
+/* Error text for a SKID_E* code. */
+const char *skid_strerror(int code);
+
+/* First error latched on this context (0 if none). */
+int skid_last_error(const skid_ctx *ctx);
+
+/* kdReadTipsy (kd.c:122-222), data part: copies particles to the device.
+ * pos/vel are float[3n], mass/soft/temp float[n]; temp may be NULL (0).
+ * soft is hsmooth for gas and eps for dark and star. */
+int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double time,
+                       const float *pos, const float *vel, const float *mass,
+                       const float *soft, const float *temp);
+
+/* kdScatterActive (kd.c:669-693) with ScatterCriterion (kd.c:600-627). */
+int skid_scatter_active(skid_ctx *ctx, int bGasAndDark, int bGasOnly, int *nScatter);
+
+/* kdBuildTree (kd.c:371-460) + smDensityInit (smooth1.c:132-335): kNN ball
+ * radii, symmetric SPH density, periodic replica scatterers. */
+int skid_density(skid_ctx *ctx, int *nExtraScat);
+
+/* kdOutDensity's data (kd.c:1526-1547): density and fBall2 by iOrder
+ * (0 and -1 for particles that are not scatterers).  Either may be NULL. */
+int skid_get_density(skid_ctx *ctx, float *rho, float *ball2);
+
+/* kdInitMove (kd.c:630-666) with CutCriterion (kd.c:555-597). */
+int skid_init_move(skid_ctx *ctx, float fDensMin, float fTempMax, float fMassMax,
+                   int bGasAndDark, int bGasOnly, int *nMove);
+
+/* smAccDensity (smooth1.c:408-518) followed by kdMoveParticles
+ * (kd.c:702-732): one move step of the active movers.  bInitial selects the
+ * first-step cut (main.c:396-401); bNoCut is the -nsp switch.  nScatter gets
+ * the live scatterer copies after the cut. */
+int skid_move_step(skid_ctx *ctx, float fStep, int bInitial, int bNoCut, int *nScatter);
+
+/* kdPruneInactive (kd.c:735-793). */
+int skid_prune_inactive(skid_ctx *ctx, float fCvg, int *nActive);
+
+/* One outer iteration of main.c:409-419 (PRUNE_STEPS move steps and a
+ * prune), replayed from a CUDA graph after its first capture. */
+int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut,
+                      int *nActive, int *nScatter);
+
+/* kdReactivateMove (kd.c:796-799). */
+int skid_reactivate_move(skid_ctx *ctx);
+
+/* kdFoF (kd.c:802-917): friends-of-friends over all movers at link length
+ * fTau.  nGroup gets the number of groups (group 0 excluded).  Groups are
+ * numbered by ascending smallest member iOrder. */
+int skid_fof(skid_ctx *ctx, float fTau, int *nGroup);
+
+/* kdInitpGroup (kd.c:969-1005) + kdCalcCenter (kd.c:1013-1075). */
+int skid_group_centers(skid_ctx *ctx);
+
+/* kdInGroup (kd.c:920-962) + kdInitpGroup + kdReadCenter (kd.c:1083-1196):
+ * unbind-only mode.  grp[n] holds group ids by iOrder; centers (nGroup
+ * records, index 0 unused) gives rCenter and vcm, or NULL to use the centre
+ * of mass. */
+int skid_set_groups(skid_ctx *ctx, const int *grp, int nGroup, const skid_group *centers);
+
+/* kdSetSoft (kd.c:103-110). */
+int skid_set_soft(skid_ctx *ctx, float fEps);
+
+/* kdUnbind (kd.c:1299-1466) with kdCellPot/kdSubPot/kdAddScoopPot
+ * (grav.c:8-135).  a = 1/(1+z); aH = a*H(a) (kd.c:1317-1318).  Every group
+ * runs in one launch.  nUnbound gets the particles removed. */
+int skid_unbind(skid_ctx *ctx, int iSoftType, float fScoop, int bGasAndDark, int bNoUnbind,
+                int nMaxMembers, float G, float z, float a, float aH, int *nUnbound);
+
+/* kdTooSmall (kd.c:1251-1293). */
+int skid_too_small(skid_ctx *ctx, int nMembers, int *nGroup);
+
+/* Group ids by iOrder (kdOutGroup, kd.c:1502-1523) and the group records
+ * (kdWriteGroup, kd.c:1611-1687; fRadius computed here).  groups has room
+ * for nGroup+1 records (index 0 = ungrouped).  Either may be NULL. */
+int skid_get_groups(skid_ctx *ctx, int *grp, skid_group *groups);
+
+/* Moved positions by iOrder (kdOutVector's data, kd.c:1550-1608); input
+ * position for particles that never moved. */
+int skid_get_moved(skid_ctx *ctx, float *pos);
+
+/* Densities after the first-step cut set untouched scatterers to 0
+ * (smooth1.c:463-470); kdOutStats reads these (kd.c:1790). */
+int skid_get_final_density(skid_ctx *ctx, float *rho);
+
+int skid_get_timings(skid_ctx *ctx, skid_timings *t);
+
+/* ---- Stage probes with explicit inputs (parity tests, adjoint checks). ---- */
+
+/* k-th nearest neighbour squared distance (self included) of each of n
+ * points among the same points (smooth1.c:41-243), written to ball2. */
+int skid_knn_ball2(skid_ctx *ctx, int n, const float *pos, int k, float *ball2);
+
+/* The move field at nm positions from the context's current live scatterer
+ * copies (smooth1.c:436-508): acc[3*nm] = sum m/(pi h^5) F(q) (x_c - y). */
+int skid_field(skid_ctx *ctx, int nm, const float *mpos, float *acc);
+
+/* Friends-of-friends of n explicit points (kd.c:802-917). */
+int skid_fof_points(skid_ctx *ctx, int n, const float *pos, float fTau, int *grp, int *nGroup);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

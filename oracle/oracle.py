@@ -82,7 +82,7 @@ def lib():
         _lib.or_knn_ball2_brute.argtypes = [C.c_int, f, C.c_int, f, f]
         _lib.or_density.argtypes = [C.c_int, f, f, f, f, d]
         _lib.or_replica_mask.argtypes = [C.c_int, f, f, f, f, C.c_int, u]
-        _lib.or_field.argtypes = [C.c_int, f, f, f, u, C.c_int, f, f, d, u]
+        _lib.or_field.argtypes = [C.c_int, f, f, f, u, C.c_int, f, f, d, d, u]
         _lib.or_fof.argtypes = [C.c_int, f, f, C.c_float, i, i]
         _lib.or_d2.argtypes = [f, f, f]
         _lib.or_d2.restype = C.c_float
@@ -144,17 +144,19 @@ def replica_mask(pos, ball2, period=None, center=(0, 0, 0), periodic=True):
 
 
 def field(spos, smass, sball2, alive, mpos, period=None):
-    """Move field (minus the SPH density gradient) at mover positions, FP64."""
+    """Move field (minus the SPH density gradient) at mover positions, FP64.
+    Returns (acc, sum of |term| per mover, touched copy bits per scatterer)."""
     spos = np.ascontiguousarray(spos, np.float32)
     smass = np.ascontiguousarray(smass, np.float32)
     sball2 = np.ascontiguousarray(sball2, np.float32)
     alive = np.ascontiguousarray(alive, np.uint32)
     mpos = np.ascontiguousarray(mpos, np.float32)
     acc = np.empty((len(mpos), 3), np.float64)
+    absacc = np.empty(len(mpos), np.float64)
     touched = np.empty(len(spos), np.uint32)
     lib().or_field(len(spos), _fp(spos), _fp(smass), _fp(sball2), _up(alive), len(mpos),
-                   _fp(mpos), _fp(_period(period)), _dp(acc), _up(touched))
-    return acc, touched
+                   _fp(mpos), _fp(_period(period)), _dp(acc), _dp(absacc), _up(touched))
+    return acc, absacc, touched
 
 
 def fof(pos, tau, period=None, iorder=None):

@@ -429,6 +429,7 @@ typedef struct {
     float b;
     double ih2, fnorm;
     double *acc;
+    double *absacc;
     int hit;
 } field_ctx;
 
@@ -445,12 +446,13 @@ static void field_visit(void *vctx, int j)
     c->acc[3 * (size_t)j + 0] += dx * F;
     c->acc[3 * (size_t)j + 1] += dy * F;
     c->acc[3 * (size_t)j + 2] += dz * F;
+    if (c->absacc) c->absacc[j] += fabs(F) * sqrt((double)d2);
     c->hit = 1;
 }
 
 static void field_core(const ktree *mt, int ns, const float *spos, const float *smass,
                        const float *sball2, const unsigned int *alive, const float period[3],
-                       double *acc, unsigned int *touched)
+                       double *acc, double *absacc, unsigned int *touched)
 {
     static const float zero_period[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
     for (int i = 0; i < ns; ++i) {
@@ -477,6 +479,7 @@ static void field_core(const ktree *mt, int ns, const float *spos, const float *
             c.ih2 = ih2;
             c.fnorm = fnorm;
             c.acc = acc;
+            c.absacc = absacc;
             c.hit = 0;
             if (mt->n > 0) range_rec(mt, 0, c.cpos, b, zero_period, 0, sball2[i], field_visit, &c);
             if (c.hit && touched) touched[i] |= 1u << bit;
@@ -486,12 +489,13 @@ static void field_core(const ktree *mt, int ns, const float *spos, const float *
 
 int or_field(int ns, const float *spos, const float *smass, const float *sball2,
              const unsigned int *alive_mask, int nm, const float *mpos,
-             const float period[3], double *acc, unsigned int *touched_mask)
+             const float period[3], double *acc, double *absacc, unsigned int *touched_mask)
 {
     ktree mt;
     kt_build(&mt, mpos, NULL, nm);
     memset(acc, 0, (size_t)nm * 3 * sizeof(double));
-    field_core(&mt, ns, spos, smass, sball2, alive_mask, period, acc, touched_mask);
+    if (absacc) memset(absacc, 0, (size_t)nm * sizeof(double));
+    field_core(&mt, ns, spos, smass, sball2, alive_mask, period, acc, absacc, touched_mask);
     kt_free(&mt);
     return 0;
 }
@@ -802,7 +806,7 @@ static int acc_pass(const or_params *P, scat_t *S, int nA, const float *mpos, do
     ktree mt;
     kt_build(&mt, mpos, NULL, nA);
     memset(acc, 0, (size_t)nA * 3 * sizeof(double));
-    field_core(&mt, S->ns, S->pos, S->mass, S->ball2, S->alive, P->period, acc, touched);
+    field_core(&mt, S->ns, S->pos, S->mass, S->ball2, S->alive, P->period, acc, NULL, touched);
     kt_free(&mt);
     float fScatDens = 0.0f;
     for (int i = 0; i < S->ns; ++i) {

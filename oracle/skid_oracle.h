@@ -91,7 +91,8 @@ int or_replica_mask(int ns, const float *spos, const float *ball2,
                     unsigned int *exist_mask);
 int or_field(int ns, const float *spos, const float *smass, const float *sball2,
              const unsigned int *alive_mask, int nm, const float *mpos,
-             const float period[3], double *acc, unsigned int *touched_mask);
+             const float period[3], double *acc, double *absacc,
+             unsigned int *touched_mask);
 
 int or_fof(int n, const float *pos, const float period[3], float tau,
            const int *iorder, int *grp);

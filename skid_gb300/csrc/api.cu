@@ -1,0 +1,690 @@
+// C ABI of libskidgpu (include/skid_gpu.h): the context and the pipeline
+// stages of main.c:347-485 on one GB300.
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "ctx.h"
+
+using namespace skid;
+
+namespace {
+
+__global__ void pack_particles(const float *pos, const float *vel, const float *mass,
+                               const float *soft, const float *temp, int n, float4 *pos4,
+                               float4 *vel4, float *tempo)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        pos4[i] = make_float4(pos[3 * (size_t)i], pos[3 * (size_t)i + 1], pos[3 * (size_t)i + 2],
+                              mass[i]);
+        vel4[i] = make_float4(vel[3 * (size_t)i], vel[3 * (size_t)i + 1], vel[3 * (size_t)i + 2],
+                              soft[i]);
+        tempo[i] = temp ? temp[i] : 0.0f;
+    }
+}
+
+// Scatterers are whole type ranges (ScatterCriterion depends on type only,
+// kd.c:600-627): map list index -> iOrder through up to three ranges.
+__global__ void gather_ranges(Ranges r, const float4 *__restrict__ pos4, float4 *out, int *io)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < r.n; i += gridDim.x * blockDim.x) {
+        int j = i, k = 0;
+        while (k < 2 && j >= r.len[k]) { j -= r.len[k]; ++k; }
+        int o = r.start[k] + j;
+        out[i] = pos4[o];
+        io[i] = o;
+    }
+}
+
+__global__ void permute_scat(const uint32_t *__restrict__ perm, const int *__restrict__ io_in,
+                             const float *__restrict__ b_sorted, const float *__restrict__ rho_sorted,
+                             int n, int *__restrict__ sidx, float *__restrict__ rho_io,
+                             float *__restrict__ ball2_io, float *__restrict__ rho_final)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int o = io_in[perm[i]];
+        sidx[i] = o;
+        rho_io[o] = rho_sorted[i];
+        rho_final[o] = rho_sorted[i];
+        ball2_io[o] = b_sorted[i];
+    }
+}
+
+__global__ void fill_float(float *p, float v, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+}
+
+__global__ void iota_kernel(int *p, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+}
+
+// CutCriterion (kd.c:555-597).
+__device__ __forceinline__ int ptype(int io, int nGas, int nDark, int n)
+{
+    return io < nGas ? 2 : (io < nGas + nDark ? 1 : (io < n ? 4 : 0));
+}
+
+__global__ void cut_criterion(const float4 *__restrict__ pos4, const float *__restrict__ rho,
+                              const float *__restrict__ temp, int n, int nGas, int nDark,
+                              int inType, float fDensMin, float fTempMax, float fMassMax, int bGD,
+                              int bGO, int *__restrict__ flag)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int t = ptype(i, nGas, nDark, n);
+        float m = pos4[i].w, r = rho[i], T = temp[i];
+        int ok = 0;
+        if (!(m > fMassMax)) {
+            switch (inType) {
+            case 1:
+                ok = r >= fDensMin;
+                break;
+            case 2: case 3:
+                if (bGD && t == 1 && r >= fDensMin) ok = 1;
+                else ok = t == 2 && r >= fDensMin && T <= fTempMax;
+                break;
+            case 4: case 5:
+                ok = t == 4;
+                break;
+            case 6: case 7:
+                if (bGD && t == 1 && r >= fDensMin) ok = 1;
+                else if (t == 2) ok = r >= fDensMin && T <= fTempMax;
+                else ok = t == 4 && !bGO;
+                break;
+            }
+        }
+        flag[i] = ok;
+    }
+}
+
+__global__ void compact_index(const int *__restrict__ flag, const int *__restrict__ pos, int n,
+                              int *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (flag[i]) out[pos[i]] = i;
+}
+
+__global__ void gather_by_index(const int *__restrict__ idx, const float4 *__restrict__ src, int n,
+                                float4 *__restrict__ dst)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        dst[i] = src[idx[i]];
+}
+
+__global__ void init_movers(const uint32_t *__restrict__ perm, const int *__restrict__ mio_in,
+                            const float4 *__restrict__ pos4, int n, int *__restrict__ mio,
+                            float4 *__restrict__ mpos, float4 *__restrict__ mold,
+                            int *__restrict__ act)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int o = mio_in[perm[i]];
+        float4 p = pos4[o];
+        p.w = 0.0f;
+        mio[i] = o;
+        mpos[i] = p;
+        mold[i] = p;
+        act[i] = i;
+    }
+}
+
+__global__ void moved_to_iorder(const float4 *__restrict__ mpos, const int *__restrict__ mio, int n,
+                                float *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int o = mio[i];
+        float4 p = mpos[i];
+        out[3 * (size_t)o] = p.x;
+        out[3 * (size_t)o + 1] = p.y;
+        out[3 * (size_t)o + 2] = p.z;
+    }
+}
+
+__global__ void pos4_to_xyz(const float4 *__restrict__ p, int n, float *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 q = p[i];
+        out[3 * (size_t)i] = q.x;
+        out[3 * (size_t)i + 1] = q.y;
+        out[3 * (size_t)i + 2] = q.z;
+    }
+}
+
+__global__ void unsort_floats(const uint32_t *__restrict__ perm, const float *__restrict__ in,
+                              int n, float *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[perm[i]] = in[i];
+}
+
+__global__ void xyz_to_pos4(const float *__restrict__ xyz, int n, float4 *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = make_float4(xyz[3 * (size_t)i], xyz[3 * (size_t)i + 1], xyz[3 * (size_t)i + 2],
+                             0.0f);
+}
+
+}  // namespace
+
+// Largest float <= the double threshold t (so float compares match the
+// reference's double compares, kd.c:724-727).
+float skid::float_floor(double t)
+{
+    float f = (float)t;
+    if ((double)f > t) f = nextafterf(f, -INFINITY);
+    return f;
+}
+
+float3 skid_ctx::wrap_hi() const
+{
+    return make_float3(float_floor((double)par.center[0] + 0.5 * (double)par.period[0]),
+                       float_floor((double)par.center[1] + 0.5 * (double)par.period[1]),
+                       float_floor((double)par.center[2] + 0.5 * (double)par.period[2]));
+}
+
+float3 skid_ctx::wrap_lo() const
+{
+    return make_float3(float_floor((double)par.center[0] - 0.5 * (double)par.period[0]),
+                       float_floor((double)par.center[1] - 0.5 * (double)par.period[1]),
+                       float_floor((double)par.center[2] - 0.5 * (double)par.period[2]));
+}
+
+// ---------------------------------------------------------------------
+// context helpers
+
+int skid_ctx::fail(int code)
+{
+    if (!last_error) last_error = code;
+    return code;
+}
+
+int skid_ctx::fail_cuda(cudaError_t e)
+{
+    (void)e;
+    cudaGetLastError();
+    return fail(SKID_ECUDA);
+}
+
+int skid_ctx::sync_check()
+{
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail_cuda(e);
+    unsigned s = 0;
+    e = cudaMemcpy(&s, d_status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail_cuda(e);
+    if (s & ST_TIMEOUT) return fail(SKID_ETIMEOUT);
+    if (s & ST_OVERFLOW) return fail(SKID_EOVERFLOW);
+    if (s) return fail(SKID_ECUDA);
+    return 0;
+}
+
+int skid_ctx::read_int(const int *d, int *h)
+{
+    cudaError_t e = cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return fail_cuda(e);
+    return sync_check();
+}
+
+void skid_ctx::timer_start()
+{
+    cudaEventRecord(ev0, st);
+}
+
+float skid_ctx::timer_stop()
+{
+    cudaEventRecord(ev1, st);
+    cudaEventSynchronize(ev1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    return ms;
+}
+
+FieldArgs skid_ctx::field_args(float fStep, bool initial, float *acc_out)
+{
+    FieldArgs a;
+    a.spos = S.spos.p;
+    a.saux = S.saux.p;
+    a.blo = stree.blo.p;
+    a.bhi = stree.bhi.p;
+    a.lo = stree.lo.p;
+    a.hi = stree.hi.p;
+    a.leafBase = stree.leafBase;
+    a.d_nS = S.d_nS;
+    a.mpos = M.mpos.p;
+    a.act = M.act.p;
+    a.d_nA = M.d_nA;
+    a.L = L;
+    a.hL = hL;
+    a.per = per;
+    a.fStep = fStep;
+    a.period = L;
+    a.wrapHi = wrap_hi();
+    a.wrapLo = wrap_lo();
+    a.acc_out = acc_out;
+    a.touched = S.touched.p;
+    a.touched_bits = initial ? S.tbits.p : nullptr;
+    a.d_work = d_scal + SC_WORK;
+    a.d_status = d_status;
+    return a;
+}
+
+// One move pass: field + move, cut, refit.  Stream-ordered, no host sync.
+int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut)
+{
+    skid_ctx *ctx = this;
+    FieldArgs a = field_args(fStep, initial, nullptr);
+    CK(field_move(a, nMove, st));
+    ++gather_launches;
+    CK(scatter_cut(S, initial, nocut, rho_final.p, ss, st));
+    CK(tree_refit(stree, S.spos.p, S.saux.p, S.d_nS, st));
+    return 0;
+}
+
+// ---------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+const char *skid_strerror(int code)
+{
+    switch (code) {
+    case SKID_OK: return "ok";
+    case SKID_EINVAL: return "invalid argument";
+    case SKID_ENOMEM: return "out of memory";
+    case SKID_ECUDA: return "CUDA runtime error";
+    case SKID_ETIMEOUT: return "bounded device wait ran out";
+    case SKID_EOVERFLOW: return "internal capacity exceeded";
+    case SKID_ENODEV: return "no usable sm_103 device";
+    case SKID_ESTATE: return "call made in the wrong pipeline state";
+    }
+    return "unknown error";
+}
+
+int skid_last_error(const skid_ctx *ctx) { return ctx ? ctx->last_error : SKID_EINVAL; }
+
+int skid_create(skid_ctx **pctx, const skid_params *par)
+{
+    if (!pctx || !par) return SKID_EINVAL;
+    *pctx = nullptr;
+    if (par->nSmooth < 1) return SKID_EINVAL;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= par->device || par->device < 0) {
+        cudaGetLastError();
+        return SKID_ENODEV;
+    }
+    if (cudaSetDevice(par->device) != cudaSuccess) return SKID_ENODEV;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, par->device) != cudaSuccess) return SKID_ENODEV;
+    if (prop.major < 10) return SKID_ENODEV;
+    skid_ctx *ctx = new (std::nothrow) skid_ctx();
+    if (!ctx) return SKID_ENOMEM;
+    ctx->par = *par;
+    ctx->L = make_float3(par->period[0], par->period[1], par->period[2]);
+    ctx->hL = make_float3(0.5f * par->period[0], 0.5f * par->period[1], 0.5f * par->period[2]);
+    ctx->per = par->period[0] < 0.25f * FLT_MAX;
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void **)&ctx->d_scal, SC_COUNT * sizeof(int)) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        delete ctx;
+        return SKID_ENOMEM;
+    }
+    cudaMemset(ctx->d_scal, 0, SC_COUNT * sizeof(int));
+    ctx->d_status = (unsigned *)(ctx->d_scal + SC_STATUS);
+    ctx->S.d_nS = ctx->d_scal + SC_NS;
+    ctx->S.d_nS2 = ctx->d_scal + SC_NS2;
+    ctx->S.d_floor = (unsigned *)(ctx->d_scal + SC_FLOOR);
+    ctx->S.d_live = ctx->d_scal + SC_LIVE;
+    ctx->M.d_nA = ctx->d_scal + SC_NA;
+    ctx->M.d_nA2 = ctx->d_scal + SC_NA2;
+    *pctx = ctx;
+    return 0;
+}
+
+int skid_destroy(skid_ctx *ctx)
+{
+    if (!ctx) return SKID_EINVAL;
+    cudaSetDevice(ctx->par.device);
+    cudaStreamSynchronize(ctx->st);
+    delete ctx;
+    return 0;
+}
+
+int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double time,
+                       const float *pos, const float *vel, const float *mass, const float *soft,
+                       const float *temp)
+{
+    if (!ctx || nGas < 0 || nDark < 0 || nStar < 0 || !pos || !vel || !mass || !soft)
+        return SKID_EINVAL;
+    long long nn = (long long)nGas + nDark + nStar;
+    if (nn > (1ll << 28)) return ctx->fail(SKID_EINVAL);
+    int n = (int)nn;
+    cudaSetDevice(ctx->par.device);
+    ctx->reset_pipeline();
+    ctx->n = n;
+    ctx->nGas = nGas;
+    ctx->nDark = nDark;
+    ctx->nStar = nStar;
+    ctx->time = time;
+    ctx->inType = (nDark ? 1 : 0) | (nGas ? 2 : 0) | (nStar ? 4 : 0);
+    if (ctx->alloc_particles(n)) return ctx->fail(SKID_ENOMEM);
+    if (n == 0) { ctx->stage = STAGE_LOADED; return 0; }
+    // staging: raw host arrays -> device, then pack to float4 records
+    float *d_raw = ctx->raw.p;
+    size_t n3 = 3 * (size_t)n;
+    CK(cudaMemcpyAsync(d_raw, pos, n3 * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_raw + n3, vel, n3 * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_raw + 2 * n3, mass, n * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_raw + 2 * n3 + n, soft, n * sizeof(float), cudaMemcpyHostToDevice,
+                       ctx->st));
+    if (temp)
+        CK(cudaMemcpyAsync(d_raw + 2 * n3 + 2 * (size_t)n, temp, n * sizeof(float),
+                           cudaMemcpyHostToDevice, ctx->st));
+    pack_particles<<<grid_for(n), 256, 0, ctx->st>>>(d_raw, d_raw + n3, d_raw + 2 * n3,
+                                                     d_raw + 2 * n3 + n,
+                                                     temp ? d_raw + 2 * n3 + 2 * (size_t)n : nullptr,
+                                                     n, ctx->pos4.p, ctx->vel4.p, ctx->temp.p);
+    CK(cudaGetLastError());
+    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho.p, 0.0f, n);
+    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho_final.p, 0.0f, n);
+    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->ball2.p, -1.0f, n);
+    CK(cudaMemsetAsync(ctx->grp.p, 0, n * sizeof(int), ctx->st));
+    ctx->kernel_launches += 4;
+    ctx->stage = STAGE_LOADED;
+    return ctx->sync_check();
+}
+
+int skid_scatter_active(skid_ctx *ctx, int bGasAndDark, int bGasOnly, int *nScatter)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_LOADED) return ctx->fail(SKID_ESTATE);
+    // ScatterCriterion (kd.c:600-627) per type
+    int t = ctx->inType;
+    bool gas = false, dark = false, star = false;
+    switch (t) {
+    case 1: dark = true; break;
+    case 2: case 3: gas = true; dark = bGasAndDark != 0; break;
+    case 4: case 5: star = true; break;
+    case 6: case 7:
+        if (bGasAndDark) { gas = dark = star = true; }
+        else { gas = true; star = !bGasOnly; }
+        break;
+    }
+    Ranges r;
+    r.n = 0;
+    int k = 0;
+    auto add = [&](bool on, int s, int l) {
+        if (on && l > 0) { r.start[k] = s; r.len[k] = l; r.n += l; ++k; }
+    };
+    add(gas, 0, ctx->nGas);
+    add(dark, ctx->nGas, ctx->nDark);
+    add(star, ctx->nGas + ctx->nDark, ctx->nStar);
+    for (; k < 3; ++k) { r.start[k] = 0; r.len[k] = 0; }
+    ctx->ranges = r;
+    ctx->nScatInit = r.n;
+    if (nScatter) *nScatter = r.n;
+    ctx->stage = STAGE_SCATTER;
+    return 0;
+}
+
+int skid_density(skid_ctx *ctx, int *nExtraScat)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_SCATTER) return ctx->fail(SKID_ESTATE);
+    int ns = ctx->nScatInit;
+    if (ns < ctx->par.nSmooth) return ctx->fail(SKID_EINVAL);   // smooth1.c:12
+    cudaSetDevice(ctx->par.device);
+    if (ctx->alloc_scatterers(ns)) return ctx->fail(SKID_ENOMEM);
+    cudaStream_t st = ctx->st;
+    ctx->timer_start();
+    Ranges r = ctx->ranges;
+    gather_ranges<<<grid_for(ns), 256, 0, st>>>(r, ctx->pos4.p, ctx->S.spos2.p, ctx->S.sidx2.p);
+    CK(cudaGetLastError());
+    CK(tree_build(ctx->stree, ctx->S.spos2.p, ns, true, ctx->ss, st));
+    CK(knn_ball2(ctx->stree, ctx->par.nSmooth, ctx->L, ctx->per, ctx->S.srho2.p,
+                 ctx->d_scal + SC_WORK, ctx->knn_heap, st));
+    // srho2 holds fBall2 (sorted); aux = (b, ih2, fNorm m, copies)
+    float3 blo = make_float3((float)((double)ctx->par.center[0] - 0.5 * (double)ctx->par.period[0]),
+                             (float)((double)ctx->par.center[1] - 0.5 * (double)ctx->par.period[1]),
+                             (float)((double)ctx->par.center[2] - 0.5 * (double)ctx->par.period[2]));
+    float3 bhi = make_float3((float)((double)ctx->par.center[0] + 0.5 * (double)ctx->par.period[0]),
+                             (float)((double)ctx->par.center[1] + 0.5 * (double)ctx->par.period[1]),
+                             (float)((double)ctx->par.center[2] + 0.5 * (double)ctx->par.period[2]));
+    CK(scatter_aux(ctx->stree.pos.p, ctx->S.srho2.p, ns, ctx->L, blo, bhi, ctx->par.periodic != 0,
+                   ctx->S.saux.p, ctx->d_scal + SC_EXTRA, st));
+    CK(tree_refit(ctx->stree, nullptr, ctx->S.saux.p, nullptr, st));
+    CK(density_gather(ctx->stree, ctx->S.srho2.p, ctx->L, ctx->per, ctx->S.srho.p,
+                      ctx->d_scal + SC_WORK, st));
+    permute_scat<<<grid_for(ns), 256, 0, st>>>(ctx->stree.perm.p, ctx->S.sidx2.p, ctx->S.srho2.p,
+                                               ctx->S.srho.p, ns, ctx->S.sidx.p, ctx->rho.p,
+                                               ctx->ball2.p, ctx->rho_final.p);
+    CK(cudaMemcpyAsync(ctx->S.spos.p, ctx->stree.pos.p, ns * sizeof(float4),
+                       cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(ctx->S.d_nS, &ctx->nScatInit, sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(ctx->S.touched.p, 0, ns, st));
+    CK(cudaMemsetAsync(ctx->S.tbits.p, 0, ns * sizeof(unsigned), st));
+    ctx->kernel_launches += 16;
+    int extra = 0;
+    if (int rc = ctx->read_int(ctx->d_scal + SC_EXTRA, &extra)) return rc;
+    ctx->nExtraScat = extra;
+    ctx->tim.density_ms += ctx->timer_stop();
+    if (nExtraScat) *nExtraScat = ctx->par.periodic ? extra : 0;
+    ctx->stage = STAGE_DENSITY;
+    return 0;
+}
+
+int skid_get_density(skid_ctx *ctx, float *rho, float *ball2)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_DENSITY) return ctx->fail(SKID_ESTATE);
+    if (rho) CK(cudaMemcpyAsync(rho, ctx->rho.p, ctx->n * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
+    if (ball2)
+        CK(cudaMemcpyAsync(ball2, ctx->ball2.p, ctx->n * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
+    return ctx->sync_check();
+}
+
+int skid_get_final_density(skid_ctx *ctx, float *rho)
+{
+    if (!ctx || !rho) return SKID_EINVAL;
+    if (ctx->stage < STAGE_DENSITY) return ctx->fail(SKID_ESTATE);
+    CK(cudaMemcpyAsync(rho, ctx->rho_final.p, ctx->n * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
+    return ctx->sync_check();
+}
+
+int skid_init_move(skid_ctx *ctx, float fDensMin, float fTempMax, float fMassMax, int bGasAndDark,
+                   int bGasOnly, int *nMove)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_DENSITY) return ctx->fail(SKID_ESTATE);
+    int n = ctx->n;
+    cudaStream_t st = ctx->st;
+    if (ctx->alloc_movers(n)) return ctx->fail(SKID_ENOMEM);
+    cut_criterion<<<grid_for(n), 256, 0, st>>>(ctx->pos4.p, ctx->rho.p, ctx->temp.p, n, ctx->nGas,
+                                               ctx->nDark, ctx->inType, fDensMin, fTempMax,
+                                               fMassMax, bGasAndDark, bGasOnly, ctx->M.keep.p);
+    CK(scan_exclusive(ctx->M.keep.p, ctx->M.kpos.p, n, ctx->M.d_nA, ctx->ss, st));
+    compact_index<<<grid_for(n), 256, 0, st>>>(ctx->M.keep.p, ctx->M.kpos.p, n, ctx->M.act2.p);
+    int nm = 0;
+    if (int rc = ctx->read_int(ctx->M.d_nA, &nm)) return rc;
+    ctx->nMove = nm;
+    // Morton order of the movers' starting positions keeps warps coherent.
+    if (nm > 0) {
+        gather_by_index<<<grid_for(nm), 256, 0, st>>>(ctx->M.act2.p, ctx->pos4.p, nm, ctx->M.mold.p);
+        CK(morton_order(ctx->M.mold.p, nm, ctx->ss, st));
+        init_movers<<<grid_for(nm), 256, 0, st>>>(ctx->ss.v0.p, ctx->M.act2.p, ctx->pos4.p, nm,
+                                                   ctx->M.mio.p, ctx->M.mpos.p, ctx->M.mold.p,
+                                                   ctx->M.act.p);
+        CK(cudaGetLastError());
+    }
+    CK(cudaMemcpyAsync(ctx->M.d_nA, &ctx->nMove, sizeof(int), cudaMemcpyHostToDevice, st));
+    ctx->kernel_launches += 8;
+    ctx->nActive = nm;
+    if (nMove) *nMove = nm;
+    ctx->stage = STAGE_MOVE;
+    return ctx->sync_check();
+}
+
+int skid_move_step(skid_ctx *ctx, float fStep, int bInitial, int bNoCut, int *nScatter)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
+    ctx->timer_start();
+    if (ctx->nMove > 0 || bInitial) {
+        if (int rc = ctx->enqueue_step(fStep, bInitial != 0, bNoCut != 0)) return rc;
+    }
+    int live = 0;
+    if (int rc = ctx->read_int(ctx->S.d_live, &live)) return rc;
+    float ms = ctx->timer_stop();
+    if (ctx->stage >= STAGE_FOF) ctx->tim.micro_ms += ms;
+    else ctx->tim.moving_ms += ms;
+    if (nScatter) *nScatter = live;
+    return 0;
+}
+
+int skid_prune_inactive(skid_ctx *ctx, float fCvg, int *nActive)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
+    ctx->timer_start();
+    CK(mover_prune(ctx->M, ctx->L, fCvg, ctx->ss, ctx->st));
+    int na = 0;
+    if (int rc = ctx->read_int(ctx->M.d_nA, &na)) return rc;
+    ctx->tim.moving_ms += ctx->timer_stop();
+    ctx->nActive = na;
+    if (nActive) *nActive = na;
+    return 0;
+}
+
+int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *nActive,
+                      int *nScatter)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
+    cudaStream_t st = ctx->st;
+    ctx->timer_start();
+    bool same = ctx->iter_graph && ctx->g_fStep == fStep && ctx->g_fCvg == fCvg &&
+                ctx->g_nocut == (bNoCut != 0);
+    bool ran = false;
+    if (!same) {
+        if (ctx->iter_graph) { cudaGraphExecDestroy(ctx->iter_graph); ctx->iter_graph = nullptr; }
+        if (!ctx->iter_eager_done) {
+            // the first iteration runs eagerly; it sizes every scratch buffer
+            for (int i = 0; i < PRUNE_STEPS; ++i)
+                if (int rc = ctx->enqueue_step(fStep, false, bNoCut != 0)) return rc;
+            CK(mover_prune(ctx->M, ctx->L, fCvg, ctx->ss, st));
+            ctx->iter_eager_done = true;
+            ran = true;
+        } else {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = 0;
+            for (int i = 0; i < PRUNE_STEPS && !rc; ++i)
+                rc = ctx->enqueue_step(fStep, false, bNoCut != 0);
+            if (!rc && mover_prune(ctx->M, ctx->L, fCvg, ctx->ss, st) != cudaSuccess) rc = SKID_ECUDA;
+            cudaError_t ce = cudaStreamEndCapture(st, &g);
+            if (rc) return ctx->fail(rc);
+            if (ce) return ctx->fail_cuda(ce);
+            ce = cudaGraphInstantiate(&ctx->iter_graph, g, 0);
+            cudaGraphDestroy(g);
+            if (ce) return ctx->fail_cuda(ce);
+            ctx->g_fStep = fStep;
+            ctx->g_fCvg = fCvg;
+            ctx->g_nocut = bNoCut != 0;
+        }
+    }
+    if (!ran) CK(cudaGraphLaunch(ctx->iter_graph, st));
+    ctx->kernel_launches += PRUNE_STEPS * 12 + 6;
+    int vals[2];
+    CK(cudaMemcpyAsync(&vals[0], ctx->M.d_nA, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&vals[1], ctx->S.d_live, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (int rc = ctx->sync_check()) return rc;
+    ctx->tim.moving_ms += ctx->timer_stop();
+    ctx->nActive = vals[0];
+    if (nActive) *nActive = vals[0];
+    if (nScatter) *nScatter = vals[1];
+    return 0;
+}
+
+int skid_reactivate_move(skid_ctx *ctx)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
+    iota_kernel<<<grid_for(ctx->nMove), 256, 0, ctx->st>>>(ctx->M.act.p, ctx->nMove);
+    CK(cudaMemcpyAsync(ctx->M.d_nA, &ctx->nMove, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+    ctx->nActive = ctx->nMove;
+    return ctx->sync_check();
+}
+
+int skid_get_moved(skid_ctx *ctx, float *pos)
+{
+    if (!ctx || !pos) return SKID_EINVAL;
+    if (ctx->stage < STAGE_LOADED) return ctx->fail(SKID_ESTATE);
+    int n = ctx->n;
+    float *d = ctx->raw.p;
+    pos4_to_xyz<<<grid_for(n), 256, 0, ctx->st>>>(ctx->pos4.p, n, d);
+    if (ctx->stage >= STAGE_MOVE && ctx->nMove > 0)
+        moved_to_iorder<<<grid_for(ctx->nMove), 256, 0, ctx->st>>>(ctx->M.mpos.p, ctx->M.mio.p,
+                                                                   ctx->nMove, d);
+    CK(cudaMemcpyAsync(pos, d, 3 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
+    return ctx->sync_check();
+}
+
+int skid_get_timings(skid_ctx *ctx, skid_timings *t)
+{
+    if (!ctx || !t) return SKID_EINVAL;
+    *t = ctx->tim;
+    t->gather_launches = ctx->gather_launches;
+    t->kernel_launches = ctx->kernel_launches;
+    return 0;
+}
+
+int skid_knn_ball2(skid_ctx *ctx, int n, const float *pos, int k, float *ball2)
+{
+    if (!ctx || n < 0 || !pos || !ball2 || k < 1 || k > n) return SKID_EINVAL;
+    cudaStream_t st = ctx->st;
+    Tree &t = ctx->probe_tree;
+    DBuf<float> &xyz = ctx->probe_f;
+    DBuf<float4> &p4 = ctx->probe_p4;
+    if (dalloc(xyz, 3 * (size_t)n + n) || dalloc(p4, n)) return ctx->fail(SKID_ENOMEM);
+    CK(cudaMemcpyAsync(xyz.p, pos, 3 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
+    xyz_to_pos4<<<grid_for(n), 256, 0, st>>>(xyz.p, n, p4.p);
+    CK(tree_build(t, p4.p, n, false, ctx->ss, st));
+    float *b_sorted = xyz.p;   // reuse: sorted results, then unsorted
+    float *b_out = xyz.p + n;
+    CK(knn_ball2(t, k, ctx->L, ctx->per, b_sorted, ctx->d_scal + SC_WORK, ctx->knn_heap, st));
+    unsort_floats<<<grid_for(n), 256, 0, st>>>(t.perm.p, b_sorted, n, b_out);
+    CK(cudaMemcpyAsync(ball2, b_out, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    return ctx->sync_check();
+}
+
+int skid_field(skid_ctx *ctx, int nm, const float *mpos, float *acc)
+{
+    if (!ctx || nm < 0 || !mpos || !acc) return SKID_EINVAL;
+    if (ctx->stage < STAGE_DENSITY) return ctx->fail(SKID_ESTATE);
+    cudaStream_t st = ctx->st;
+    DBuf<float> &xyz = ctx->probe_f;
+    DBuf<float4> &p4 = ctx->probe_p4;
+    DBuf<int> &act = ctx->probe_i;
+    if (dalloc(xyz, 3 * (size_t)nm) || dalloc(p4, nm) || dalloc(act, nm + 2) ||
+        dalloc(ctx->probe_acc, 3 * (size_t)nm))
+        return ctx->fail(SKID_ENOMEM);
+    CK(cudaMemcpyAsync(xyz.p, mpos, 3 * (size_t)nm * sizeof(float), cudaMemcpyHostToDevice, st));
+    xyz_to_pos4<<<grid_for(nm), 256, 0, st>>>(xyz.p, nm, p4.p);
+    iota_kernel<<<grid_for(nm), 256, 0, st>>>(act.p, nm);
+    CK(cudaMemcpyAsync(act.p + nm, &nm, sizeof(int), cudaMemcpyHostToDevice, st));
+    FieldArgs a = ctx->field_args(0.0f, false, ctx->probe_acc.p);
+    a.mpos = p4.p;
+    a.act = act.p;
+    a.d_nA = act.p + nm;
+    a.touched = ctx->probe_touched();
+    if (!a.touched) return ctx->fail(SKID_ENOMEM);
+    CK(field_move(a, nm, st));
+    CK(cudaMemcpyAsync(acc, ctx->probe_acc.p, 3 * (size_t)nm * sizeof(float), cudaMemcpyDeviceToHost,
+                       st));
+    return ctx->sync_check();
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+// Shared device helpers for libskidgpu (sm_103a).
+//
+// Distances reproduce the reference's float arithmetic exactly: no FMA
+// (explicit __fmul_rn/__fadd_rn), ((dx*dx + dy*dy) + dz*dz), and periodic
+// images formed as fl(x +/- L) before the subtraction (kd.h:122-214,
+// smooth1.c:72-75,104-107).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define SKID_LEAF 32          // points per tree leaf = one warp
+#define SKID_FULL 0xffffffffu
+
+namespace skid {
+
+// Device status word bits (latched; read by the host after a sync).
+enum : unsigned {
+    ST_TIMEOUT = 1u,     // a bounded wait ran out
+    ST_OVERFLOW = 2u,    // a capacity was exceeded
+    ST_BADSTATE = 4u,
+};
+
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+__device__ __forceinline__ float d2of(float dx, float dy, float dz)
+{
+    return fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+}
+
+// Query-frame component: the query's periodic image nearest the candidate,
+// then fl(image - c).  Same rule as the oracle's img_dx.
+__device__ __forceinline__ float img_dx(float q, float c, float L, float h)
+{
+    float d0 = fsub(q, c);
+    if (d0 > h) return fsub(fsub(q, L), c);
+    if (d0 < -h) return fsub(fadd(q, L), c);
+    return d0;
+}
+
+// Per-lane, per-box image class of a query coordinate: all candidates c in
+// [lo,hi] have q-c in [q-hi, q-lo].  Returns 0 (no shift for any), -1 (all
+// need q-L), +1 (all need q+L) or 2 (mixed: decide per candidate).
+__device__ __forceinline__ int img_class(float q, float lo, float hi, float h)
+{
+    float a = fsub(q, hi), b = fsub(q, lo);   // a <= b
+    if (a >= -h && b <= h) return 0;
+    if (a > h) return -1;
+    if (b < -h) return 1;
+    return 2;
+}
+
+// Lower bound of the float squared distance from q (any periodic image) to
+// a box, with an absolute per-dimension slack covering the roundings of
+// fl(fl(q+sL) - c); conservative for culling.
+__device__ __forceinline__ float box_lb1(float q, float lo, float hi, float L, bool per)
+{
+    float d = fmaxf(fmaxf(lo - q, q - hi), 0.0f);
+    if (per) {
+        float qp = q + L, qm = q - L;
+        d = fminf(d, fmaxf(fmaxf(lo - qp, qp - hi), 0.0f));
+        d = fminf(d, fmaxf(fmaxf(lo - qm, qm - hi), 0.0f));
+    }
+    float slack = 4.8e-7f * (fabsf(q) + (per ? L : 0.0f) + fmaxf(fabsf(lo), fabsf(hi)));
+    return fmaxf(d - slack, 0.0f);
+}
+
+__device__ __forceinline__ float box_lb(float3 q, float4 lo, float4 hi, float3 L, bool per)
+{
+    float dx = box_lb1(q.x, lo.x, hi.x, L.x, per);
+    float dy = box_lb1(q.y, lo.y, hi.y, L.y, per);
+    float dz = box_lb1(q.z, lo.z, hi.z, L.z, per);
+    return (dx * dx + dy * dy + dz * dz) * (1.0f - 4e-6f);
+}
+
+// Spread the low 21 bits of v to every third bit.
+__device__ __forceinline__ uint64_t spread3(uint64_t v)
+{
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+__device__ __forceinline__ uint64_t morton63(float3 p, float3 lo, float3 inv)
+{
+    float fx = fminf(fmaxf((p.x - lo.x) * inv.x, 0.0f), 2097151.0f);
+    float fy = fminf(fmaxf((p.y - lo.y) * inv.y, 0.0f), 2097151.0f);
+    float fz = fminf(fmaxf((p.z - lo.z) * inv.z, 0.0f), 2097151.0f);
+    return (spread3((uint64_t)fx) << 2) | (spread3((uint64_t)fy) << 1) | spread3((uint64_t)fz);
+}
+
+// Order-preserving float <-> uint for atomic min/max.
+__device__ __forceinline__ unsigned f2ord(float f)
+{
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__device__ __forceinline__ void set_status(unsigned *st, unsigned bit) { atomicOr(st, bit); }
+
+// Implicit complete binary tree over leaves (root 1, children 2i and 2i+1,
+// leaves at [nLeafP2, 2 nLeafP2)), the heap layout of kd.h:6-15.
+__device__ __forceinline__ int next_node(int c)
+{
+    // SETNEXT (kd.h:11-15): the next node in depth-first order after the
+    // subtree of c.
+    while (c & 1) c >>= 1;
+    return c + 1;
+}
+
+struct TreeView {
+    int n;               // points
+    int nLeaf;           // leaves holding points
+    int leafBase;        // nLeafP2: node index of leaf 0
+    const float4 *pos;   // sorted points (x, y, z, mass)
+    const float4 *lo;    // node boxes [2*leafBase]; lo.w: max ball2 below
+    const float4 *hi;    // hi.w: flags
+};
+
+}  // namespace skid

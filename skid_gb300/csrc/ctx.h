@@ -1,0 +1,256 @@
+// The skid_ctx behind the opaque handle of include/skid_gpu.h.
+#pragma once
+
+#include "../../include/skid_gpu.h"
+#include "internal.h"
+
+namespace skid {
+
+constexpr int PRUNE_STEPS = 5;   // main.c:13
+
+// Device scalar slots (ints) in ctx->d_scal.
+enum {
+    SC_WORK = 0,     // work-queue counter of tree walks
+    SC_STATUS = 1,   // latched status bits
+    SC_NS = 2,
+    SC_NS2 = 3,
+    SC_FLOOR = 4,
+    SC_LIVE = 5,
+    SC_NA = 6,
+    SC_NA2 = 7,
+    SC_EXTRA = 8,
+    SC_NG = 9,       // groups
+    SC_NG2 = 10,
+    SC_NUNB = 11,    // particles unbound
+    SC_WORK2 = 12,
+    SC_COUNT = 32
+};
+
+enum Stage {
+    STAGE_NONE = 0,
+    STAGE_LOADED,
+    STAGE_SCATTER,
+    STAGE_DENSITY,
+    STAGE_MOVE,
+    STAGE_FOF,
+    STAGE_GROUPS,
+    STAGE_UNBOUND,
+    STAGE_FINAL
+};
+
+struct Ranges {
+    int start[3], len[3], n;
+};
+
+float float_floor(double t);
+
+#define CK(x)                                               \
+    do {                                                    \
+        cudaError_t e__ = (x);                              \
+        if (e__ != cudaSuccess) return ctx->fail_cuda(e__); \
+    } while (0)
+
+// Group state (sized by the number of groups).
+struct GroupState {
+    int nGroup = 0;                 // including group 0
+    DBuf<int> start, count;         // member range per group in `members`
+    DBuf<int> members;              // iOrder, grouped, ascending iOrder inside a group
+    DBuf<int> gof;                  // group of each member slot
+    DBuf<skid_group> rec;           // per group record
+    DBuf<double> sums;              // per group FP64 sums
+    DBuf<int> map;                  // too-small remap
+    DBuf<int> gtmp, gtmp2;
+    DBuf<skid_group> rec2;
+};
+
+struct UnbindParams {
+    float3 period;
+    bool per;
+    float fScoop;
+    int nmax;          // -maxgroup
+    float G, a, aH, opz;
+    int plummer, subpot, nounbind;
+};
+
+struct UnbindScratch {
+    DBuf<float4> qr, qv, slist;
+    DBuf<float2> pot;
+    DBuf<int> qid, scnt, soff, nt, toff, cnt;
+    DBuf<int2> items;
+    DBuf<float> ssoft, usoft;
+};
+
+inline int grid_for(int n, int threads = 256)
+{
+    int b = (n + threads - 1) / threads;
+    int cap = num_sms() * 8;
+    if (b > cap) b = cap;
+    return b < 1 ? 1 : b;
+}
+
+// fof.cu
+cudaError_t fof_run(Tree &t, const float4 *pts, int np, const int *mio, int niorder, float tau,
+                    float3 L, bool per, SortScratch &ss, DBuf<int> &par, DBuf<int> &minio,
+                    DBuf<int> &flag, int *grp, int *d_ng, int *d_work, unsigned *d_status,
+                    cudaStream_t st);
+// groups.cu
+cudaError_t group_order(const int *grp, int n, int ng, SortScratch &ss, GroupState &G,
+                        cudaStream_t st);
+cudaError_t group_props(GroupState &G, const float4 *pos4, const float4 *vel4, const float4 *moved,
+                        float3 L, float3 wrapHi, float3 wrapLo, bool com, bool keep_centre,
+                        cudaStream_t st);
+cudaError_t too_small(GroupState &G, int *grp, int n, int nmin, int *d_ng, SortScratch &ss,
+                      cudaStream_t st);
+cudaError_t group_radius(GroupState &G, const int *grp, int n, const float4 *pos4, float3 L,
+                         cudaStream_t st);
+// unbind.cu
+cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *pos4,
+                       const float4 *vel4, Tree &ut, const UnbindParams &P, int *grp,
+                       int *d_unbound, SortScratch &ss, UnbindScratch &U, cudaStream_t st);
+
+}  // namespace skid
+
+struct skid_ctx {
+    skid_params par{};
+    float3 L{}, hL{};
+    bool per = false;
+    cudaStream_t st = nullptr;
+    int *d_scal = nullptr;
+    unsigned *d_status = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    int n = 0, nGas = 0, nDark = 0, nStar = 0, inType = 0;
+    double time = 0.0;
+    int stage = skid::STAGE_NONE;
+    int last_error = 0;
+
+    // particles by iOrder
+    skid::DBuf<float4> pos4, vel4;
+    skid::DBuf<float> temp, rho, rho_final, ball2, raw;
+    skid::DBuf<int> grp;
+
+    // scatterers, movers, groups
+    skid::Ranges ranges{};
+    int nScatInit = 0, nExtraScat = 0;
+    skid::Tree stree;
+    skid::ScatState S;
+    int nMove = 0, nActive = 0;
+    skid::MoverState M;
+    skid::Tree mtree;               // tree over movers (FoF)
+    skid::DBuf<int> parent;         // union-find
+    skid::GroupState G;
+    skid::Tree utree;               // tree over ungrouped particles (scoop)
+    skid::UnbindScratch U;
+    skid::DBuf<int> fof_minio, fof_flag;
+    skid::DBuf<float4> moved4;      // moved positions by iOrder
+    skid::SortScratch ss;
+    skid::DBuf<float> knn_heap;     // kNN heaps when k is too large for shared memory
+
+    // outer-iteration CUDA graph
+    cudaGraphExec_t iter_graph = nullptr;
+    float g_fStep = 0.0f, g_fCvg = 0.0f;
+    bool g_nocut = false;
+    bool iter_eager_done = false;
+
+    // probes
+    skid::Tree probe_tree;
+    skid::DBuf<float> probe_f, probe_acc;
+    skid::DBuf<float4> probe_p4;
+    skid::DBuf<int> probe_i, probe_i2;
+    skid::DBuf<unsigned char> probe_t;
+
+    skid_timings tim{};
+    long long gather_launches = 0, kernel_launches = 0;
+
+    int fail(int code);
+    int fail_cuda(cudaError_t e);
+    int sync_check();
+    int read_int(const int *d, int *h);
+    void timer_start();
+    float timer_stop();
+    skid::FieldArgs field_args(float fStep, bool initial, float *acc_out);
+    float3 wrap_hi() const;
+    float3 wrap_lo() const;
+    int enqueue_step(float fStep, bool initial, bool nocut);
+
+    unsigned char *probe_touched()
+    {
+        size_t need = S.spos.n ? S.spos.n : 1;
+        if (skid::dalloc(probe_t, need)) return nullptr;
+        return probe_t.p;
+    }
+
+    void reset_pipeline()
+    {
+        if (iter_graph) { cudaGraphExecDestroy(iter_graph); iter_graph = nullptr; }
+        iter_eager_done = false;
+        stage = skid::STAGE_NONE;
+        nScatInit = nExtraScat = nMove = nActive = 0;
+        G.nGroup = 0;
+        tim = skid_timings{};
+        cudaMemsetAsync(d_scal, 0, skid::SC_COUNT * sizeof(int), st);
+    }
+
+    int alloc_particles(int np)
+    {
+        using skid::dalloc;
+        size_t m = np > 0 ? np : 1;
+        if (dalloc(pos4, m) || dalloc(vel4, m) || dalloc(temp, m) || dalloc(rho, m) ||
+            dalloc(rho_final, m) || dalloc(ball2, m) || dalloc(grp, m) || dalloc(raw, 9 * m))
+            return -1;
+        return 0;
+    }
+
+    int alloc_scatterers(int ns)
+    {
+        using skid::dalloc;
+        size_t m = ns > 0 ? ns : 1;
+        if (dalloc(S.spos, m) || dalloc(S.saux, m) || dalloc(S.spos2, m) || dalloc(S.saux2, m) ||
+            dalloc(S.srho, m) || dalloc(S.srho2, m) || dalloc(S.sidx, m) || dalloc(S.sidx2, m) ||
+            dalloc(S.touched, m) || dalloc(S.tbits, m) || dalloc(S.keep, m) || dalloc(S.kpos, m))
+            return -1;
+        // exact capacity: cut/compaction passes loop to the capacity
+        return 0;
+    }
+
+    int alloc_movers(int nm)
+    {
+        using skid::dalloc;
+        size_t m = nm > 0 ? nm : 1;
+        if (dalloc(M.mpos, m) || dalloc(M.mold, m) || dalloc(M.mio, m) || dalloc(M.act, m) ||
+            dalloc(M.act2, m) || dalloc(M.keep, m) || dalloc(M.kpos, m))
+            return -1;
+        return 0;
+    }
+
+    ~skid_ctx()
+    {
+        using skid::dfree;
+        if (iter_graph) cudaGraphExecDestroy(iter_graph);
+        dfree(pos4); dfree(vel4); dfree(temp); dfree(rho); dfree(rho_final); dfree(ball2);
+        dfree(raw); dfree(grp);
+        for (skid::Tree *t : {&stree, &mtree, &utree, &probe_tree}) {
+            dfree(t->pos); dfree(t->perm); dfree(t->lo); dfree(t->hi); dfree(t->blo);
+            dfree(t->bhi); dfree(t->flag);
+        }
+        dfree(S.spos); dfree(S.saux); dfree(S.spos2); dfree(S.saux2); dfree(S.srho);
+        dfree(S.srho2); dfree(S.sidx); dfree(S.sidx2); dfree(S.touched); dfree(S.tbits);
+        dfree(S.keep); dfree(S.kpos);
+        dfree(M.mpos); dfree(M.mold); dfree(M.mio); dfree(M.act); dfree(M.act2); dfree(M.keep);
+        dfree(M.kpos);
+        dfree(parent);
+        dfree(G.start); dfree(G.count); dfree(G.members); dfree(G.rec); dfree(G.sums);
+        dfree(G.map); dfree(G.gtmp); dfree(G.gtmp2); dfree(G.gof); dfree(G.rec2);
+        dfree(U.qr); dfree(U.qv); dfree(U.slist); dfree(U.pot); dfree(U.qid); dfree(U.scnt);
+        dfree(U.soff); dfree(U.nt); dfree(U.toff); dfree(U.cnt); dfree(U.items); dfree(U.ssoft);
+        dfree(U.usoft); dfree(fof_minio); dfree(fof_flag); dfree(moved4);
+        dfree(ss.k0); dfree(ss.k1); dfree(ss.v0); dfree(ss.v1); dfree(ss.hist); dfree(ss.blk);
+        dfree(ss.box);
+        dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);
+        dfree(probe_t); dfree(knn_heap);
+        if (d_scal) cudaFree(d_scal);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (st) cudaStreamDestroy(st);
+    }
+};

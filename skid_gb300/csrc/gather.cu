@@ -1,0 +1,286 @@
+// Gather kernels over the scatterer tree.
+//
+// density_gather: the reference scatters each pair (i, j in NN(i)) to both
+// ends (smooth1.c:248-263).  Here each particle gathers both halves itself:
+//   rho_i = sum_j 1/2 m_j W(d2(i->j), b_i) [d2 < b_i]     (its own neighbours)
+//         + sum_k 1/2 m_k W(d2(k->i), b_k) [d2 < b_k]     (balls that hold it)
+// with W the M4 spline of h^2 = b/4.  Each distance is taken in the frame the
+// reference uses for that half (the query of the ball).  Deterministic order,
+// Kahan-compensated FP32 sums.
+//
+// field_move: the move step.  The reference has every live scatterer copy
+// gather the active movers inside its ball and add m/(pi h^5) F(q)(x_c - y)
+// to them (smAccDensity/smBallGather, smooth1.c:338-508), then moves each
+// mover by fStep along -a/|a| (kdMoveParticles, kd.c:702-732).  Here each
+// mover walks the scatterer tree (ball boxes) and sums the copies whose ball
+// holds it, then moves itself in the same kernel; a copy is the scatterer's
+// periodic image nearest the mover, x_c = fl(x + sL), and must be live.  The
+// warp marks which scatterers it touched (for the density floor of the cut,
+// smooth1.c:460-461).
+#include <cfloat>
+
+#include "internal.h"
+
+namespace skid {
+
+namespace {
+
+constexpr int G_WARPS = 4;
+
+__device__ __forceinline__ float w_m4(float r2)
+{
+    float q = sqrtf(r2);
+    float rs = 2.0f - q;
+    return r2 < 1.0f ? 1.0f - 0.75f * rs * r2 : 0.25f * rs * rs * rs;
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+__device__ __forceinline__ float shifted(float x, int s, float L)
+{
+    return s == 0 ? x : (s < 0 ? fsub(x, L) : fadd(x, L));
+}
+
+__global__ void __launch_bounds__(G_WARPS * 32)
+density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL, bool per,
+               float *__restrict__ rho, int *work)
+{
+    __shared__ float4 cpos[G_WARPS][SKID_LEAF];
+    __shared__ float4 caux[G_WARPS][SKID_LEAF];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (;;) {
+        int leaf = 0;
+        if (lane == 0) leaf = atomicAdd(work, 1);
+        leaf = __shfl_sync(SKID_FULL, leaf, 0);
+        if (leaf >= t.nLeaf) break;
+        int base = leaf * SKID_LEAF;
+        int qi = base + lane;
+        bool valid = qi < t.n;
+        float4 qp = t.pos[valid ? qi : base];
+        float3 q = make_float3(qp.x, qp.y, qp.z);
+        float bi = ball2[valid ? qi : base];
+        float ih2i = 4.0f / bi;
+        float fni = 0.5f * (float)M_1_PI * sqrtf(ih2i) * ih2i;
+        float s = 0.0f, c = 0.0f;
+        int cp = 1;
+        for (;;) {
+            float4 blo = t.lo[cp], bhi = t.hi[cp];
+            float bd = box_lb(q, blo, bhi, L, per);
+            bool want = bd < fmaxf(bi, blo.w);
+            if (__any_sync(SKID_FULL, want)) {
+                if (cp < t.leafBase) { cp <<= 1; continue; }
+                int lf = cp - t.leafBase;
+                if (lf < t.nLeaf) {
+                    int cb = lf * SKID_LEAF;
+                    int cnt = min(SKID_LEAF, t.n - cb);
+                    __syncwarp();
+                    if (lane < cnt) {
+                        float b = ball2[cb + lane];
+                        float ih2 = 4.0f / b;
+                        cpos[w][lane] = t.pos[cb + lane];
+                        caux[w][lane] = make_float4(b, ih2, 0.5f * (float)M_1_PI * sqrtf(ih2) * ih2, 0.0f);
+                    }
+                    __syncwarp();
+                    int cx = img_class(q.x, blo.x, bhi.x, hL.x);
+                    int cy = img_class(q.y, blo.y, bhi.y, hL.y);
+                    int cz = img_class(q.z, blo.z, bhi.z, hL.z);
+                    bool mixed = (cx == 2) | (cy == 2) | (cz == 2);
+                    bool slow = __any_sync(SKID_FULL, mixed);
+                    bool noshift = (cx == 0) & (cy == 0) & (cz == 0);
+                    float sx = shifted(q.x, cx, L.x), sy = shifted(q.y, cy, L.y), sz = shifted(q.z, cz, L.z);
+                    for (int j = 0; j < cnt; ++j) {
+                        float4 cj = cpos[w][j];
+                        float4 aj = caux[w][j];
+                        float dik, dki;
+                        if (slow) {
+                            dik = d2of(img_dx(q.x, cj.x, L.x, hL.x), img_dx(q.y, cj.y, L.y, hL.y),
+                                       img_dx(q.z, cj.z, L.z, hL.z));
+                            dki = d2of(img_dx(cj.x, q.x, L.x, hL.x), img_dx(cj.y, q.y, L.y, hL.y),
+                                       img_dx(cj.z, q.z, L.z, hL.z));
+                        } else {
+                            dik = d2of(fsub(sx, cj.x), fsub(sy, cj.y), fsub(sz, cj.z));
+                            if (noshift) {
+                                dki = dik;
+                            } else {
+                                dki = d2of(fsub(shifted(cj.x, -cx, L.x), q.x),
+                                           fsub(shifted(cj.y, -cy, L.y), q.y),
+                                           fsub(shifted(cj.z, -cz, L.z), q.z));
+                            }
+                        }
+                        if (dik < bi) kahan_add(s, c, cj.w * fni * w_m4(dik * ih2i));
+                        if (dki < aj.x) kahan_add(s, c, cj.w * aj.z * w_m4(dki * aj.y));
+                    }
+                }
+            }
+            cp = next_node(cp);
+            if (cp == 1) break;
+        }
+        if (valid) rho[qi] = s;
+    }
+}
+
+__global__ void __launch_bounds__(G_WARPS * 32)
+field_kernel(FieldArgs a)
+{
+    __shared__ float4 cpos[G_WARPS][SKID_LEAF];
+    __shared__ float4 caux[G_WARPS][SKID_LEAF];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nA = *a.d_nA;
+    const int nS = *a.d_nS;
+    const int nLeafM = (nA + SKID_LEAF - 1) / SKID_LEAF;
+    const int nLeafS = (nS + SKID_LEAF - 1) / SKID_LEAF;
+    const bool initial = a.touched_bits != nullptr;
+    for (;;) {
+        int leaf = 0;
+        if (lane == 0) leaf = atomicAdd(a.d_work, 1);
+        leaf = __shfl_sync(SKID_FULL, leaf, 0);
+        if (leaf >= nLeafM) break;
+        int slot = leaf * SKID_LEAF + lane;
+        bool valid = slot < nA;
+        int mi = a.act[valid ? slot : leaf * SKID_LEAF];
+        float4 yp = a.mpos[mi];
+        float3 y = make_float3(yp.x, yp.y, yp.z);
+        float ax = 0.0f, ay = 0.0f, az = 0.0f;
+        int cp = 1;
+        for (;;) {
+            float4 blo = a.blo[cp], bhi = a.bhi[cp];
+            bool want = box_lb(y, blo, bhi, a.L, a.per) <= 0.0f;
+            if (__any_sync(SKID_FULL, want)) {
+                if (cp < a.leafBase) { cp <<= 1; continue; }
+                int lf = cp - a.leafBase;
+                if (lf < nLeafS) {
+                    int cb = lf * SKID_LEAF;
+                    int cnt = min(SKID_LEAF, nS - cb);
+                    __syncwarp();
+                    if (lane < cnt) {
+                        cpos[w][lane] = a.spos[cb + lane];
+                        caux[w][lane] = a.saux[cb + lane];
+                    }
+                    __syncwarp();
+                    float4 plo = a.lo[cp], phi = a.hi[cp];
+                    // class of y - c: the scatterer image nearest y is c - class*L
+                    int cx = -img_class(y.x, plo.x, phi.x, a.hL.x);
+                    int cy = -img_class(y.y, plo.y, phi.y, a.hL.y);
+                    int cz = -img_class(y.z, plo.z, phi.z, a.hL.z);
+                    bool mixed = (cx == -2) | (cy == -2) | (cz == -2);
+                    bool slow = __any_sync(SKID_FULL, mixed);
+                    bool noshift = __all_sync(SKID_FULL, (cx == 0) & (cy == 0) & (cz == 0));
+                    unsigned mytouch = 0;
+                    for (int j = 0; j < cnt; ++j) {
+                        float4 c = cpos[w][j];
+                        float4 x = caux[w][j];
+                        float dx, dy, dz;
+                        int sx = 0, sy = 0, sz = 0;
+                        if (noshift) {
+                            dx = fsub(c.x, y.x); dy = fsub(c.y, y.y); dz = fsub(c.z, y.z);
+                        } else {
+                            if (slow) {
+                                // per candidate: nearest image of the scatterer to y
+                                float d0 = fsub(c.x, y.x);
+                                sx = d0 > a.hL.x ? -1 : (d0 < -a.hL.x ? 1 : 0);
+                                d0 = fsub(c.y, y.y);
+                                sy = d0 > a.hL.y ? -1 : (d0 < -a.hL.y ? 1 : 0);
+                                d0 = fsub(c.z, y.z);
+                                sz = d0 > a.hL.z ? -1 : (d0 < -a.hL.z ? 1 : 0);
+                            } else {
+                                sx = cx; sy = cy; sz = cz;
+                            }
+                            dx = fsub(shifted(c.x, sx, a.L.x), y.x);
+                            dy = fsub(shifted(c.y, sy, a.L.y), y.y);
+                            dz = fsub(shifted(c.z, sz, a.L.z), y.z);
+                        }
+                        float d2 = d2of(dx, dy, dz);
+                        unsigned bit = 0;
+                        if (valid && d2 < x.x) {
+                            unsigned img = (unsigned)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
+                            if ((__float_as_uint(x.w) >> img) & 1u) {
+                                bit = 1u << img;
+                                float r2 = fmul(d2, x.y);
+                                float rs = sqrtf(r2);
+                                float F = r2 < 1.0f ? __fmaf_rn(2.25f, rs, -3.0f)
+                                                    : (-3.0f / rs + 3.0f - 0.75f * rs);
+                                F = fmul(F, x.z);
+                                ax = fadd(ax, fmul(dx, F));
+                                ay = fadd(ay, fmul(dy, F));
+                                az = fadd(az, fmul(dz, F));
+                            }
+                        }
+                        unsigned hb = __reduce_or_sync(SKID_FULL, bit);
+                        if (lane == j) mytouch = hb;
+                    }
+                    if (mytouch) {
+                        if (initial) atomicOr(&a.touched_bits[cb + lane], mytouch);
+                        else a.touched[cb + lane] = 1;
+                    }
+                }
+            }
+            cp = next_node(cp);
+            if (cp == 1) break;
+        }
+        if (!valid) continue;
+        if (a.acc_out) {
+            a.acc_out[3 * (size_t)slot + 0] = ax;
+            a.acc_out[3 * (size_t)slot + 1] = ay;
+            a.acc_out[3 * (size_t)slot + 2] = az;
+        }
+        if (a.fStep > 0.0f) {
+            // kdMoveParticles (kd.c:711-728)
+            float s = d2of(ax, ay, az);
+            float ai = sqrtf(s);
+            ai = ai > 0.0f ? __fdiv_rn(a.fStep, ai) : 0.0f;
+            y.x = fsub(y.x, fmul(ai, ax));
+            y.y = fsub(y.y, fmul(ai, ay));
+            y.z = fsub(y.z, fmul(ai, az));
+            if (y.x > a.wrapHi.x) y.x = fsub(y.x, a.period.x);
+            if (y.x <= a.wrapLo.x) y.x = fadd(y.x, a.period.x);
+            if (y.y > a.wrapHi.y) y.y = fsub(y.y, a.period.y);
+            if (y.y <= a.wrapLo.y) y.y = fadd(y.y, a.period.y);
+            if (y.z > a.wrapHi.z) y.z = fsub(y.z, a.period.z);
+            if (y.z <= a.wrapLo.z) y.z = fadd(y.z, a.period.z);
+            a.mpos[mi] = make_float4(y.x, y.y, y.z, yp.w);
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t density_gather(const Tree &t, const float *ball2_sorted, float3 L, bool per,
+                           float *rho_sorted, int *d_work, cudaStream_t st)
+{
+    if (t.n <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_work, 0, sizeof(int), st);
+    if (e) return e;
+    int perSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, density_kernel, G_WARPS * 32, 0);
+    if (perSM < 1) perSM = 1;
+    int blocks = num_sms() * perSM;
+    int need = (t.nLeaf + G_WARPS - 1) / G_WARPS;
+    if (blocks > need) blocks = need;
+    float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
+    density_kernel<<<blocks, G_WARPS * 32, 0, st>>>(t.view(), ball2_sorted, L, hL, per, rho_sorted,
+                                                    d_work);
+    return cudaGetLastError();
+}
+
+cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st)
+{
+    if (max_movers <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(a.d_work, 0, sizeof(int), st);
+    if (e) return e;
+    int perSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, field_kernel, G_WARPS * 32, 0);
+    if (perSM < 1) perSM = 1;
+    int blocks = num_sms() * perSM;
+    int need = ((max_movers + SKID_LEAF - 1) / SKID_LEAF + G_WARPS - 1) / G_WARPS;
+    if (blocks > need) blocks = need;
+    field_kernel<<<blocks, G_WARPS * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace skid

@@ -1,0 +1,177 @@
+// k-nearest-neighbour ball radii (fBall2) of every point of a tree, among the
+// tree's own points, self included (smDensityInit/smBallSearch,
+// smooth1.c:41-243).  Only the k-th smallest squared distance is kept: the
+// density gather needs fBall2 alone, and that value does not depend on how
+// equal distances are ordered.
+//
+// One warp per leaf of 32 query points, one query per lane.  Each lane keeps
+// a max-heap of its k best squared distances in shared memory (slot i of
+// lane l at i*32+l, so every heap access is bank-conflict free).  The warp
+// first scans its own leaf, then climbs to the root visiting each sibling
+// subtree depth-first (the search order of smBallSearch, smooth1.c:89-127),
+// entering a node when any lane's heap bound reaches its box.
+#include <cfloat>
+
+#include "internal.h"
+
+namespace skid {
+
+namespace {
+
+constexpr int KNN_WARPS = 4;
+
+struct KnnLane {
+    float3 q;       // query
+    float thr;      // current k-th smallest (heap top)
+    float *heap;    // this lane's heap base (stride 32)
+};
+
+__device__ __forceinline__ void heap_replace_top(float *heap, int k, float d)
+{
+    int i = 0;
+    for (;;) {
+        int c = 2 * i + 1;
+        if (c >= k) break;
+        float vc = heap[c * 32];
+        if (c + 1 < k) {
+            float vr = heap[(c + 1) * 32];
+            if (vr > vc) { vc = vr; ++c; }
+        }
+        if (vc <= d) break;
+        heap[i * 32] = vc;
+        i = c;
+    }
+    heap[i * 32] = d;
+}
+
+// Process one leaf: candidates staged in shared memory, every lane tests all.
+__device__ __forceinline__ void knn_leaf(const TreeView &t, int node, float4 blo, float4 bhi,
+                                         KnnLane &ln, int k, float3 L, float3 hL, float4 *cand,
+                                         int lane)
+{
+    int leaf = node - t.leafBase;
+    if (leaf >= t.nLeaf) return;
+    int base = leaf * SKID_LEAF;
+    int cnt = min(SKID_LEAF, t.n - base);
+    __syncwarp();
+    if (lane < cnt) cand[lane] = t.pos[base + lane];
+    __syncwarp();
+    int cx = img_class(ln.q.x, blo.x, bhi.x, hL.x);
+    int cy = img_class(ln.q.y, blo.y, bhi.y, hL.y);
+    int cz = img_class(ln.q.z, blo.z, bhi.z, hL.z);
+    bool mixed = (cx == 2) | (cy == 2) | (cz == 2);
+    if (__any_sync(SKID_FULL, mixed)) {
+        for (int j = 0; j < cnt; ++j) {
+            float4 c = cand[j];
+            float dx = img_dx(ln.q.x, c.x, L.x, hL.x);
+            float dy = img_dx(ln.q.y, c.y, L.y, hL.y);
+            float dz = img_dx(ln.q.z, c.z, L.z, hL.z);
+            float d2 = d2of(dx, dy, dz);
+            if (d2 < ln.thr) {
+                heap_replace_top(ln.heap, k, d2);
+                ln.thr = ln.heap[0];
+            }
+        }
+        return;
+    }
+    float sx = cx == 0 ? ln.q.x : (cx < 0 ? fsub(ln.q.x, L.x) : fadd(ln.q.x, L.x));
+    float sy = cy == 0 ? ln.q.y : (cy < 0 ? fsub(ln.q.y, L.y) : fadd(ln.q.y, L.y));
+    float sz = cz == 0 ? ln.q.z : (cz < 0 ? fsub(ln.q.z, L.z) : fadd(ln.q.z, L.z));
+#pragma unroll 4
+    for (int j = 0; j < cnt; ++j) {
+        float4 c = cand[j];
+        float d2 = d2of(fsub(sx, c.x), fsub(sy, c.y), fsub(sz, c.z));
+        if (d2 < ln.thr) {
+            heap_replace_top(ln.heap, k, d2);
+            ln.thr = ln.heap[0];
+        }
+    }
+}
+
+// Heaps live in shared memory after the candidate buffers, or -- for k too
+// large for one warp's heaps to fit -- in global scratch (gheap, one slab per
+// resident warp).
+__global__ void __launch_bounds__(KNN_WARPS * 32)
+knn_kernel(TreeView t, int k, float3 L, float3 hL, bool per, float *__restrict__ ball2,
+           int *work, float *gheap)
+{
+    extern __shared__ float4 smem4[];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int nw = blockDim.x >> 5;
+    float4 *cand = smem4 + w * SKID_LEAF;
+    float *heaps = gheap ? gheap + (size_t)blockIdx.x * nw * k * 32
+                         : reinterpret_cast<float *>(smem4 + nw * SKID_LEAF);
+    KnnLane ln;
+    ln.heap = heaps + (size_t)w * k * 32 + lane;
+    for (;;) {
+        int leaf = 0;
+        if (lane == 0) leaf = atomicAdd(work, 1);
+        leaf = __shfl_sync(SKID_FULL, leaf, 0);
+        if (leaf >= t.nLeaf) break;
+        int base = leaf * SKID_LEAF;
+        int qi = base + lane;
+        bool valid = qi < t.n;
+        float4 qp = t.pos[valid ? qi : base];
+        ln.q = make_float3(qp.x, qp.y, qp.z);
+        for (int i = 0; i < k; ++i) ln.heap[i * 32] = FLT_MAX;
+        ln.thr = FLT_MAX;
+        int own = t.leafBase + leaf;
+        knn_leaf(t, own, t.lo[own], t.hi[own], ln, k, L, hL, cand, lane);
+        int cell = own;
+        while (cell > 1) {
+            int cp = cell ^ 1;
+            int end = next_node(cp);
+            for (;;) {
+                float4 blo = t.lo[cp], bhi = t.hi[cp];
+                float bd = box_lb(ln.q, blo, bhi, L, per);
+                bool want = bd < ln.thr;
+                if (__any_sync(SKID_FULL, want)) {
+                    if (cp < t.leafBase) { cp <<= 1; continue; }
+                    knn_leaf(t, cp, blo, bhi, ln, k, L, hL, cand, lane);
+                }
+                cp = next_node(cp);
+                if (cp == end) break;
+            }
+            cell >>= 1;
+        }
+        if (valid) ball2[qi] = ln.thr;
+    }
+}
+
+}  // namespace
+
+cudaError_t knn_ball2(const Tree &t, int k, float3 L, bool per, float *ball2_sorted, int *d_work,
+                      DBuf<float> &gheap, cudaStream_t st)
+{
+    if (t.n <= 0) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t heapBytes = (size_t)k * 32 * sizeof(float);
+    size_t candBytes = SKID_LEAF * sizeof(float4);
+    int nw = KNN_WARPS;
+    while (nw > 1 && (size_t)nw * (candBytes + heapBytes) > (size_t)optin) nw >>= 1;
+    bool global = (size_t)nw * (candBytes + heapBytes) > (size_t)optin;
+    size_t smem = (size_t)nw * candBytes + (global ? 0 : (size_t)nw * heapBytes);
+    cudaError_t e = cudaFuncSetAttribute(knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e) return e;
+    int perSM = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, knn_kernel, nw * 32, smem);
+    if (e) return e;
+    if (perSM < 1) return cudaErrorInvalidConfiguration;
+    int blocks = num_sms() * perSM;
+    int need = (t.nLeaf + nw - 1) / nw;
+    if (blocks > need) blocks = need;
+    float *gh = nullptr;
+    if (global) {
+        if ((e = dalloc(gheap, (size_t)blocks * nw * k * 32))) return e;
+        gh = gheap.p;
+    }
+    float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
+    if ((e = cudaMemsetAsync(d_work, 0, sizeof(int), st))) return e;
+    knn_kernel<<<blocks, nw * 32, smem, st>>>(t.view(), k, L, hL, per, ball2_sorted, d_work, gh);
+    return cudaGetLastError();
+}
+
+}  // namespace skid

@@ -1,0 +1,295 @@
+"""ctypes binding of libskidgpu (include/skid_gpu.h).
+
+There is no CPU fallback: if the library is missing or cannot load, every
+call raises.  Arrays are numpy, indexed by iOrder.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .options import FLT_MAX
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libskidgpu.so")
+
+SKID_ERRORS = {
+    -1: "invalid argument", -2: "out of memory", -3: "CUDA runtime error",
+    -4: "bounded device wait ran out", -5: "internal capacity exceeded",
+    -6: "no usable sm_103 device", -7: "call made in the wrong pipeline state",
+}
+
+
+class SkidError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        super().__init__(f"{where}: {SKID_ERRORS.get(code, 'error')} ({code})")
+
+
+class Params(C.Structure):
+    _fields_ = [("period", C.c_float * 3), ("center", C.c_float * 3), ("periodic", C.c_int),
+                ("nSmooth", C.c_int), ("device", C.c_int)]
+
+
+class Group(C.Structure):
+    _fields_ = [("nMembers", C.c_int), ("fMass", C.c_float), ("rel", C.c_float * 3),
+                ("rCenter", C.c_float * 3), ("rBound", C.c_float * 3), ("vcm", C.c_float * 3),
+                ("fRadius", C.c_float)]
+
+
+class Timings(C.Structure):
+    _fields_ = [("density_ms", C.c_float), ("moving_ms", C.c_float), ("fof_ms", C.c_float),
+                ("micro_ms", C.c_float), ("groups_ms", C.c_float), ("unbind_ms", C.c_float),
+                ("toosmall_ms", C.c_float), ("gather_launches", C.c_longlong),
+                ("kernel_launches", C.c_longlong)]
+
+
+GROUP_DTYPE = np.dtype([("nMembers", "<i4"), ("fMass", "<f4"), ("rel", "<f4", 3),
+                        ("rCenter", "<f4", 3), ("rBound", "<f4", 3), ("vcm", "<f4", 3),
+                        ("fRadius", "<f4")])
+assert GROUP_DTYPE.itemsize == C.sizeof(Group)
+
+_I = C.POINTER(C.c_int)
+_F = C.POINTER(C.c_float)
+_D = C.POINTER(C.c_double)
+_V = C.c_void_p
+
+# entry point -> argtypes (all return int status)
+SIGNATURES = {
+    "skid_create": [C.POINTER(C.c_void_p), C.POINTER(Params)],
+    "skid_destroy": [_V],
+    "skid_last_error": [_V],
+    "skid_set_particles": [_V, C.c_int, C.c_int, C.c_int, C.c_double, _F, _F, _F, _F, _F],
+    "skid_scatter_active": [_V, C.c_int, C.c_int, _I],
+    "skid_density": [_V, _I],
+    "skid_get_density": [_V, _F, _F],
+    "skid_init_move": [_V, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, _I],
+    "skid_move_step": [_V, C.c_float, C.c_int, C.c_int, _I],
+    "skid_prune_inactive": [_V, C.c_float, _I],
+    "skid_move_iterate": [_V, C.c_float, C.c_float, C.c_int, _I, _I],
+    "skid_reactivate_move": [_V],
+    "skid_fof": [_V, C.c_float, _I],
+    "skid_group_centers": [_V],
+    "skid_set_groups": [_V, _I, C.c_int, C.c_void_p],
+    "skid_set_soft": [_V, C.c_float],
+    "skid_unbind": [_V, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                    C.c_float, C.c_float, _I],
+    "skid_too_small": [_V, C.c_int, _I],
+    "skid_get_groups": [_V, _I, C.c_void_p],
+    "skid_get_moved": [_V, _F],
+    "skid_get_final_density": [_V, _F],
+    "skid_get_timings": [_V, C.POINTER(Timings)],
+    "skid_knn_ball2": [_V, C.c_int, _F, C.c_int, _F],
+    "skid_field": [_V, C.c_int, _F, _F],
+    "skid_fof_points": [_V, C.c_int, _F, C.c_float, _I, _I],
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libskidgpu; raises if it is missing (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"libskidgpu not built ({path}); run skid_gb300.build")
+        lib = C.CDLL(path)
+        for name, args in SIGNATURES.items():
+            f = getattr(lib, name, None)
+            if f is None:
+                continue
+            f.argtypes = args
+            f.restype = C.c_int
+        lib.skid_strerror.argtypes = [C.c_int]
+        lib.skid_strerror.restype = C.c_char_p
+        _lib = lib
+    return _lib
+
+
+def exported_symbols(path: str = LIB_PATH):
+    lib = C.CDLL(path)
+    return {name for name in list(SIGNATURES) + ["skid_strerror"] if hasattr(lib, name)}
+
+
+def _f(a):
+    return a.ctypes.data_as(_F) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_I) if a is not None else None
+
+
+def _c32(a, shape=None):
+    a = np.ascontiguousarray(a, np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Context:
+    """One libskidgpu context (one GPU stream).  Methods mirror the C ABI."""
+
+    def __init__(self, period=None, center=(0.0, 0.0, 0.0), periodic=None, nSmooth=64, device=0):
+        self.lib = load()
+        p = Params()
+        per = [FLT_MAX] * 3 if period is None else (list(period) if np.ndim(period) else [float(period)] * 3)
+        for d in range(3):
+            p.period[d] = per[d]
+            p.center[d] = center[d]
+        p.periodic = int(period is not None) if periodic is None else int(periodic)
+        p.nSmooth = int(nSmooth)
+        p.device = int(device)
+        self.params = p
+        h = C.c_void_p()
+        self._call("skid_create", C.byref(h), C.byref(p))
+        self.h = h
+        self.n = 0
+
+    def _call(self, name, *args):
+        rc = getattr(self.lib, name)(*args)
+        if rc != 0:
+            raise SkidError(rc, name)
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.skid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- pipeline ----
+    def set_particles(self, snap):
+        self.n = snap.n
+        self._pos = _c32(snap.pos, (-1, 3))
+        self._vel = _c32(snap.vel, (-1, 3))
+        self._mass = _c32(snap.mass)
+        self._soft = _c32(snap.soft)
+        self._temp = _c32(snap.temp)
+        self._call("skid_set_particles", self.h, snap.n_gas, snap.n_dark, snap.n_star,
+                   float(snap.time), _f(self._pos), _f(self._vel), _f(self._mass), _f(self._soft),
+                   _f(self._temp))
+
+    def scatter_active(self, bGasAndDark=False, bGasOnly=False) -> int:
+        n = C.c_int()
+        self._call("skid_scatter_active", self.h, int(bGasAndDark), int(bGasOnly), C.byref(n))
+        return n.value
+
+    def density(self) -> int:
+        n = C.c_int()
+        self._call("skid_density", self.h, C.byref(n))
+        return n.value
+
+    def get_density(self):
+        rho = np.empty(self.n, np.float32)
+        b = np.empty(self.n, np.float32)
+        self._call("skid_get_density", self.h, _f(rho), _f(b))
+        return rho, b
+
+    def get_final_density(self):
+        rho = np.empty(self.n, np.float32)
+        self._call("skid_get_final_density", self.h, _f(rho))
+        return rho
+
+    def init_move(self, fDensMin=0.0, fTempMax=FLT_MAX, fMassMax=FLT_MAX, bGasAndDark=False,
+                  bGasOnly=False) -> int:
+        n = C.c_int()
+        self._call("skid_init_move", self.h, fDensMin, fTempMax, fMassMax, int(bGasAndDark),
+                   int(bGasOnly), C.byref(n))
+        return n.value
+
+    def move_step(self, fStep, bInitial=False, bNoCut=False) -> int:
+        n = C.c_int()
+        self._call("skid_move_step", self.h, fStep, int(bInitial), int(bNoCut), C.byref(n))
+        return n.value
+
+    def prune_inactive(self, fCvg) -> int:
+        n = C.c_int()
+        self._call("skid_prune_inactive", self.h, fCvg, C.byref(n))
+        return n.value
+
+    def move_iterate(self, fStep, fCvg, bNoCut=False):
+        a, s = C.c_int(), C.c_int()
+        self._call("skid_move_iterate", self.h, fStep, fCvg, int(bNoCut), C.byref(a), C.byref(s))
+        return a.value, s.value
+
+    def reactivate_move(self):
+        self._call("skid_reactivate_move", self.h)
+
+    def fof(self, fTau) -> int:
+        n = C.c_int()
+        self._call("skid_fof", self.h, fTau, C.byref(n))
+        return n.value
+
+    def group_centers(self):
+        self._call("skid_group_centers", self.h)
+
+    def set_groups(self, grp, centers=None):
+        grp = np.ascontiguousarray(grp, np.int32)
+        ng = int(grp.max(initial=0)) + 1
+        cptr = None
+        if centers is not None:
+            centers = np.ascontiguousarray(centers, GROUP_DTYPE)
+            cptr = centers.ctypes.data_as(C.c_void_p)
+        self._call("skid_set_groups", self.h, _i(grp), ng, cptr)
+
+    def set_soft(self, fEps):
+        self._call("skid_set_soft", self.h, fEps)
+
+    def unbind(self, iSoftType, fScoop, bGasAndDark, bNoUnbind, nMaxMembers, G, z, a, aH) -> int:
+        n = C.c_int()
+        self._call("skid_unbind", self.h, int(iSoftType), fScoop, int(bGasAndDark), int(bNoUnbind),
+                   int(min(nMaxMembers, 2**31 - 1)), G, z, a, aH, C.byref(n))
+        return n.value
+
+    def too_small(self, nMembers) -> int:
+        n = C.c_int()
+        self._call("skid_too_small", self.h, int(nMembers), C.byref(n))
+        return n.value
+
+    def get_groups(self, ngroups: int):
+        grp = np.empty(self.n, np.int32)
+        rec = np.zeros(ngroups + 1, GROUP_DTYPE)
+        self._call("skid_get_groups", self.h, _i(grp), rec.ctypes.data_as(C.c_void_p))
+        return grp, rec
+
+    def get_moved(self):
+        out = np.empty((self.n, 3), np.float32)
+        self._call("skid_get_moved", self.h, _f(out))
+        return out
+
+    def timings(self) -> dict:
+        t = Timings()
+        self._call("skid_get_timings", self.h, C.byref(t))
+        return {k: getattr(t, k) for k, _ in Timings._fields_}
+
+    # ---- stage probes ----
+    def knn_ball2(self, pos, k):
+        pos = _c32(pos, (-1, 3))
+        out = np.empty(len(pos), np.float32)
+        self._call("skid_knn_ball2", self.h, len(pos), _f(pos), int(k), _f(out))
+        return out
+
+    def field(self, mpos):
+        mpos = _c32(mpos, (-1, 3))
+        acc = np.empty((len(mpos), 3), np.float32)
+        self._call("skid_field", self.h, len(mpos), _f(mpos), _f(acc))
+        return acc
+
+    def fof_points(self, pos, tau):
+        pos = _c32(pos, (-1, 3))
+        grp = np.empty(len(pos), np.int32)
+        ng = C.c_int()
+        self._call("skid_fof_points", self.h, len(pos), _f(pos), tau, _i(grp), C.byref(ng))
+        return grp, ng.value

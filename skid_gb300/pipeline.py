@@ -1,0 +1,284 @@
+"""The skid pipeline (main.c:347-495) driven through libskidgpu.
+
+``run(snapshot, options)`` makes the reference's calls in the reference's
+order and returns the catalogue and the per-particle outputs; ``write_outputs``
+writes the .grp/.gtp/.den/.ray/.stat files like kd.c:1502-1839.  Progress
+lines match the reference's stdout (main.c:402,416,436; kd.c:158,1326,1461,
+1509; smooth1.c:304).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import gpu, tipsy
+from .options import FLT_MAX, Options
+
+PRUNE_STEPS = 5      # main.c:13
+MICRO_STEP = 0.1     # main.c:14
+DARK, GAS, STAR = 1, 2, 4
+
+
+@dataclasses.dataclass
+class Result:
+    grp: np.ndarray              # final group id by iOrder
+    groups: np.ndarray           # gpu.GROUP_DTYPE records, index 0 = ungrouped
+    n_group: int
+    rho: np.ndarray | None       # initial densities (for .den)
+    rho_final: np.ndarray | None # densities after the first-step cut (for .stat)
+    moved: np.ndarray | None     # moved positions (for .ray)
+    counts: dict
+    timings: dict
+    lines: list
+
+
+def _f32(x) -> float:
+    return float(np.float32(x))
+
+
+def run(snap: tipsy.Snapshot, opts: Options, ctx: gpu.Context | None = None, log=None,
+        want_density: bool | None = None, want_moved: bool | None = None) -> Result:
+    lines = []
+
+    def say(s):
+        lines.append(s)
+        if log:
+            log(s)
+
+    own = ctx is None
+    if own:
+        ctx = gpu.Context(period=opts.period if opts.periodic else None, center=opts.center,
+                          periodic=opts.periodic, nSmooth=opts.nSmooth)
+    t0 = time.perf_counter()
+    try:
+        say(f"nDark:{snap.n_dark} nGas:{snap.n_gas} nStar:{snap.n_star}")
+        ctx.set_particles(snap)
+        in_type = (DARK if snap.n_dark else 0) | (GAS if snap.n_gas else 0) | (STAR if snap.n_star else 0)
+        counts = {}
+        rho = moved = None
+        want_density = opts.bOutDens if want_density is None else want_density
+        want_moved = opts.bOutRay if want_moved is None else want_moved
+        if opts.bUnbindOnly:
+            grp_in, centers = read_unbind_inputs(opts, snap)
+            ctx.set_groups(grp_in, centers)
+            n_fof = int(grp_in.max(initial=0))
+        else:
+            ctx.scatter_active(opts.bGasAndDark, opts.bGasOnly)
+            nextra = ctx.density()
+            if opts.periodic:
+                say(f"nExtraScat:{nextra}")
+            if want_density:
+                rho, _ = ctx.get_density()
+            n_active = ctx.init_move(opts.fDensMin, opts.fTempMax, opts.fMassMax,
+                                     opts.bGasAndDark, opts.bGasOnly)
+            counts["nMove"] = n_active
+            initial = in_type == DARK or opts.bForceInitialCut
+            nscat = ctx.move_step(opts.fStep, initial, opts.bNoScatterCut)
+            say(f"Ittr:0 nActive:{n_active} nScatter:{nscat}")
+            it = 1
+            while n_active:
+                if opts.maxIter and it > opts.maxIter:
+                    break
+                n_active, nscat = ctx.move_iterate(opts.fStep, opts.fCvg, opts.bNoScatterCut)
+                say(f"Ittr:{it} nActive:{n_active} nScatter:{nscat}")
+                it += 1
+            counts["nIter"] = it - 1
+            n_fof = ctx.fof(opts.fTau)
+            ctx.reactivate_move()
+            micro = _f32(MICRO_STEP * opts.fStep)
+            for i in range(PRUNE_STEPS):
+                nscat = ctx.move_step(micro, False, opts.bNoScatterCut)
+                say(f"Microstep:{i + 1} nScatter:{nscat}")
+            counts["nScatFinal"] = nscat
+            if want_moved:
+                moved = ctx.get_moved()
+            ctx.group_centers()
+        if opts.bEps:
+            ctx.set_soft(opts.fEps)
+        say(f"Groups before Unbind:{n_fof}")
+        counts["nGroupFoF"] = n_fof
+        nu = ctx.unbind(opts.iSoftType, opts.fScoop, opts.bGasAndDark, opts.bNoUnbind,
+                        opts.nMaxMembers, opts.G, opts.z, opts.a_shift, opts.a_hubble)
+        say(f"Number of particles Unbound:{nu}")
+        counts["nUnbound"] = nu
+        ng = ctx.too_small(opts.nMembers)
+        counts["nGroup"] = ng
+        grp, rec = ctx.get_groups(ng)
+        say(f"Number of Groups:{ng}")
+        rho_final = ctx.get_final_density() if (opts.bOutStats and not opts.bUnbindOnly) else None
+        tm = ctx.timings()
+        tm["wall_s"] = time.perf_counter() - t0
+        return Result(grp, rec, ng, rho, rho_final, moved, counts, tm, lines)
+    finally:
+        if own:
+            ctx.close()
+
+
+def read_unbind_inputs(opts: Options, snap: tipsy.Snapshot):
+    """kdInGroup (kd.c:920-962) and kdReadCenter (kd.c:1083-1196) inputs."""
+    name = opts.achGroup
+    if name.endswith(".grp"):
+        name = name[:-4]
+    grp = tipsy.read_grp(name + ".grp")
+    if len(grp) != snap.n:
+        raise ValueError(f"ERROR: Mismatched number of particles: {len(grp)} in {name}.grp, "
+                         f"{snap.n} in the TIPSY input")
+    ng = int(grp.max(initial=0)) + 1
+    centers = None
+    gtp = name + ".gtp"
+    if os.path.exists(gtp):
+        star = tipsy.read_gtp(gtp, standard=opts.bStandard)
+        if len(star) != ng - 1:
+            raise ValueError(f"ERROR: grp and gtp files don't match: {len(star)} vs. {ng - 1}.")
+        centers = np.zeros(ng, gpu.GROUP_DTYPE)
+        centers["rCenter"][1:] = star["pos"]
+        centers["vcm"][1:] = star["vel"]
+    return grp, centers
+
+
+# ---------------------------------------------------------------------------
+# output files
+
+def _g(x) -> str:
+    """printf %g."""
+    return "%g" % x
+
+
+def write_outputs(res: Result, snap: tipsy.Snapshot, opts: Options, outdir: str = ".") -> list:
+    base = os.path.join(outdir, opts.achName)
+    written = []
+    tipsy.write_grp(base + ".grp", res.grp)
+    written.append(base + ".grp")
+    star = np.zeros(res.n_group, tipsy.STAR_DT)
+    g = res.groups[1:res.n_group + 1]
+    star["mass"] = g["fMass"]
+    star["pos"] = g["rCenter"]
+    star["vel"] = g["vcm"]
+    star["eps"] = g["fRadius"]
+    star["tform"] = np.float32(snap.time)
+    tipsy.write_tipsy(base + ".gtp", snap.time, star=star, standard=opts.bStandard)
+    written.append(base + ".gtp")
+    if opts.bOutDens and res.rho is not None:
+        with open(base + ".den", "w") as f:
+            f.write(f"{snap.n}\n")
+            f.write("".join("%.10g\n" % float(r) for r in res.rho))
+        written.append(base + ".den")
+    if opts.bOutRay and res.moved is not None:
+        write_ray(base + ".ray", res.moved, snap, opts)
+        written.append(base + ".ray")
+    if opts.bOutStats:
+        write_stats(base + ".stat", res, snap, opts)
+        written.append(base + ".stat")
+    return written
+
+
+def write_ray(path, moved, snap, opts):
+    """kdOutVector (kd.c:1550-1608): displacement moved - initial, wrapped."""
+    with open(path, "w") as f:
+        f.write(f"{snap.n}\n")
+        for d in range(3):
+            h = np.float32(0.5 * opts.period[d])
+            dx = (moved[:, d] - snap.pos[:, d]).astype(np.float32)
+            dx = np.where(dx > h, dx - np.float32(2) * h, dx).astype(np.float32)
+            dx = np.where(dx <= -h, dx + np.float32(2) * h, dx).astype(np.float32)
+            f.write("".join(_g(float(x)) + "\n" for x in dx))
+
+
+def group_stats(res: Result, snap: tipsy.Snapshot, opts: Options):
+    """kdOutStats (kd.c:1703-1839): 21 columns per group."""
+    G = np.float32(opts.G)
+    fexp = np.float32(opts.a_shift)
+    fexphub = np.float32(opts.a_hubble)
+    h = [np.float32(0.5 * opts.period[d]) for d in range(3)]
+    rho = res.rho_final if res.rho_final is not None else np.zeros(snap.n, np.float32)
+    order = np.argsort(res.grp, kind="stable")
+    bounds = np.searchsorted(res.grp[order], np.arange(res.n_group + 2))
+    n_gas, n_dark = snap.n_gas, snap.n_dark
+    rows = []
+    for g in range(1, res.n_group + 1):
+        idx = order[bounds[g]:bounds[g + 1]]
+        n = len(idx)
+        rec = res.groups[g]
+        q = np.empty((n, 3), np.float32)
+        for d in range(3):
+            dx = (snap.pos[idx, d] - rec["rCenter"][d]).astype(np.float32)
+            dx = np.where(dx > h[d], dx - np.float32(2) * h[d], dx).astype(np.float32)
+            dx = np.where(dx <= -h[d], dx + np.float32(2) * h[d], dx).astype(np.float32)
+            q[:, d] = dx
+        r2 = ((q[:, 0] * q[:, 0] + q[:, 1] * q[:, 1]).astype(np.float32) + q[:, 2] * q[:, 2]).astype(np.float32)
+        srt = np.argsort(r2, kind="stable")
+        idx, q, r2 = idx[srt], q[srt], r2[srt]
+        m = snap.mass[idx]
+        half = np.float32(0.0)
+        for mj in m:
+            half = np.float32(half + np.float32(0.5) * mj)
+        tot = gasm = starm = vc = mvc = vdisp = np.float32(0.0)
+        rvmax = rhm = np.float32(0.0)
+        for j in range(n):
+            tot = np.float32(tot + m[j])
+            soft = snap.soft[idx[j]]
+            if r2[j] > np.float32(4.0) * soft * soft and G * tot / np.float32(math.sqrt(r2[j])) > vc:
+                rvmax = np.float32(math.sqrt(r2[j]))
+                vc = np.float32(G * tot / rvmax)
+            io = idx[j]
+            t = GAS if io < n_gas else (DARK if io < n_gas + n_dark else STAR)
+            if t == GAS and rho[io] >= opts.fDensMin and snap.temp[io] <= opts.fTempMax:
+                gasm = np.float32(gasm + m[j])
+            if t == STAR:
+                starm = np.float32(starm + m[j])
+            if tot > half and mvc == 0.0:
+                rhm = np.float32(math.sqrt(r2[j]))
+                mvc = np.float32(G * tot / rhm)
+            for d in range(3):
+                dv = np.float32(fexp * (snap.vel[io, d] - rec["vcm"][d]) + fexphub * q[j, d])
+                vdisp = np.float32(vdisp + dv * dv)
+        rout = np.float32(math.sqrt(r2[n - 1]))
+        lvc = np.float32(G * tot / rout)
+        if vc == 0.0:
+            vc = lvc
+            rvmax = rout
+        vdisp = np.float32(math.sqrt(vdisp / (3.0 * n)))
+        rows.append((g, n, tot, gasm, starm, math.sqrt(vc), math.sqrt(mvc), math.sqrt(lvc), rvmax,
+                     rhm, rout, vdisp, *rec["rCenter"], *rec["vcm"], *rec["rBound"]))
+    return rows
+
+
+def write_stats(path, res, snap, opts):
+    rows = group_stats(res, snap, opts)
+    with open(path, "w") as f:
+        for r in rows:
+            f.write(f"{r[0]} {r[1]} " + " ".join(_g(float(x)) for x in r[2:]) + "\n")
+
+
+def main(argv=None) -> int:
+    """`python -m skid_gb300.pipeline <skid flags> < input` (reads stdin like skid)."""
+    argv = sys.argv[1:] if argv is None else argv
+    try:
+        opts = Options.parse(argv)
+    except Exception as e:
+        print(f"USAGE: skid -tau <fLinkLength> [OPTIONAL ARGUMENTS] ({e})", file=sys.stderr)
+        return 1
+    print("SKID v1.4.1 (GB300)")
+    data = sys.stdin.buffer.read()
+    snap = tipsy.read_tipsy(data, standard=opts.bStandard)
+    res = run(snap, opts, log=lambda s: print(s, flush=True))
+    write_outputs(res, snap, opts)
+    t = res.timings
+    print("SKID GPU Time (device ms):")
+    if not opts.bUnbindOnly:
+        print(f"   Initial Density:    {t['density_ms']:.3f}")
+        print(f"   Moving Particles:   {t['moving_ms']:.3f}")
+        print(f"   Friends of Friends: {t['fof_ms']:.3f}")
+        print(f"   Microstepping:      {t['micro_ms']:.3f}")
+    if not opts.bNoUnbind:
+        print(f"   Unbinding:          {t['unbind_ms']:.3f}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

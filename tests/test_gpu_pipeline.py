@@ -1,0 +1,47 @@
+"""The whole group-finding pipeline on the GPU against the reference's
+golden outputs and the oracle: >= 99.9 % per-particle agreement after
+membership matching, the same groups above -m, matched .gtp records, the
+reference's progress counts."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_pipeline_vs_reference(gpu_ready, name):
+    from skid_gb300 import pipeline
+    snap, opts, ref, counts, meta = gc.load(name)
+    res = pipeline.run(snap, opts, want_density=True)
+    gc.check_catalogue(res.grp, res.groups, ref, opts)
+    if "nExtraScat" in counts:
+        assert f"nExtraScat:{counts['nExtraScat']}" in res.lines
+    assert res.counts["nGroupFoF"] == counts["nGroupFoF"]
+    assert res.counts["nGroup"] == counts["nGroup"]
+    assert abs(res.counts["nUnbound"] - counts["nUnbound"]) <= max(2, 0.001 * snap.n)
+    if "den" in ref:
+        rel = np.abs(res.rho - ref["den"]) / np.maximum(ref["den"], 1e-30)
+        assert rel[ref["den"] > 0].max() < 1e-5
+
+
+@pytest.mark.parametrize("seed,n,flags", [
+    (31, 20000, ["-tau", "0.01", "-s", "64", "-m", "16", "-p", "1", "-H", "2.89441"]),
+    (32, 12000, ["-tau", "0.012", "-s", "32", "-m", "8", "-p", "1", "-nsp", "-H", "2.89441"]),
+])
+def test_pipeline_vs_oracle(gpu_ready, seed, n, flags):
+    from skid_gb300 import compare, pipeline
+    from skid_gb300.options import Options
+    from tests.helpers import small_snapshot
+    snap = small_snapshot(n=n, n_halo=12, seed=seed, r200=0.05)
+    opts = Options.parse(flags)
+    res = pipeline.run(snap, opts)
+    r = oracle.run(snap, opts)
+    m = compare.match_groups(r["grp"], res.grp)
+    assert m.agreement >= 0.999, m.agreement
+    assert m.same_groups()
+    assert res.counts["nGroupFoF"] == r["nGroupFoF"]
+    assert res.counts["nGroup"] == r["nGroup"]
+    assert res.counts["nIter"] == r["nIter"]

@@ -1,0 +1,64 @@
+"""Pin the oracle against the reference's own outputs (golden fixtures)."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests import golden_cases as gc
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_oracle_matches_reference(name):
+    snap, opts, ref, counts, meta = gc.load(name)
+    r = oracle.run(snap, opts)
+    gc.check_catalogue(r["grp"], r["groups"], ref, opts)
+    if "nExtraScat" in counts:
+        assert r["nExtraScat"] == counts["nExtraScat"]
+    assert r["nGroupFoF"] == counts["nGroupFoF"]
+    assert abs(r["nUnbound"] - counts["nUnbound"]) <= max(2, 0.001 * snap.n)
+    assert r["nGroup"] == counts["nGroup"]
+    assert r["nIter"] == counts["nIter"]
+    if "den" in ref:
+        rel = np.abs(r["rho"] - ref["den"]) / np.maximum(ref["den"], 1e-30)
+        assert rel[ref["den"] > 0].max() < 1e-5
+        assert np.all(r["rho"][ref["den"] == 0] == 0)
+
+
+def test_knn_tree_equals_brute():
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(-0.5, 0.5, (1500, 3)).astype(np.float32)
+    pos[:300] *= np.float32(0.05)   # a dense clump
+    for period in (1.0, None):
+        for k in (1, 8, 64):
+            a = oracle.knn_ball2(pos, k, period)
+            b = oracle.knn_ball2(pos, k, period, brute=True)
+            assert np.array_equal(a, b)
+
+
+def test_fof_matches_bruteforce_components():
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(-0.5, 0.5, (800, 3)).astype(np.float32)
+    tau = 0.06
+    grp, ng = oracle.fof(pos, tau, 1.0)
+    # brute force components with the same edge rule
+    n = len(pos)
+    par = list(range(n))
+
+    def find(x):
+        while par[x] != x:
+            par[x] = par[par[x]]
+            x = par[x]
+        return x
+    for i in range(n):
+        for j in range(i + 1, n):
+            d = min(oracle.d2(pos[i], pos[j], 1.0), oracle.d2(pos[j], pos[i], 1.0))
+            if d < np.float32(tau) * np.float32(tau):
+                par[find(i)] = find(j)
+    roots = {}
+    for i in range(n):
+        roots.setdefault(find(i), []).append(i)
+    assert ng == len(roots)
+    for members in roots.values():
+        assert len(set(grp[members])) == 1
+    # numbering: ascending smallest member
+    firsts = sorted(min(m) for m in roots.values())
+    assert [grp[f] for f in firsts] == list(range(1, ng + 1))
