@@ -52,7 +52,8 @@ class Params(C.Structure):
                 ("bNoUnbind", C.c_int), ("iSoftType", C.c_int), ("bEps", C.c_int),
                 ("fEps", C.c_float), ("G", C.c_float), ("Omega0", C.c_float),
                 ("Lambda", C.c_float), ("fQuintess", C.c_float), ("H0", C.c_float),
-                ("z", C.c_float), ("maxIter", C.c_int), ("verbose", C.c_int)]
+                ("z", C.c_float), ("maxIter", C.c_int), ("verbose", C.c_int),
+                ("stopAfter", C.c_int)]
 
 
 class Group(C.Structure):
@@ -174,9 +175,10 @@ def d2(q, c, period=None):
     return float(lib().or_d2(_fp(q), _fp(c), _fp(_period(period))))
 
 
-def run(snap, flags, verbose=False, max_iter=0):
+def run(snap, flags, verbose=False, max_iter=0, stop_after=0):
     """Run the whole pipeline on a Snapshot with skid-style options (a
-    ``skid_gb300.options.Options``).  Returns a dict of arrays."""
+    ``skid_gb300.options.Options``).  Returns a dict of arrays.  stop_after=1
+    stops after the group centres (FoF groups), 2 after unbinding."""
     from skid_gb300.options import Options
     o = flags if isinstance(flags, Options) else Options.parse(flags)
     p = Params()
@@ -195,6 +197,7 @@ def run(snap, flags, verbose=False, max_iter=0):
     p.G, p.Omega0, p.Lambda, p.fQuintess, p.H0, p.z = o.G, o.Omega0, o.Lambda, o.fQuintess, o.H0, o.z
     p.maxIter = max_iter or o.maxIter
     p.verbose = int(verbose)
+    p.stopAfter = int(stop_after)
     n = snap.n
     pos = np.ascontiguousarray(snap.pos, np.float32)
     vel = np.ascontiguousarray(snap.vel, np.float32)

@@ -1054,6 +1054,16 @@ int or_run(const or_params *P, int nGas, int nDark, int nStar, double time,
         }
     }
     free(gsum);
+    if (P->stopAfter == 1) {
+        res->nGroupFoF = nGroup - 1;
+        res->nGroup = nGroup - 1;
+        for (int g = 0; g < nGroup && g < cap_groups; ++g) groups[g] = G[g];
+        free(G);
+        free(mgrp); free(mio); free(mr); free(mold); free(ar); free(act); free(acc);
+        free(spos); free(smass); free(sb2); free(srho); free(rho); free(sidx); free(sft);
+        free(S.rho); free(S.alive); free(S.zeroed);
+        return 0;
+    }
     /* 9. unbinding (kd.c:1299-1466) */
     if (P->bEps) for (int i = 0; i < n; ++i) sft[i] = P->fEps;
     res->nGroupFoF = nGroup - 1;
@@ -1131,6 +1141,15 @@ int or_run(const or_params *P, int nGas, int nDark, int nStar, double time,
     free(order);
     res->nUnbound = nUnbind;
     if (P->verbose) printf("Number of particles Unbound:%d\n", nUnbind);
+    if (P->stopAfter == 2) {
+        res->nGroup = nGroup - 1;
+        for (int g = 0; g < nGroup && g < cap_groups; ++g) groups[g] = G[g];
+        free(G);
+        free(mgrp); free(mio); free(mr); free(mold); free(ar); free(act); free(acc);
+        free(spos); free(smass); free(sb2); free(srho); free(rho); free(sidx); free(sft);
+        free(S.rho); free(S.alive); free(S.zeroed);
+        return 0;
+    }
     /* 10. too small (kd.c:1251-1293) */
     int *map = (int *)malloc((size_t)nGroup * sizeof(int));
     int ng2 = 1;

@@ -55,6 +55,7 @@ typedef struct or_params {
     float G, Omega0, Lambda, fQuintess, H0, z;
     int   maxIter;        /* cap on outer move iterations; <=0 means none */
     int   verbose;        /* print the reference's progress lines */
+    int   stopAfter;      /* 0 full run; 1 stop after group centres; 2 after unbinding */
 } or_params;
 
 typedef struct or_group {

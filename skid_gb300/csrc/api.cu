@@ -370,6 +370,12 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
     ctx->nStar = nStar;
     ctx->time = time;
     ctx->inType = (nDark ? 1 : 0) | (nGas ? 2 : 0) | (nStar ? 4 : 0);
+    ctx->mass_total = 0.0;
+    ctx->soft_min = n > 0 ? soft[0] : 0.0f;
+    for (int i = 0; i < n; ++i) {
+        ctx->mass_total += fabs((double)mass[i]);
+        if (soft[i] < ctx->soft_min) ctx->soft_min = soft[i];
+    }
     if (ctx->alloc_particles(n)) return ctx->fail(SKID_ENOMEM);
     if (n == 0) { ctx->stage = STAGE_LOADED; return 0; }
     // staging: raw host arrays -> device, then pack to float4 records

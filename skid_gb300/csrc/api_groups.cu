@@ -168,6 +168,7 @@ int skid_set_soft(skid_ctx *ctx, float fEps)
     if (!ctx) return SKID_EINVAL;
     if (ctx->stage < STAGE_LOADED) return ctx->fail(SKID_ESTATE);
     set_soft_k<<<grid_for(ctx->n), 256, 0, ctx->st>>>(ctx->vel4.p, ctx->n, fEps);
+    ctx->soft_min = fEps;
     return ctx->sync_check();
 }
 
@@ -202,9 +203,11 @@ int skid_unbind(skid_ctx *ctx, int iSoftType, float fScoop, int bGasAndDark, int
     P.a = a;
     P.aH = aH;
     P.opz = (float)(1.0 + (double)z);
+    P.z = z;
     P.plummer = iSoftType == SKID_SOFT_PLUMMER;
     P.subpot = ctx->inType == 1 || ctx->inType == 4;   // kd.c:1441
     P.nounbind = bNoUnbind != 0;
+    P.scale = ctx->pot_scale(G);
     CK(unbind_run(ctx->G, ctx->G.gof.p, ctx->n, ctx->pos4.p, ctx->vel4.p, ctx->utree, P, ctx->grp.p,
                   ctx->d_scal + SC_NUNB, ctx->ss, ctx->U, st));
     int nu = 0;

@@ -2,6 +2,8 @@
 #pragma once
 
 #include "../../include/skid_gpu.h"
+#include <cmath>
+
 #include "internal.h"
 
 namespace skid {
@@ -68,13 +70,14 @@ struct UnbindParams {
     bool per;
     float fScoop;
     int nmax;          // -maxgroup
-    float G, a, aH, opz;
+    float G, a, aH, opz, z;
+    float scale;       // 2^S of the fixed-point potentials
     int plummer, subpot, nounbind;
 };
 
 struct UnbindScratch {
     DBuf<float4> qr, qv, slist;
-    DBuf<float2> pot;
+    DBuf<long long> pot;
     DBuf<int> qid, scnt, soff, nt, toff, cnt;
     DBuf<int2> items;
     DBuf<float> ssoft, usoft;
@@ -121,6 +124,8 @@ struct skid_ctx {
 
     int n = 0, nGas = 0, nDark = 0, nStar = 0, inType = 0;
     double time = 0.0;
+    double mass_total = 0.0;        // host-side, for the fixed-point potential scale
+    float soft_min = 0.0f;
     int stage = skid::STAGE_NONE;
     int last_error = 0;
 
@@ -171,6 +176,19 @@ struct skid_ctx {
     skid::FieldArgs field_args(float fStep, bool initial, float *acc_out);
     float3 wrap_hi() const;
     float3 wrap_lo() const;
+
+    // 2^S such that |potential| * 2^S < 2^62: the spline potential is at most
+    // 1.4 * 2/(eps_i+eps_j) <= 1.4/eps_min per unit G*mass (grav.h:11-31), and
+    // the Plummer form at most 2/(eps_i+eps_j).
+    float pot_scale(float G) const
+    {
+        if (!(soft_min > 0.0f)) return ldexpf(1.0f, 40);
+        double B = 4.0 * fabs((double)G) * mass_total * 1.4 / (double)soft_min;
+        int S = (int)floor(62.0 - log2(B > 1e-300 ? B : 1e-300));
+        if (S < 0) S = 0;
+        if (S > 60) S = 60;
+        return ldexpf(1.0f, S);
+    }
     int enqueue_step(float fStep, bool initial, bool nocut);
 
     unsigned char *probe_touched()

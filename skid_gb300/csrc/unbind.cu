@@ -12,10 +12,17 @@
 //   update rcm/vcm (FP64), swap it with the last member, and for pure dark
 //   or pure star input subtract its potential from the others (kdSubPot).
 //
+// Potentials are accumulated in 64-bit fixed point (term * 2^S rounded to an
+// integer).  The reference adds float terms into a double, which is exact
+// for realistic groups, so when kdSubPot later subtracts the same terms the
+// remainder is exact -- in particular a group's last member ends with
+// potential exactly 0 (or its scoop part) and is unbound with E = 1/2 dv^2 >= 0.
+// Integer sums reproduce that exactly and in any order.
+//
 // Kernels: scoop lists (one thread per group walks the tree of ungrouped
-// particles), the all-pairs potential (one block per 128-member tile,
-// compensated FP32 sums kept as a float pair), and the removal loop (one
-// block per group, block-wide arg-max with first-index ties).
+// particles), the all-pairs potential (one block per 128-member tile), and
+// the removal loop (one block per group, block-wide arg-max with
+// first-index ties).
 #include <cfloat>
 
 #include "ctx.h"
@@ -26,6 +33,11 @@ namespace {
 
 constexpr int POT_TILE = 128;
 constexpr int RM_THREADS = 256;
+// Groups up to this size evaluate E exactly as the reference does (FP64
+// expression rounded to float, kd.c:1396-1399), so equal-energy members are
+// ordered by the reference's own rounding; larger groups use FP32 (GB300's
+// FP64 rate is a small fraction of its FP32 rate).
+constexpr int EXACT_E_MAX = 1024;
 
 __device__ __forceinline__ float spline_pot(float d2, float twoh, int plummer)
 {
@@ -52,15 +64,8 @@ __device__ __forceinline__ float wrap_h(float d, float h)
     return d;
 }
 
-// Two-sum accumulation into a float pair (hi, lo).
-__device__ __forceinline__ void pair_add(float &hi, float &lo, float x)
-{
-    float s = hi + x;
-    float bp = s - hi;
-    float err = (hi - (s - bp)) + (x - bp);
-    hi = s;
-    lo += err;
-}
+// Fixed-point quantum of a float term (scale = 2^S, exact multiply).
+__device__ __forceinline__ long long fx(float t, float scale) { return __float2ll_rn(t * scale); }
 
 __global__ void prep_members(const int *__restrict__ members, const int *__restrict__ gof, int n,
                              const float4 *__restrict__ pos4, const float4 *__restrict__ vel4,
@@ -153,7 +158,8 @@ pot_kernel(const int2 *__restrict__ items, const int *d_nitems, const int *__res
            const int *__restrict__ gcount, const float4 *__restrict__ qr,
            const float4 *__restrict__ qv, const int *__restrict__ soff,
            const int *__restrict__ scnt, const float4 *__restrict__ slist,
-           const float *__restrict__ ssoft, float G, int plummer, float2 *__restrict__ pot)
+           const float *__restrict__ ssoft, float G, int plummer, float scale,
+           long long *__restrict__ pot)
 {
     __shared__ float4 sr[POT_TILE];
     __shared__ float ss[POT_TILE];
@@ -166,7 +172,7 @@ pot_kernel(const int2 *__restrict__ items, const int *d_nitems, const int *__res
         bool valid = i < n;
         float4 ri = valid ? qr[s + i] : make_float4(0, 0, 0, 0);
         float ei = valid ? qv[s + i].w : 0.0f;
-        float hi = 0.0f, lo = 0.0f;
+        long long acc = 0;
         for (int jb = 0; jb < n; jb += POT_TILE) {
             __syncthreads();
             int j = jb + threadIdx.x;
@@ -176,15 +182,13 @@ pot_kernel(const int2 *__restrict__ items, const int *d_nitems, const int *__res
             }
             __syncthreads();
             int cnt = min(POT_TILE, n - jb);
-            float part = 0.0f;
             for (int k = 0; k < cnt; ++k) {
                 float4 rj = sr[k];
                 float d2 = d2of(fsub(ri.x, rj.x), fsub(ri.y, rj.y), fsub(ri.z, rj.z));
                 float dir = spline_pot(d2, fadd(ei, ss[k]), plummer);
                 float term = fmul(fmul(G, rj.w), dir);
-                part += (jb + k != i) ? term : 0.0f;
+                acc += (jb + k != i) ? fx(term, scale) : 0ll;
             }
-            pair_add(hi, lo, part);
         }
         // kdAddScoopPot: grav.c:112-127
         int so = soff[g], sc = scnt[g];
@@ -197,19 +201,14 @@ pot_kernel(const int2 *__restrict__ items, const int *d_nitems, const int *__res
             }
             __syncthreads();
             int cnt = min(POT_TILE, sc - jb);
-            float part = 0.0f;
             for (int k = 0; k < cnt; ++k) {
                 float4 rj = sr[k];
                 float d2 = d2of(fsub(rj.x, ri.x), fsub(rj.y, ri.y), fsub(rj.z, ri.z));
                 float dir = spline_pot(d2, fadd(ss[k], ei), plummer);
-                part += fmul(fmul(G, rj.w), dir);
+                acc += fx(fmul(fmul(G, rj.w), dir), scale);
             }
-            pair_add(hi, lo, part);
         }
-        if (valid) {
-            float h2 = hi + lo;
-            pot[s + i] = make_float2(h2, lo - (h2 - hi));
-        }
+        if (valid) pot[s + i] = acc;
     }
 }
 
@@ -245,11 +244,13 @@ struct RemoveArgs {
     int ng, nmax;
     float4 *qr, *qv;
     int *qid;
-    float2 *pot;
+    long long *pot;
     skid_group *rec;
     int *grp;
     int *d_unbound;
     float G, fShift, fCosmo, opz;   // a, a*H(a), 1+z
+    float z;
+    float scale, inv_scale;         // 2^S, 2^-S
     float3 hP;
     int plummer, subpot, nounbind;
 };
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(RM_THREADS) remove_kernel(RemoveArgs A)
         float4 *qr = A.qr + s;
         float4 *qv = A.qv + s;
         int *qid = A.qid + s;
-        float2 *pot = A.pot + s;
+        long long *pot = A.pot + s;
         // centre of mass and velocity (kd.c:1360-1375), FP64 sums of float products
         double m = 0.0, c[6] = {0, 0, 0, 0, 0, 0};
         for (int i = tid; i < n0; i += RM_THREADS) {
@@ -302,6 +303,9 @@ __global__ void __launch_bounds__(RM_THREADS) remove_kernel(RemoveArgs A)
         }
         __syncthreads();
         int nrem = 0;
+        const bool exact = n0 <= EXACT_E_MAX;
+        const double opz_d = 1.0 + (double)A.z;
+        const double inv_d = 1.0 / (double)A.scale;
         while (true) {
             int n = s_n;
             bool have = s_have != 0;
@@ -309,26 +313,34 @@ __global__ void __launch_bounds__(RM_THREADS) remove_kernel(RemoveArgs A)
             float es = s_eps;
             float cm0 = s_cm[0], cm1 = s_cm[1], cm2 = s_cm[2];
             float vm0 = s_cm[3], vm1 = s_cm[4], vm2 = s_cm[5];
+            double dc0 = d_cm[0], dc1 = d_cm[1], dc2 = d_cm[2];
+            double dv0m = d_cm[3], dv1m = d_cm[4], dv2m = d_cm[5];
             ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
             for (int i = tid; i < n; i += RM_THREADS) {
                 float4 r = qr[i], v = qv[i];
-                float2 p = pot[i];
+                long long p = pot[i];
                 if (have && A.subpot) {
                     // kdSubPot (grav.c:44-59)
                     float d2 = d2of(fsub(rs.x, r.x), fsub(rs.y, r.y), fsub(rs.z, r.z));
                     float dir = spline_pot(d2, fadd(es, v.w), A.plummer);
-                    float t = fmul(fmul(A.G, rs.w), dir);
-                    float hi = p.x, lo = p.y;
-                    pair_add(hi, lo, -t);
-                    float h2 = hi + lo;
-                    p = make_float2(h2, lo - (h2 - hi));
+                    p -= fx(fmul(fmul(A.G, rs.w), dir), A.scale);
                     pot[i] = p;
                 }
-                float dv0 = A.fShift * (v.x - vm0) + A.fCosmo * (r.x - cm0);
-                float dv1 = A.fShift * (v.y - vm1) + A.fCosmo * (r.y - cm1);
-                float dv2 = A.fShift * (v.z - vm2) + A.fCosmo * (r.z - cm2);
-                float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
-                float E = 0.5f * dd - (p.x + p.y) * A.opz;
+                float E;
+                if (exact) {
+                    double fs = A.fShift, fc = A.fCosmo;
+                    float dv0 = (float)(fs * ((double)v.x - dv0m) + fc * ((double)r.x - dc0));
+                    float dv1 = (float)(fs * ((double)v.y - dv1m) + fc * ((double)r.y - dc1));
+                    float dv2 = (float)(fs * ((double)v.z - dv2m) + fc * ((double)r.z - dc2));
+                    float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
+                    E = (float)(0.5 * (double)dd - ((double)p * inv_d) * opz_d);
+                } else {
+                    float dv0 = A.fShift * (v.x - vm0) + A.fCosmo * (r.x - cm0);
+                    float dv1 = A.fShift * (v.y - vm1) + A.fCosmo * (r.y - cm1);
+                    float dv2 = A.fShift * (v.z - vm2) + A.fCosmo * (r.z - cm2);
+                    float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
+                    E = 0.5f * dd - (__ll2float_rn(p) * A.inv_scale) * A.opz;
+                }
                 if (E > mx.v) { mx.v = E; mx.i = i; }
                 if (E < mn.v) { mn.v = E; mn.i = i; }
             }
@@ -370,7 +382,7 @@ __global__ void __launch_bounds__(RM_THREADS) remove_kernel(RemoveArgs A)
                         // swap with the last member (kd.c:1435-1440)
                         float4 rl = qr[nn], vl = qv[nn];
                         int il = qid[nn], ir = qid[ib];
-                        float2 pl = pot[nn], pb = pot[ib];
+                        long long pl = pot[nn], pb = pot[ib];
                         qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
                         qr[nn] = r; qv[nn] = v; qid[nn] = ir; pot[nn] = pb;
                         s_r = r;
@@ -451,7 +463,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
         int blocks = nitems < num_sms() * 16 ? nitems : num_sms() * 16;
         pot_kernel<<<blocks, POT_TILE, 0, st>>>(U.items.p, U.cnt.p + 1, G.start.p, G.count.p, U.qr.p,
                                                 U.qv.p, U.soff.p, U.scnt.p, U.slist.p, U.ssoft.p,
-                                                P.G, P.plummer, U.pot.p);
+                                                P.G, P.plummer, P.scale, U.pot.p);
     }
     // removal loop, one block per group
     RemoveArgs A;
@@ -470,6 +482,9 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     A.fShift = P.a;
     A.fCosmo = P.aH;
     A.opz = P.opz;
+    A.z = P.z;
+    A.scale = P.scale;
+    A.inv_scale = 1.0f / P.scale;
     A.hP = hP;
     A.plummer = P.plummer;
     A.subpot = P.subpot;
