@@ -70,7 +70,11 @@ typedef struct skid_group {
 typedef struct skid_timings {
     float density_ms, moving_ms, fof_ms, micro_ms, groups_ms, unbind_ms, toosmall_ms;
     long long gather_launches;  /* move-field kernel launches so far */
-    long long kernel_launches;  /* all kernels launched so far */
+    long long kernel_launches;  /* all kernels launched so far, all contexts */
+    double field_ms;            /* summed CUDA-event time of the move-field kernel */
+    double field_bytes;         /* its algorithmic bytes: 24 per active mover
+                                   (position read + write) + 20 per live
+                                   scatterer (position, mass, fBall2) */
 } skid_timings;
 
 /* kdInit (kd.c:46-82) + smInit (smooth1.c:8-29). */
@@ -85,12 +89,20 @@ const char *skid_strerror(int code);
 /* First error latched on this context (0 if none). */
 int skid_last_error(const skid_ctx *ctx);
 
+/* Text of the first CUDA runtime error behind a SKID_ECUDA ("none" if none). */
+const char *skid_last_cuda_error(const skid_ctx *ctx);
+
 /* kdReadTipsy (kd.c:122-222), data part: copies particles to the device.
  * pos/vel are float[3n], mass/soft/temp float[n]; temp may be NULL (0).
  * soft is hsmooth for gas and eps for dark and star. */
 int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double time,
                        const float *pos, const float *vel, const float *mass,
                        const float *soft, const float *temp);
+
+/* Return to the state right after skid_set_particles, keeping the particles
+ * on the device (for repeated runs on one snapshot; no reference
+ * counterpart: the reference reads its input once). */
+int skid_restart(skid_ctx *ctx);
 
 /* kdScatterActive (kd.c:669-693) with ScatterCriterion (kd.c:600-627). */
 int skid_scatter_active(skid_ctx *ctx, int bGasAndDark, int bGasOnly, int *nScatter);
@@ -164,6 +176,16 @@ int skid_get_moved(skid_ctx *ctx, float *pos);
 int skid_get_final_density(skid_ctx *ctx, float *rho);
 
 int skid_get_timings(skid_ctx *ctx, skid_timings *t);
+
+/* Work counters of the move-field kernel (no reference counterpart): with
+ * enable set, later move steps count tree nodes visited, leaves visited,
+ * candidate scatterer tests and in-ball hits.  out4 (may be NULL) receives
+ * the counts so far; the counters then restart from zero. */
+int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time or
+ * order their own work against the library's (no reference counterpart). */
+int skid_stream(skid_ctx *ctx, void **stream);
 
 /* ---- Stage probes with explicit inputs (parity tests, adjoint checks). ---- */
 

@@ -54,6 +54,12 @@ __global__ void permute_scat(const uint32_t *__restrict__ perm, const int *__res
     }
 }
 
+__global__ void ball_aux(const float *__restrict__ b, int n, float4 *__restrict__ aux)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        aux[i] = make_float4(b[i], 0.0f, 0.0f, __uint_as_float(1u));
+}
+
 __global__ void fill_float(float *p, float v, int n)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
@@ -204,7 +210,7 @@ int skid_ctx::fail(int code)
 
 int skid_ctx::fail_cuda(cudaError_t e)
 {
-    (void)e;
+    if (!last_cuda) last_cuda = (int)e;
     cudaGetLastError();
     return fail(SKID_ECUDA);
 }
@@ -245,43 +251,64 @@ float skid_ctx::timer_stop()
 
 FieldArgs skid_ctx::field_args(float fStep, bool initial, float *acc_out)
 {
+    (void)initial;
     FieldArgs a;
-    a.spos = S.spos.p;
-    a.saux = S.saux.p;
-    a.blo = stree.blo.p;
-    a.bhi = stree.bhi.p;
-    a.lo = stree.lo.p;
-    a.hi = stree.hi.p;
-    a.leafBase = stree.leafBase;
-    a.d_nS = S.d_nS;
+    a.cpos = C.cpos.p;
+    a.ccoef = C.ccoef.p;
+    a.blo = ctree.blo.p;
+    a.bhi = ctree.bhi.p;
+    a.leafBase = ctree.leafBase;
+    a.d_nC = C.d_n;
     a.mpos = M.mpos.p;
     a.act = M.act.p;
     a.d_nA = M.d_nA;
-    a.L = L;
-    a.hL = hL;
-    a.per = per;
     a.fStep = fStep;
     a.period = L;
     a.wrapHi = wrap_hi();
     a.wrapLo = wrap_lo();
     a.acc_out = acc_out;
-    a.touched = S.touched.p;
-    a.touched_bits = initial ? S.tbits.p : nullptr;
+    a.touched = C.touched.p;
     a.d_work = d_scal + SC_WORK;
     a.d_status = d_status;
+    a.stats = field_stats_on ? d_fstats : nullptr;
+    a.G = movers_per_warp();
     return a;
 }
 
+__global__ void field_bytes_kernel(const int *d_nA, const int *d_nS, double *acc)
+{
+    acc[0] += 24.0 * (double)*d_nA + 20.0 * (double)*d_nS;
+    acc[1] += 1.0;
+}
+
 // One move pass: field + move, cut, refit.  Stream-ordered, no host sync.
-int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut)
+// `slot` picks the event pair that times this step's field kernel.
+int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int G)
 {
     skid_ctx *ctx = this;
     FieldArgs a = field_args(fStep, initial, nullptr);
+    a.G = G;
+    field_bytes_kernel<<<1, 1, 0, st>>>(M.d_nA, C.d_n, d_fbytes); skid::note_launch();
+    // while capturing, external records make the events real timing nodes of
+    // the outer-iteration graph (a plain record would only order the capture)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cs));
+    unsigned evflags = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
+    CK(cudaEventRecordWithFlags(fev[2 * slot], st, evflags));
     CK(field_move(a, nMove, st));
-    ++gather_launches;
-    CK(scatter_cut(S, initial, nocut, rho_final.p, ss, st));
-    CK(tree_refit(stree, S.spos.p, S.saux.p, S.d_nS, st));
+    CK(cudaEventRecordWithFlags(fev[2 * slot + 1], st, evflags));
+    CK(scatter_cut(C, initial, nocut, rho_final.p, ss, st));
+    CK(tree_refit(ctree, C.cpos.p, nullptr, C.d_n, st, true, C.d_dirty));
     return 0;
+}
+
+void skid_ctx::collect_field_times(int nslots)
+{
+    for (int i = 0; i < nslots; ++i) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, fev[2 * i], fev[2 * i + 1]) == cudaSuccess) tim.field_ms += ms;
+        else cudaGetLastError();
+    }
 }
 
 // ---------------------------------------------------------------------
@@ -306,6 +333,12 @@ const char *skid_strerror(int code)
 
 int skid_last_error(const skid_ctx *ctx) { return ctx ? ctx->last_error : SKID_EINVAL; }
 
+const char *skid_last_cuda_error(const skid_ctx *ctx)
+{
+    if (!ctx || !ctx->last_cuda) return "none";
+    return cudaGetErrorString((cudaError_t)ctx->last_cuda);
+}
+
 int skid_create(skid_ctx **pctx, const skid_params *par)
 {
     if (!pctx || !par) return SKID_EINVAL;
@@ -326,18 +359,22 @@ int skid_create(skid_ctx **pctx, const skid_params *par)
     ctx->L = make_float3(par->period[0], par->period[1], par->period[2]);
     ctx->hL = make_float3(0.5f * par->period[0], 0.5f * par->period[1], 0.5f * par->period[2]);
     ctx->per = par->period[0] < 0.25f * FLT_MAX;
-    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc((void **)&ctx->d_scal, SC_COUNT * sizeof(int)) != cudaSuccess ||
-        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+    bool ok = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc((void **)&ctx->d_scal, SC_COUNT * sizeof(int)) == cudaSuccess &&
+              cudaMalloc((void **)&ctx->d_fbytes, 2 * sizeof(double)) == cudaSuccess &&
+              cudaEventCreate(&ctx->ev0) == cudaSuccess && cudaEventCreate(&ctx->ev1) == cudaSuccess;
+    for (cudaEvent_t &e : ctx->fev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    if (!ok) {
         delete ctx;
         return SKID_ENOMEM;
     }
     cudaMemset(ctx->d_scal, 0, SC_COUNT * sizeof(int));
+    cudaMemset(ctx->d_fbytes, 0, 2 * sizeof(double));
     ctx->d_status = (unsigned *)(ctx->d_scal + SC_STATUS);
-    ctx->S.d_nS = ctx->d_scal + SC_NS;
-    ctx->S.d_nS2 = ctx->d_scal + SC_NS2;
-    ctx->S.d_floor = (unsigned *)(ctx->d_scal + SC_FLOOR);
-    ctx->S.d_live = ctx->d_scal + SC_LIVE;
+    ctx->C.d_n = ctx->d_scal + SC_NC;
+    ctx->C.d_n2 = ctx->d_scal + SC_NC2;
+    ctx->C.d_floor = (unsigned *)(ctx->d_scal + SC_FLOOR);
+    ctx->C.d_dirty = ctx->d_scal + SC_DIRTY;
     ctx->M.d_nA = ctx->d_scal + SC_NA;
     ctx->M.d_nA2 = ctx->d_scal + SC_NA2;
     *pctx = ctx;
@@ -376,6 +413,8 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
         ctx->mass_total += fabs((double)mass[i]);
         if (soft[i] < ctx->soft_min) ctx->soft_min = soft[i];
     }
+    ctx->soft_min_input = ctx->soft_min;
+    ctx->soft_changed = false;
     if (ctx->alloc_particles(n)) return ctx->fail(SKID_ENOMEM);
     if (n == 0) { ctx->stage = STAGE_LOADED; return 0; }
     // staging: raw host arrays -> device, then pack to float4 records
@@ -392,13 +431,43 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
     pack_particles<<<grid_for(n), 256, 0, ctx->st>>>(d_raw, d_raw + n3, d_raw + 2 * n3,
                                                      d_raw + 2 * n3 + n,
                                                      temp ? d_raw + 2 * n3 + 2 * (size_t)n : nullptr,
-                                                     n, ctx->pos4.p, ctx->vel4.p, ctx->temp.p);
+                                                     n, ctx->pos4.p, ctx->vel4.p, ctx->temp.p); skid::note_launch();
     CK(cudaGetLastError());
-    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho.p, 0.0f, n);
-    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho_final.p, 0.0f, n);
-    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->ball2.p, -1.0f, n);
+    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho.p, 0.0f, n); skid::note_launch();
+    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho_final.p, 0.0f, n); skid::note_launch();
+    fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->ball2.p, -1.0f, n); skid::note_launch();
     CK(cudaMemsetAsync(ctx->grp.p, 0, n * sizeof(int), ctx->st));
-    ctx->kernel_launches += 4;
+
+    ctx->stage = STAGE_LOADED;
+    return ctx->sync_check();
+}
+
+__global__ void restore_soft(float4 *vel4, const float *soft, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        vel4[i].w = soft[i];
+}
+
+int skid_restart(skid_ctx *ctx)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (ctx->stage < STAGE_LOADED) return ctx->fail(SKID_ESTATE);
+    int n = ctx->n;
+    double mt = ctx->mass_total;
+    float sm = ctx->soft_min_input;
+    ctx->reset_pipeline();
+    ctx->mass_total = mt;
+    ctx->soft_min = sm;
+    if (n > 0) {
+        if (ctx->soft_changed) {
+            restore_soft<<<grid_for(n), 256, 0, ctx->st>>>(ctx->vel4.p, ctx->soft_orig.p, n); skid::note_launch();
+            ctx->soft_changed = false;
+        }
+        fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho.p, 0.0f, n); skid::note_launch();
+        fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho_final.p, 0.0f, n); skid::note_launch();
+        fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->ball2.p, -1.0f, n); skid::note_launch();
+        CK(cudaMemsetAsync(ctx->grp.p, 0, n * sizeof(int), ctx->st));
+    }
     ctx->stage = STAGE_LOADED;
     return ctx->sync_check();
 }
@@ -447,34 +516,34 @@ int skid_density(skid_ctx *ctx, int *nExtraScat)
     cudaStream_t st = ctx->st;
     ctx->timer_start();
     Ranges r = ctx->ranges;
-    gather_ranges<<<grid_for(ns), 256, 0, st>>>(r, ctx->pos4.p, ctx->S.spos2.p, ctx->S.sidx2.p);
+    gather_ranges<<<grid_for(ns), 256, 0, st>>>(r, ctx->pos4.p, ctx->spos0.p, ctx->sidx0.p); skid::note_launch();
     CK(cudaGetLastError());
-    CK(tree_build(ctx->stree, ctx->S.spos2.p, ns, true, ctx->ss, st));
-    CK(knn_ball2(ctx->stree, ctx->par.nSmooth, ctx->L, ctx->per, ctx->S.srho2.p,
+    CK(tree_build(ctx->stree, ctx->spos0.p, ns, true, ctx->ss, st));
+    CK(knn_ball2(ctx->stree, ctx->par.nSmooth, ctx->L, ctx->per, ctx->sb2.p,
                  ctx->d_scal + SC_WORK, ctx->knn_heap, st));
-    // srho2 holds fBall2 (sorted); aux = (b, ih2, fNorm m, copies)
+    // node max fBall2 for the density gather
+    ball_aux<<<grid_for(ns), 256, 0, st>>>(ctx->sb2.p, ns, ctx->saux.p); skid::note_launch();
+    CK(tree_refit(ctx->stree, nullptr, ctx->saux.p, nullptr, st));
+    CK(density_gather(ctx->stree, ctx->sb2.p, ctx->L, ctx->per, ctx->srho.p,
+                      ctx->d_scal + SC_WORK, st));
+    permute_scat<<<grid_for(ns), 256, 0, st>>>(ctx->stree.perm.p, ctx->sidx0.p, ctx->sb2.p,
+                                               ctx->srho.p, ns, ctx->sidx.p, ctx->rho.p,
+                                               ctx->ball2.p, ctx->rho_final.p); skid::note_launch();
+    // move-phase copies (originals + periodic replicas) and their tree
     float3 blo = make_float3((float)((double)ctx->par.center[0] - 0.5 * (double)ctx->par.period[0]),
                              (float)((double)ctx->par.center[1] - 0.5 * (double)ctx->par.period[1]),
                              (float)((double)ctx->par.center[2] - 0.5 * (double)ctx->par.period[2]));
     float3 bhi = make_float3((float)((double)ctx->par.center[0] + 0.5 * (double)ctx->par.period[0]),
                              (float)((double)ctx->par.center[1] + 0.5 * (double)ctx->par.period[1]),
                              (float)((double)ctx->par.center[2] + 0.5 * (double)ctx->par.period[2]));
-    CK(scatter_aux(ctx->stree.pos.p, ctx->S.srho2.p, ns, ctx->L, blo, bhi, ctx->par.periodic != 0,
-                   ctx->S.saux.p, ctx->d_scal + SC_EXTRA, st));
-    CK(tree_refit(ctx->stree, nullptr, ctx->S.saux.p, nullptr, st));
-    CK(density_gather(ctx->stree, ctx->S.srho2.p, ctx->L, ctx->per, ctx->S.srho.p,
-                      ctx->d_scal + SC_WORK, st));
-    permute_scat<<<grid_for(ns), 256, 0, st>>>(ctx->stree.perm.p, ctx->S.sidx2.p, ctx->S.srho2.p,
-                                               ctx->S.srho.p, ns, ctx->S.sidx.p, ctx->rho.p,
-                                               ctx->ball2.p, ctx->rho_final.p);
-    CK(cudaMemcpyAsync(ctx->S.spos.p, ctx->stree.pos.p, ns * sizeof(float4),
-                       cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(ctx->S.d_nS, &ctx->nScatInit, sizeof(int), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(ctx->S.touched.p, 0, ns, st));
-    CK(cudaMemsetAsync(ctx->S.tbits.p, 0, ns * sizeof(unsigned), st));
-    ctx->kernel_launches += 16;
-    int extra = 0;
-    if (int rc = ctx->read_int(ctx->d_scal + SC_EXTRA, &extra)) return rc;
+    int nc = 0;
+    CK(build_copies(ctx->stree.pos.p, ctx->sb2.p, ctx->srho.p, ctx->sidx.p, ns, ctx->L, blo, bhi,
+                    ctx->par.periodic != 0, ctx->C, ctx->ss, &nc, st));
+    CK(tree_shape(ctx->ctree, nc, true));
+    CK(tree_refit(ctx->ctree, ctx->C.cpos.p, nullptr, ctx->C.d_n, st, true));
+    ctx->nCopies = nc;
+    int extra = nc - ns;
+    if (int rc = ctx->sync_check()) return rc;
     ctx->nExtraScat = extra;
     ctx->tim.density_ms += ctx->timer_stop();
     if (nExtraScat) *nExtraScat = ctx->par.periodic ? extra : 0;
@@ -510,23 +579,49 @@ int skid_init_move(skid_ctx *ctx, float fDensMin, float fTempMax, float fMassMax
     if (ctx->alloc_movers(n)) return ctx->fail(SKID_ENOMEM);
     cut_criterion<<<grid_for(n), 256, 0, st>>>(ctx->pos4.p, ctx->rho.p, ctx->temp.p, n, ctx->nGas,
                                                ctx->nDark, ctx->inType, fDensMin, fTempMax,
-                                               fMassMax, bGasAndDark, bGasOnly, ctx->M.keep.p);
+                                               fMassMax, bGasAndDark, bGasOnly, ctx->M.keep.p); skid::note_launch();
     CK(scan_exclusive(ctx->M.keep.p, ctx->M.kpos.p, n, ctx->M.d_nA, ctx->ss, st));
-    compact_index<<<grid_for(n), 256, 0, st>>>(ctx->M.keep.p, ctx->M.kpos.p, n, ctx->M.act2.p);
+    compact_index<<<grid_for(n), 256, 0, st>>>(ctx->M.keep.p, ctx->M.kpos.p, n, ctx->M.act2.p); skid::note_launch();
     int nm = 0;
     if (int rc = ctx->read_int(ctx->M.d_nA, &nm)) return rc;
     ctx->nMove = nm;
+    ctx->M.cap = nm > 0 ? nm : 1;   // prune passes and sorts run over this capacity
     // Morton order of the movers' starting positions keeps warps coherent.
     if (nm > 0) {
-        gather_by_index<<<grid_for(nm), 256, 0, st>>>(ctx->M.act2.p, ctx->pos4.p, nm, ctx->M.mold.p);
+        gather_by_index<<<grid_for(nm), 256, 0, st>>>(ctx->M.act2.p, ctx->pos4.p, nm, ctx->M.mold.p); skid::note_launch();
         CK(morton_order(ctx->M.mold.p, nm, ctx->ss, st));
+        // key frame for the re-sorts at every prune: the periodic box, or the
+        // movers' starting bounding box grown by half its size
+        unsigned hb[6];
+        CK(cudaMemcpyAsync(hb, ctx->ss.box.p, sizeof(hb), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        float lo3[3], hi3[3];
+        for (int d = 0; d < 3; ++d) {
+            unsigned u = hb[d], v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+            memcpy(&lo3[d], &v, 4);
+            u = hb[3 + d];
+            v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+            memcpy(&hi3[d], &v, 4);
+            if (ctx->per) {
+                lo3[d] = ctx->par.center[d] - 0.5f * ctx->par.period[d];
+                hi3[d] = ctx->par.center[d] + 0.5f * ctx->par.period[d];
+            } else {
+                float g = 0.5f * (hi3[d] - lo3[d]);
+                lo3[d] -= g;
+                hi3[d] += g;
+            }
+        }
+        float ext = fmaxf(fmaxf(hi3[0] - lo3[0], hi3[1] - lo3[1]), fmaxf(hi3[2] - lo3[2], 1e-30f));
+        float sc = 2097151.0f / ext;
+        ctx->mkey_lo = make_float3(lo3[0], lo3[1], lo3[2]);
+        ctx->mkey_inv = make_float3(sc, sc, sc);
         init_movers<<<grid_for(nm), 256, 0, st>>>(ctx->ss.v0.p, ctx->M.act2.p, ctx->pos4.p, nm,
                                                    ctx->M.mio.p, ctx->M.mpos.p, ctx->M.mold.p,
-                                                   ctx->M.act.p);
+                                                   ctx->M.act.p); skid::note_launch();
         CK(cudaGetLastError());
     }
     CK(cudaMemcpyAsync(ctx->M.d_nA, &ctx->nMove, sizeof(int), cudaMemcpyHostToDevice, st));
-    ctx->kernel_launches += 8;
+
     ctx->nActive = nm;
     if (nMove) *nMove = nm;
     ctx->stage = STAGE_MOVE;
@@ -538,11 +633,14 @@ int skid_move_step(skid_ctx *ctx, float fStep, int bInitial, int bNoCut, int *nS
     if (!ctx) return SKID_EINVAL;
     if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
     ctx->timer_start();
-    if (ctx->nMove > 0 || bInitial) {
-        if (int rc = ctx->enqueue_step(fStep, bInitial != 0, bNoCut != 0)) return rc;
+    bool ran = ctx->nMove > 0 || bInitial;
+    if (ran) {
+        int rc = ctx->enqueue_step(fStep, bInitial != 0, bNoCut != 0, 0, ctx->movers_per_warp());
+        if (rc) return rc;
     }
     int live = 0;
-    if (int rc = ctx->read_int(ctx->S.d_live, &live)) return rc;
+    if (int rc = ctx->read_int(ctx->C.d_n, &live)) return rc;
+    if (ran) ctx->collect_field_times(1);
     float ms = ctx->timer_stop();
     if (ctx->stage >= STAGE_FOF) ctx->tim.micro_ms += ms;
     else ctx->tim.moving_ms += ms;
@@ -555,7 +653,7 @@ int skid_prune_inactive(skid_ctx *ctx, float fCvg, int *nActive)
     if (!ctx) return SKID_EINVAL;
     if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
     ctx->timer_start();
-    CK(mover_prune(ctx->M, ctx->L, fCvg, ctx->ss, ctx->st));
+    CK(mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, ctx->st));
     int na = 0;
     if (int rc = ctx->read_int(ctx->M.d_nA, &na)) return rc;
     ctx->tim.moving_ms += ctx->timer_stop();
@@ -564,6 +662,8 @@ int skid_prune_inactive(skid_ctx *ctx, float fCvg, int *nActive)
     return 0;
 }
 
+static int graph_slot(int G) { return G == 32 ? 0 : (G == 8 ? 1 : 2); }
+
 int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *nActive,
                       int *nScatter)
 {
@@ -571,42 +671,64 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
     if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
     cudaStream_t st = ctx->st;
     ctx->timer_start();
-    bool same = ctx->iter_graph && ctx->g_fStep == fStep && ctx->g_fCvg == fCvg &&
-                ctx->g_nocut == (bNoCut != 0);
+    int G = ctx->movers_per_warp();
+    int gs = graph_slot(G);
+    bool same = ctx->iter_graph[gs] && ctx->g_fStep[gs] == fStep && ctx->g_fCvg[gs] == fCvg &&
+                ctx->g_nocut[gs] == (bNoCut != 0) && ctx->g_stats[gs] == ctx->field_stats_on;
     bool ran = false;
     if (!same) {
-        if (ctx->iter_graph) { cudaGraphExecDestroy(ctx->iter_graph); ctx->iter_graph = nullptr; }
+        if (ctx->iter_graph[gs]) {
+            cudaGraphExecDestroy(ctx->iter_graph[gs]);
+            ctx->iter_graph[gs] = nullptr;
+        }
         if (!ctx->iter_eager_done) {
             // the first iteration runs eagerly; it sizes every scratch buffer
             for (int i = 0; i < PRUNE_STEPS; ++i)
-                if (int rc = ctx->enqueue_step(fStep, false, bNoCut != 0)) return rc;
-            CK(mover_prune(ctx->M, ctx->L, fCvg, ctx->ss, st));
+                if (int rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G)) return rc;
+            CK(mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st));
             ctx->iter_eager_done = true;
             ran = true;
         } else {
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            set_capturing(true);
             int rc = 0;
             for (int i = 0; i < PRUNE_STEPS && !rc; ++i)
-                rc = ctx->enqueue_step(fStep, false, bNoCut != 0);
-            if (!rc && mover_prune(ctx->M, ctx->L, fCvg, ctx->ss, st) != cudaSuccess) rc = SKID_ECUDA;
+                rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G);
+            if (!rc && mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st))
+                rc = SKID_ECUDA;
+            set_capturing(false);
             cudaError_t ce = cudaStreamEndCapture(st, &g);
             if (rc) return ctx->fail(rc);
             if (ce) return ctx->fail_cuda(ce);
-            ce = cudaGraphInstantiate(&ctx->iter_graph, g, 0);
+            size_t nn = 0;
+            cudaGraphGetNodes(g, nullptr, &nn);
+            std::vector<cudaGraphNode_t> nodes(nn);
+            if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+            ctx->iter_graph_kernels[gs] = 0;
+            for (auto nd : nodes) {
+                cudaGraphNodeType ty;
+                if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+                    ++ctx->iter_graph_kernels[gs];
+            }
+            ce = cudaGraphInstantiate(&ctx->iter_graph[gs], g, 0);
             cudaGraphDestroy(g);
             if (ce) return ctx->fail_cuda(ce);
-            ctx->g_fStep = fStep;
-            ctx->g_fCvg = fCvg;
-            ctx->g_nocut = bNoCut != 0;
+            ctx->g_fStep[gs] = fStep;
+            ctx->g_fCvg[gs] = fCvg;
+            ctx->g_nocut[gs] = bNoCut != 0;
+            ctx->g_stats[gs] = ctx->field_stats_on;
         }
     }
-    if (!ran) CK(cudaGraphLaunch(ctx->iter_graph, st));
-    ctx->kernel_launches += PRUNE_STEPS * 12 + 6;
+    if (!ran) {
+        CK(cudaGraphLaunch(ctx->iter_graph[gs], st));
+        note_launch((int)ctx->iter_graph_kernels[gs]);
+    }
     int vals[2];
     CK(cudaMemcpyAsync(&vals[0], ctx->M.d_nA, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&vals[1], ctx->S.d_live, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&vals[1], ctx->C.d_n, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (int rc = ctx->sync_check()) return rc;
+    ctx->collect_field_times(PRUNE_STEPS);
     ctx->tim.moving_ms += ctx->timer_stop();
     ctx->nActive = vals[0];
     if (nActive) *nActive = vals[0];
@@ -618,7 +740,7 @@ int skid_reactivate_move(skid_ctx *ctx)
 {
     if (!ctx) return SKID_EINVAL;
     if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
-    iota_kernel<<<grid_for(ctx->nMove), 256, 0, ctx->st>>>(ctx->M.act.p, ctx->nMove);
+    iota_kernel<<<grid_for(ctx->nMove), 256, 0, ctx->st>>>(ctx->M.act.p, ctx->nMove); skid::note_launch();
     CK(cudaMemcpyAsync(ctx->M.d_nA, &ctx->nMove, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
     ctx->nActive = ctx->nMove;
     return ctx->sync_check();
@@ -630,10 +752,10 @@ int skid_get_moved(skid_ctx *ctx, float *pos)
     if (ctx->stage < STAGE_LOADED) return ctx->fail(SKID_ESTATE);
     int n = ctx->n;
     float *d = ctx->raw.p;
-    pos4_to_xyz<<<grid_for(n), 256, 0, ctx->st>>>(ctx->pos4.p, n, d);
+    pos4_to_xyz<<<grid_for(n), 256, 0, ctx->st>>>(ctx->pos4.p, n, d); skid::note_launch();
     if (ctx->stage >= STAGE_MOVE && ctx->nMove > 0)
         moved_to_iorder<<<grid_for(ctx->nMove), 256, 0, ctx->st>>>(ctx->M.mpos.p, ctx->M.mio.p,
-                                                                   ctx->nMove, d);
+                                                                   ctx->nMove, d); skid::note_launch();
     CK(cudaMemcpyAsync(pos, d, 3 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
     return ctx->sync_check();
 }
@@ -642,8 +764,32 @@ int skid_get_timings(skid_ctx *ctx, skid_timings *t)
 {
     if (!ctx || !t) return SKID_EINVAL;
     *t = ctx->tim;
-    t->gather_launches = ctx->gather_launches;
-    t->kernel_launches = ctx->kernel_launches;
+    double fb[2] = {0.0, 0.0};
+    if (cudaMemcpy(fb, ctx->d_fbytes, sizeof(fb), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return ctx->fail(SKID_ECUDA);
+    t->gather_launches = (long long)fb[1];
+    t->kernel_launches = launches_total();
+    t->field_bytes = fb[0];
+    return 0;
+}
+
+int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4)
+{
+    if (!ctx) return SKID_EINVAL;
+    if (!ctx->d_fstats && cudaMalloc((void **)&ctx->d_fstats, 4 * sizeof(unsigned long long)))
+        return ctx->fail(SKID_ENOMEM);
+    if (out4) {
+        CK(cudaMemcpy(out4, ctx->d_fstats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    }
+    CK(cudaMemset(ctx->d_fstats, 0, 4 * sizeof(unsigned long long)));
+    ctx->field_stats_on = enable != 0;   // graphs are recaptured on the next iteration
+    return 0;
+}
+
+int skid_stream(skid_ctx *ctx, void **stream)
+{
+    if (!ctx || !stream) return SKID_EINVAL;
+    *stream = (void *)ctx->st;
     return 0;
 }
 
@@ -656,12 +802,12 @@ int skid_knn_ball2(skid_ctx *ctx, int n, const float *pos, int k, float *ball2)
     DBuf<float4> &p4 = ctx->probe_p4;
     if (dalloc(xyz, 3 * (size_t)n + n) || dalloc(p4, n)) return ctx->fail(SKID_ENOMEM);
     CK(cudaMemcpyAsync(xyz.p, pos, 3 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
-    xyz_to_pos4<<<grid_for(n), 256, 0, st>>>(xyz.p, n, p4.p);
+    xyz_to_pos4<<<grid_for(n), 256, 0, st>>>(xyz.p, n, p4.p); skid::note_launch();
     CK(tree_build(t, p4.p, n, false, ctx->ss, st));
     float *b_sorted = xyz.p;   // reuse: sorted results, then unsorted
     float *b_out = xyz.p + n;
     CK(knn_ball2(t, k, ctx->L, ctx->per, b_sorted, ctx->d_scal + SC_WORK, ctx->knn_heap, st));
-    unsort_floats<<<grid_for(n), 256, 0, st>>>(t.perm.p, b_sorted, n, b_out);
+    unsort_floats<<<grid_for(n), 256, 0, st>>>(t.perm.p, b_sorted, n, b_out); skid::note_launch();
     CK(cudaMemcpyAsync(ball2, b_out, n * sizeof(float), cudaMemcpyDeviceToHost, st));
     return ctx->sync_check();
 }
@@ -678,13 +824,15 @@ int skid_field(skid_ctx *ctx, int nm, const float *mpos, float *acc)
         dalloc(ctx->probe_acc, 3 * (size_t)nm))
         return ctx->fail(SKID_ENOMEM);
     CK(cudaMemcpyAsync(xyz.p, mpos, 3 * (size_t)nm * sizeof(float), cudaMemcpyHostToDevice, st));
-    xyz_to_pos4<<<grid_for(nm), 256, 0, st>>>(xyz.p, nm, p4.p);
-    iota_kernel<<<grid_for(nm), 256, 0, st>>>(act.p, nm);
+    xyz_to_pos4<<<grid_for(nm), 256, 0, st>>>(xyz.p, nm, p4.p); skid::note_launch();
+    iota_kernel<<<grid_for(nm), 256, 0, st>>>(act.p, nm); skid::note_launch();
     CK(cudaMemcpyAsync(act.p + nm, &nm, sizeof(int), cudaMemcpyHostToDevice, st));
     FieldArgs a = ctx->field_args(0.0f, false, ctx->probe_acc.p);
     a.mpos = p4.p;
     a.act = act.p;
     a.d_nA = act.p + nm;
+    a.G = 32;
+    a.stats = nullptr;
     a.touched = ctx->probe_touched();
     if (!a.touched) return ctx->fail(SKID_ENOMEM);
     CK(field_move(a, nm, st));

@@ -50,10 +50,12 @@ __global__ void set_centres(const skid_group *__restrict__ in, int ng, skid_grou
     }
 }
 
-__global__ void set_soft_k(float4 *vel4, int n, float eps)
+__global__ void set_soft_k(float4 *vel4, int n, float eps, float *keep)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (keep) keep[i] = vel4[i].w;
         vel4[i].w = eps;
+    }
 }
 
 __global__ void gather_group0(const int *__restrict__ members, const int *__restrict__ start,
@@ -95,7 +97,7 @@ int skid_fof(skid_ctx *ctx, float fTau, int *nGroup)
         // warps for the micro-steps)
         if (dalloc(ctx->moved4, ctx->n)) return ctx->fail(SKID_ENOMEM);
         reorder_movers<<<grid_for(nm), 256, 0, st>>>(ctx->mtree.perm.p, nm, ctx->M.mold.p,
-                                                     ctx->M.mio.p, ctx->moved4.p, ctx->M.act2.p);
+                                                     ctx->M.mio.p, ctx->moved4.p, ctx->M.act2.p); skid::note_launch();
         // mtree.pos holds the positions in the new order
         CK(cudaMemcpyAsync(ctx->M.mpos.p, ctx->mtree.pos.p, nm * sizeof(float4),
                            cudaMemcpyDeviceToDevice, st));
@@ -103,7 +105,7 @@ int skid_fof(skid_ctx *ctx, float fTau, int *nGroup)
                            cudaMemcpyDeviceToDevice, st));
         CK(cudaMemcpyAsync(ctx->M.mio.p, ctx->M.act2.p, nm * sizeof(int), cudaMemcpyDeviceToDevice,
                            st));
-        iota_k<<<grid_for(nm), 256, 0, st>>>(ctx->M.act.p, nm);
+        iota_k<<<grid_for(nm), 256, 0, st>>>(ctx->M.act.p, nm); skid::note_launch();
         CK(cudaMemcpyAsync(ctx->M.d_nA, &ctx->nMove, sizeof(int), cudaMemcpyHostToDevice, st));
     }
     int ng = 0;
@@ -111,7 +113,7 @@ int skid_fof(skid_ctx *ctx, float fTau, int *nGroup)
     ctx->G.nGroup = ng + 1;
     ctx->nActive = nm;
     ctx->tim.fof_ms += ctx->timer_stop();
-    ctx->kernel_launches += 12;
+
     if (nGroup) *nGroup = ng;
     ctx->stage = STAGE_FOF;
     return 0;
@@ -128,13 +130,13 @@ int skid_group_centers(skid_ctx *ctx)
     CK(cudaMemcpyAsync(ctx->moved4.p, ctx->pos4.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
     if (ctx->nMove > 0)
         scatter_movers<<<grid_for(ctx->nMove), 256, 0, st>>>(ctx->M.mpos.p, ctx->M.mio.p, ctx->nMove,
-                                                             ctx->moved4.p);
+                                                             ctx->moved4.p); skid::note_launch();
     CK(group_order(ctx->grp.p, n, ctx->G.nGroup, ctx->ss, ctx->G, st));
     CK(group_props(ctx->G, ctx->pos4.p, ctx->vel4.p, ctx->moved4.p, ctx->L, ctx->wrap_hi(),
                    ctx->wrap_lo(), false, false, st));
     if (int rc = ctx->sync_check()) return rc;
     ctx->tim.groups_ms += ctx->timer_stop();
-    ctx->kernel_launches += 8;
+
     ctx->stage = STAGE_GROUPS;
     return 0;
 }
@@ -156,7 +158,7 @@ int skid_set_groups(skid_ctx *ctx, const int *grp, int nGroup, const skid_group 
         DBuf<skid_group> &tmp = ctx->G.rec2;
         if (dalloc(tmp, nGroup)) return ctx->fail(SKID_ENOMEM);
         CK(cudaMemcpyAsync(tmp.p, centers, nGroup * sizeof(skid_group), cudaMemcpyHostToDevice, st));
-        set_centres<<<grid_for(nGroup), 256, 0, st>>>(tmp.p, nGroup, ctx->G.rec.p);
+        set_centres<<<grid_for(nGroup), 256, 0, st>>>(tmp.p, nGroup, ctx->G.rec.p); skid::note_launch();
     }
     if (int rc = ctx->sync_check()) return rc;
     ctx->stage = STAGE_GROUPS;
@@ -167,7 +169,13 @@ int skid_set_soft(skid_ctx *ctx, float fEps)
 {
     if (!ctx) return SKID_EINVAL;
     if (ctx->stage < STAGE_LOADED) return ctx->fail(SKID_ESTATE);
-    set_soft_k<<<grid_for(ctx->n), 256, 0, ctx->st>>>(ctx->vel4.p, ctx->n, fEps);
+    float *keep = nullptr;
+    if (!ctx->soft_changed) {
+        if (dalloc(ctx->soft_orig, ctx->n > 0 ? ctx->n : 1)) return ctx->fail(SKID_ENOMEM);
+        keep = ctx->soft_orig.p;
+        ctx->soft_changed = true;
+    }
+    set_soft_k<<<grid_for(ctx->n), 256, 0, ctx->st>>>(ctx->vel4.p, ctx->n, fEps, keep); skid::note_launch();
     ctx->soft_min = fEps;
     return ctx->sync_check();
 }
@@ -188,12 +196,12 @@ int skid_unbind(skid_ctx *ctx, int iSoftType, float fScoop, int bGasAndDark, int
     if (dalloc(u4, n0 > 0 ? n0 : 1) || dalloc(ctx->U.usoft, n0 > 0 ? n0 : 1)) return ctx->fail(SKID_ENOMEM);
     if (n0 > 0) {
         gather_group0<<<grid_for(n0), 256, 0, st>>>(ctx->G.members.p, ctx->G.start.p, ctx->G.count.p,
-                                                    ctx->pos4.p, u4.p);
+                                                    ctx->pos4.p, u4.p); skid::note_launch();
     }
     CK(tree_build(ctx->utree, u4.p, n0, false, ctx->ss, st));
     if (n0 > 0)
         gather_usoft<<<grid_for(n0), 256, 0, st>>>(ctx->utree.perm.p, ctx->G.members.p, ctx->G.start.p,
-                                                   n0, ctx->vel4.p, ctx->U.usoft.p);
+                                                   n0, ctx->vel4.p, ctx->U.usoft.p); skid::note_launch();
     UnbindParams P;
     P.period = ctx->L;
     P.per = ctx->per;
@@ -213,7 +221,7 @@ int skid_unbind(skid_ctx *ctx, int iSoftType, float fScoop, int bGasAndDark, int
     int nu = 0;
     if (int rc = ctx->read_int(ctx->d_scal + SC_NUNB, &nu)) return rc;
     ctx->tim.unbind_ms += ctx->timer_stop();
-    ctx->kernel_launches += 12;
+
     if (nUnbound) *nUnbound = nu;
     ctx->stage = STAGE_UNBOUND;
     return 0;
@@ -231,7 +239,7 @@ int skid_too_small(skid_ctx *ctx, int nMembers, int *nGroup)
     CK(group_radius(ctx->G, ctx->grp.p, ctx->n, ctx->pos4.p, ctx->L, ctx->st));
     if (int rc = ctx->sync_check()) return rc;
     ctx->tim.toosmall_ms += ctx->timer_stop();
-    ctx->kernel_launches += 6;
+
     if (nGroup) *nGroup = ng;
     ctx->stage = STAGE_FINAL;
     return 0;
@@ -263,8 +271,8 @@ int skid_fof_points(skid_ctx *ctx, int n, const float *pos, float fTau, int *grp
     if (dalloc(xyz, 3 * (size_t)n) || dalloc(p4, n) || dalloc(io, n) || dalloc(g, n))
         return ctx->fail(SKID_ENOMEM);
     CK(cudaMemcpyAsync(xyz.p, pos, 3 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
-    xyz_to_p4<<<grid_for(n), 256, 0, st>>>(xyz.p, n, p4.p);
-    iota_k<<<grid_for(n), 256, 0, st>>>(io.p, n);
+    xyz_to_p4<<<grid_for(n), 256, 0, st>>>(xyz.p, n, p4.p); skid::note_launch();
+    iota_k<<<grid_for(n), 256, 0, st>>>(io.p, n); skid::note_launch();
     CK(fof_run(ctx->probe_tree, p4.p, n, io.p, n, fTau, ctx->L, ctx->per, ctx->ss, ctx->parent,
                ctx->fof_minio, ctx->fof_flag, g.p, ctx->d_scal + SC_NG, ctx->d_scal + SC_WORK,
                ctx->d_status, st));

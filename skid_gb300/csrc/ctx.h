@@ -14,10 +14,10 @@ constexpr int PRUNE_STEPS = 5;   // main.c:13
 enum {
     SC_WORK = 0,     // work-queue counter of tree walks
     SC_STATUS = 1,   // latched status bits
-    SC_NS = 2,
-    SC_NS2 = 3,
+    SC_NC = 2,       // live scatterer copies
+    SC_NC2 = 3,
     SC_FLOOR = 4,
-    SC_LIVE = 5,
+    SC_DIRTY = 5,
     SC_NA = 6,
     SC_NA2 = 7,
     SC_EXTRA = 8,
@@ -83,14 +83,6 @@ struct UnbindScratch {
     DBuf<float> ssoft, usoft;
 };
 
-inline int grid_for(int n, int threads = 256)
-{
-    int b = (n + threads - 1) / threads;
-    int cap = num_sms() * 8;
-    if (b > cap) b = cap;
-    return b < 1 ? 1 : b;
-}
-
 // fof.cu
 cudaError_t fof_run(Tree &t, const float4 *pts, int np, const int *mio, int niorder, float tau,
                     float3 L, bool per, SortScratch &ss, DBuf<int> &par, DBuf<int> &minio,
@@ -126,19 +118,29 @@ struct skid_ctx {
     double time = 0.0;
     double mass_total = 0.0;        // host-side, for the fixed-point potential scale
     float soft_min = 0.0f;
+    float soft_min_input = 0.0f;
     int stage = skid::STAGE_NONE;
     int last_error = 0;
+    int last_cuda = 0;              // first CUDA runtime error seen
 
     // particles by iOrder
     skid::DBuf<float4> pos4, vel4;
     skid::DBuf<float> temp, rho, rho_final, ball2, raw;
+    skid::DBuf<float> soft_orig;    // input softening, kept once -e overrides it
+    bool soft_changed = false;
     skid::DBuf<int> grp;
 
     // scatterers, movers, groups
     skid::Ranges ranges{};
     int nScatInit = 0, nExtraScat = 0;
-    skid::Tree stree;
-    skid::ScatState S;
+    skid::Tree stree;               // periodic tree over the scatterers (kNN, density)
+    skid::DBuf<float4> spos0;       // scatterers in list order (tree input)
+    skid::DBuf<int> sidx0, sidx;    // iOrder in list / tree order
+    skid::DBuf<float> sb2, srho;    // fBall2 and density in tree order
+    skid::DBuf<float4> saux;        // density-gather node data
+    skid::CopyState C;              // move-phase scatterer copies
+    skid::Tree ctree;               // tree over the copies (ball boxes)
+    int nCopies = 0;
     int nMove = 0, nActive = 0;
     skid::MoverState M;
     skid::Tree mtree;               // tree over movers (FoF)
@@ -151,10 +153,18 @@ struct skid_ctx {
     skid::SortScratch ss;
     skid::DBuf<float> knn_heap;     // kNN heaps when k is too large for shared memory
 
-    // outer-iteration CUDA graph
-    cudaGraphExec_t iter_graph = nullptr;
-    float g_fStep = 0.0f, g_fCvg = 0.0f;
-    bool g_nocut = false;
+    // outer-iteration CUDA graphs, one per movers-per-warp setting
+    cudaGraphExec_t iter_graph[3] = {nullptr, nullptr, nullptr};
+    long long iter_graph_kernels[3] = {0, 0, 0};
+    float g_fStep[3] = {0, 0, 0}, g_fCvg[3] = {0, 0, 0};
+    bool g_nocut[3] = {false, false, false};
+    bool g_stats[3] = {false, false, false};
+    float3 mkey_lo{}, mkey_inv{};   // Morton frame of mover positions
+    // move-field kernel timing: an event pair per step slot of an iteration
+    cudaEvent_t fev[2 * skid::PRUNE_STEPS] = {};
+    double *d_fbytes = nullptr;     // [bytes, launches] accumulated on device
+    unsigned long long *d_fstats = nullptr;   // move-field work counters
+    bool field_stats_on = false;
     bool iter_eager_done = false;
 
     // probes
@@ -189,24 +199,36 @@ struct skid_ctx {
         if (S > 60) S = 60;
         return ldexpf(1.0f, S);
     }
-    int enqueue_step(float fStep, bool initial, bool nocut);
+    int enqueue_step(float fStep, bool initial, bool nocut, int slot, int G);
+    int movers_per_warp() const
+    {
+        // 32 movers per warp while the active set is dense; fewer as it thins
+        return nActive >= 32768 ? 32 : (nActive >= 2048 ? 8 : 1);
+    }
+    void drop_graphs()
+    {
+        for (auto &g : iter_graph)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+    void collect_field_times(int nslots);
 
     unsigned char *probe_touched()
     {
-        size_t need = S.spos.n ? S.spos.n : 1;
+        size_t need = C.cap > 0 ? C.cap : 1;
         if (skid::dalloc(probe_t, need)) return nullptr;
         return probe_t.p;
     }
 
     void reset_pipeline()
     {
-        if (iter_graph) { cudaGraphExecDestroy(iter_graph); iter_graph = nullptr; }
+        drop_graphs();
         iter_eager_done = false;
         stage = skid::STAGE_NONE;
         nScatInit = nExtraScat = nMove = nActive = 0;
         G.nGroup = 0;
         tim = skid_timings{};
         cudaMemsetAsync(d_scal, 0, skid::SC_COUNT * sizeof(int), st);
+        cudaMemsetAsync(d_fbytes, 0, 2 * sizeof(double), st);
     }
 
     int alloc_particles(int np)
@@ -223,11 +245,9 @@ struct skid_ctx {
     {
         using skid::dalloc;
         size_t m = ns > 0 ? ns : 1;
-        if (dalloc(S.spos, m) || dalloc(S.saux, m) || dalloc(S.spos2, m) || dalloc(S.saux2, m) ||
-            dalloc(S.srho, m) || dalloc(S.srho2, m) || dalloc(S.sidx, m) || dalloc(S.sidx2, m) ||
-            dalloc(S.touched, m) || dalloc(S.tbits, m) || dalloc(S.keep, m) || dalloc(S.kpos, m))
+        if (dalloc(spos0, m) || dalloc(sidx0, m) || dalloc(sidx, m) || dalloc(sb2, m) ||
+            dalloc(srho, m) || dalloc(saux, m))
             return -1;
-        // exact capacity: cut/compaction passes loop to the capacity
         return 0;
     }
 
@@ -238,22 +258,23 @@ struct skid_ctx {
         if (dalloc(M.mpos, m) || dalloc(M.mold, m) || dalloc(M.mio, m) || dalloc(M.act, m) ||
             dalloc(M.act2, m) || dalloc(M.keep, m) || dalloc(M.kpos, m))
             return -1;
+        M.cap = (int)m;
         return 0;
     }
 
     ~skid_ctx()
     {
         using skid::dfree;
-        if (iter_graph) cudaGraphExecDestroy(iter_graph);
+        drop_graphs();
         dfree(pos4); dfree(vel4); dfree(temp); dfree(rho); dfree(rho_final); dfree(ball2);
-        dfree(raw); dfree(grp);
-        for (skid::Tree *t : {&stree, &mtree, &utree, &probe_tree}) {
+        dfree(raw); dfree(grp); dfree(soft_orig);
+        for (skid::Tree *t : {&stree, &ctree, &mtree, &utree, &probe_tree}) {
             dfree(t->pos); dfree(t->perm); dfree(t->lo); dfree(t->hi); dfree(t->blo);
             dfree(t->bhi); dfree(t->flag);
         }
-        dfree(S.spos); dfree(S.saux); dfree(S.spos2); dfree(S.saux2); dfree(S.srho);
-        dfree(S.srho2); dfree(S.sidx); dfree(S.sidx2); dfree(S.touched); dfree(S.tbits);
-        dfree(S.keep); dfree(S.kpos);
+        dfree(spos0); dfree(sidx0); dfree(sidx); dfree(sb2); dfree(srho); dfree(saux);
+        dfree(C.cpos); dfree(C.ccoef); dfree(C.cpos2); dfree(C.ccoef2); dfree(C.touched);
+        dfree(C.keep); dfree(C.kpos); dfree(C.mask); dfree(C.cnt); dfree(C.off);
         dfree(M.mpos); dfree(M.mold); dfree(M.mio); dfree(M.act); dfree(M.act2); dfree(M.keep);
         dfree(M.kpos);
         dfree(parent);
@@ -267,6 +288,10 @@ struct skid_ctx {
         dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);
         dfree(probe_t); dfree(knn_heap);
         if (d_scal) cudaFree(d_scal);
+        if (d_fbytes) cudaFree(d_fbytes);
+        if (d_fstats) cudaFree(d_fstats);
+        for (cudaEvent_t &e : fev)
+            if (e) cudaEventDestroy(e);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (st) cudaStreamDestroy(st);

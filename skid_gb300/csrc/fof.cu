@@ -195,9 +195,9 @@ cudaError_t fof_run(Tree &t, const float4 *pts, int np, const int *mio, int nior
         return e;
     float tau2 = tau * tau;
     float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
-    uf_init<<<grid_for(np), 256, 0, st>>>(par.p, np);
+    uf_init<<<grid_for(np), 256, 0, st>>>(par.p, np); skid::note_launch();
     clique_kernel<<<grid_for(2 * t.leafBase), 256, 0, st>>>(t.lo.p, t.hi.p, t.leafBase, np, tau2,
-                                                           par.p, d_status);
+                                                           par.p, d_status); skid::note_launch();
     if ((e = cudaMemsetAsync(d_work, 0, sizeof(int), st))) return e;
     int perSM = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, link_kernel, F_WARPS * 32, 0);
@@ -205,14 +205,14 @@ cudaError_t fof_run(Tree &t, const float4 *pts, int np, const int *mio, int nior
     int blocks = num_sms() * perSM;
     int need = (t.nLeaf + F_WARPS - 1) / F_WARPS;
     if (blocks > need) blocks = need;
-    link_kernel<<<blocks, F_WARPS * 32, 0, st>>>(t.view(), tau2, L, hL, per, par.p, d_work, d_status);
-    fill_int<<<grid_for(np), 256, 0, st>>>(minio.p, 0x7fffffff, np);
-    root_min_iorder<<<grid_for(np), 256, 0, st>>>(par.p, np, t.perm.p, mio, minio.p);
+    link_kernel<<<blocks, F_WARPS * 32, 0, st>>>(t.view(), tau2, L, hL, per, par.p, d_work, d_status); skid::note_launch();
+    fill_int<<<grid_for(np), 256, 0, st>>>(minio.p, 0x7fffffff, np); skid::note_launch();
+    root_min_iorder<<<grid_for(np), 256, 0, st>>>(par.p, np, t.perm.p, mio, minio.p); skid::note_launch();
     int *fl = flag.p, *rank = flag.p + niorder;
     if ((e = cudaMemsetAsync(fl, 0, niorder * sizeof(int), st))) return e;
-    mark_roots<<<grid_for(np), 256, 0, st>>>(par.p, minio.p, np, fl);
+    mark_roots<<<grid_for(np), 256, 0, st>>>(par.p, minio.p, np, fl); skid::note_launch();
     if ((e = scan_exclusive(fl, rank, niorder, d_ng, ss, st))) return e;
-    write_groups<<<grid_for(np), 256, 0, st>>>(par.p, minio.p, rank, np, t.perm.p, mio, grp);
+    write_groups<<<grid_for(np), 256, 0, st>>>(par.p, minio.p, rank, np, t.perm.p, mio, grp); skid::note_launch();
     return cudaGetLastError();
 }
 

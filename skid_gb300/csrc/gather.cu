@@ -125,105 +125,97 @@ density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL,
     }
 }
 
+// Movers per warp G: 32 (one per lane), 8 (4 lanes each) or 1 (the warp
+// shares one mover).  Fewer movers per warp keep the union of their
+// neighbourhoods small when the active movers are sparse.  Each lane tests
+// G candidates of a visited leaf (one cheap pass that sets a hit mask), then
+// runs the field terms for its hits only; a mover's lanes are combined with
+// a fixed xor-butterfly, so sums are deterministic for a given G.
+template <int G>
 __global__ void __launch_bounds__(G_WARPS * 32)
 field_kernel(FieldArgs a)
 {
-    __shared__ float4 cpos[G_WARPS][SKID_LEAF];
-    __shared__ float4 caux[G_WARPS][SKID_LEAF];
+    constexpr int L = 32 / G;   // lanes per mover
+    __shared__ float4 cpos_s[G_WARPS][SKID_LEAF];
+    __shared__ float2 ccoef_s[G_WARPS][SKID_LEAF];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nA = *a.d_nA;
-    const int nS = *a.d_nS;
-    const int nLeafM = (nA + SKID_LEAF - 1) / SKID_LEAF;
-    const int nLeafS = (nS + SKID_LEAF - 1) / SKID_LEAF;
-    const bool initial = a.touched_bits != nullptr;
+    const int nC = *a.d_nC;
+    const int nItems = (nA + G - 1) / G;
+    const int sub = lane % L;
+    unsigned long long st_nodes = 0, st_leaves = 0, st_tests = 0, st_hits = 0;
     for (;;) {
-        int leaf = 0;
-        if (lane == 0) leaf = atomicAdd(a.d_work, 1);
-        leaf = __shfl_sync(SKID_FULL, leaf, 0);
-        if (leaf >= nLeafM) break;
-        int slot = leaf * SKID_LEAF + lane;
+        int item = 0;
+        if (lane == 0) item = atomicAdd(a.d_work, 1);
+        item = __shfl_sync(SKID_FULL, item, 0);
+        if (item >= nItems) break;
+        int slot = item * G + lane / L;
         bool valid = slot < nA;
-        int mi = a.act[valid ? slot : leaf * SKID_LEAF];
+        int mi = a.act[valid ? slot : item * G];
         float4 yp = a.mpos[mi];
         float3 y = make_float3(yp.x, yp.y, yp.z);
         float ax = 0.0f, ay = 0.0f, az = 0.0f;
         int cp = 1;
         for (;;) {
             float4 blo = a.blo[cp], bhi = a.bhi[cp];
-            bool want = box_lb(y, blo, bhi, a.L, a.per) <= 0.0f;
+            bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y && y.y <= bhi.y &&
+                        y.z >= blo.z && y.z <= bhi.z;
+            ++st_nodes;
             if (__any_sync(SKID_FULL, want)) {
                 if (cp < a.leafBase) { cp <<= 1; continue; }
-                int lf = cp - a.leafBase;
-                if (lf < nLeafS) {
-                    int cb = lf * SKID_LEAF;
-                    int cnt = min(SKID_LEAF, nS - cb);
-                    __syncwarp();
-                    if (lane < cnt) {
-                        cpos[w][lane] = a.spos[cb + lane];
-                        caux[w][lane] = a.saux[cb + lane];
-                    }
-                    __syncwarp();
-                    float4 plo = a.lo[cp], phi = a.hi[cp];
-                    // class of y - c: the scatterer image nearest y is c - class*L
-                    int cx = -img_class(y.x, plo.x, phi.x, a.hL.x);
-                    int cy = -img_class(y.y, plo.y, phi.y, a.hL.y);
-                    int cz = -img_class(y.z, plo.z, phi.z, a.hL.z);
-                    bool mixed = (cx == -2) | (cy == -2) | (cz == -2);
-                    bool slow = __any_sync(SKID_FULL, mixed);
-                    bool noshift = __all_sync(SKID_FULL, (cx == 0) & (cy == 0) & (cz == 0));
-                    unsigned mytouch = 0;
-                    for (int j = 0; j < cnt; ++j) {
-                        float4 c = cpos[w][j];
-                        float4 x = caux[w][j];
-                        float dx, dy, dz;
-                        int sx = 0, sy = 0, sz = 0;
-                        if (noshift) {
-                            dx = fsub(c.x, y.x); dy = fsub(c.y, y.y); dz = fsub(c.z, y.z);
-                        } else {
-                            if (slow) {
-                                // per candidate: nearest image of the scatterer to y
-                                float d0 = fsub(c.x, y.x);
-                                sx = d0 > a.hL.x ? -1 : (d0 < -a.hL.x ? 1 : 0);
-                                d0 = fsub(c.y, y.y);
-                                sy = d0 > a.hL.y ? -1 : (d0 < -a.hL.y ? 1 : 0);
-                                d0 = fsub(c.z, y.z);
-                                sz = d0 > a.hL.z ? -1 : (d0 < -a.hL.z ? 1 : 0);
-                            } else {
-                                sx = cx; sy = cy; sz = cz;
-                            }
-                            dx = fsub(shifted(c.x, sx, a.L.x), y.x);
-                            dy = fsub(shifted(c.y, sy, a.L.y), y.y);
-                            dz = fsub(shifted(c.z, sz, a.L.z), y.z);
-                        }
-                        float d2 = d2of(dx, dy, dz);
-                        unsigned bit = 0;
-                        if (valid && d2 < x.x) {
-                            unsigned img = (unsigned)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
-                            if ((__float_as_uint(x.w) >> img) & 1u) {
-                                bit = 1u << img;
-                                float r2 = fmul(d2, x.y);
-                                float rs = sqrtf(r2);
-                                float F = r2 < 1.0f ? __fmaf_rn(2.25f, rs, -3.0f)
-                                                    : (-3.0f / rs + 3.0f - 0.75f * rs);
-                                F = fmul(F, x.z);
-                                ax = fadd(ax, fmul(dx, F));
-                                ay = fadd(ay, fmul(dy, F));
-                                az = fadd(az, fmul(dz, F));
-                            }
-                        }
-                        unsigned hb = __reduce_or_sync(SKID_FULL, bit);
-                        if (lane == j) mytouch = hb;
-                    }
-                    if (mytouch) {
-                        if (initial) atomicOr(&a.touched_bits[cb + lane], mytouch);
-                        else a.touched[cb + lane] = 1;
-                    }
+                int cb = (cp - a.leafBase) * SKID_LEAF;
+                int cnt = min(SKID_LEAF, nC - cb);
+                __syncwarp();
+                if (lane < cnt) {
+                    cpos_s[w][lane] = a.cpos[cb + lane];
+                    float4 cc = a.ccoef[cb + lane];
+                    ccoef_s[w][lane] = make_float2(cc.x, cc.y);
                 }
+                __syncwarp();
+                ++st_leaves;
+                unsigned mask = 0;
+                if (want) {
+#pragma unroll
+                    for (int i = 0; i < G; ++i) {
+                        int j = sub + i * L;
+                        if (j < cnt) {
+                            float4 c = cpos_s[w][j];
+                            // smBallGather's test (smooth1.c:365-369), from the copy
+                            float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
+                            if (d2 < c.w) mask |= 1u << j;
+                        }
+                    }
+                    st_tests += (unsigned)min(G, max(0, (cnt - sub + L - 1) / L));
+                }
+                st_hits += __popc(mask);
+                for (unsigned m = mask; m; m &= m - 1) {
+                    int j = __ffs(m) - 1;
+                    float4 c = cpos_s[w][j];
+                    float2 k = ccoef_s[w][j];
+                    float dx = fsub(c.x, y.x), dy = fsub(c.y, y.y), dz = fsub(c.z, y.z);
+                    // smooth1.c:450-458
+                    float r2 = fmul(d2of(dx, dy, dz), k.x);
+                    float rs = sqrtf(r2);
+                    float F = r2 < 1.0f ? __fmaf_rn(2.25f, rs, -3.0f)
+                                        : (-3.0f / rs + 3.0f - 0.75f * rs);
+                    F = fmul(F, k.y);
+                    ax = fadd(ax, fmul(dx, F));
+                    ay = fadd(ay, fmul(dy, F));
+                    az = fadd(az, fmul(dz, F));
+                }
+                unsigned any = __reduce_or_sync(SKID_FULL, mask);
+                if ((any >> lane) & 1u) a.touched[cb + lane] = 1;
             }
             cp = next_node(cp);
             if (cp == 1) break;
         }
-        if (!valid) continue;
+#pragma unroll
+        for (int o = L / 2; o > 0; o >>= 1) {
+            ax = fadd(ax, __shfl_xor_sync(SKID_FULL, ax, o));
+            ay = fadd(ay, __shfl_xor_sync(SKID_FULL, ay, o));
+            az = fadd(az, __shfl_xor_sync(SKID_FULL, az, o));
+        }
+        if (!valid || sub != 0) continue;
         if (a.acc_out) {
             a.acc_out[3 * (size_t)slot + 0] = ax;
             a.acc_out[3 * (size_t)slot + 1] = ay;
@@ -246,6 +238,19 @@ field_kernel(FieldArgs a)
             a.mpos[mi] = make_float4(y.x, y.y, y.z, yp.w);
         }
     }
+    if (a.stats) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            st_tests += __shfl_xor_sync(SKID_FULL, st_tests, o);
+            st_hits += __shfl_xor_sync(SKID_FULL, st_hits, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&a.stats[0], st_nodes);
+            atomicAdd(&a.stats[1], st_leaves);
+            atomicAdd(&a.stats[2], st_tests);
+            atomicAdd(&a.stats[3], st_hits);
+        }
+    }
 }
 
 }  // namespace
@@ -264,7 +269,21 @@ cudaError_t density_gather(const Tree &t, const float *ball2_sorted, float3 L, b
     if (blocks > need) blocks = need;
     float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
     density_kernel<<<blocks, G_WARPS * 32, 0, st>>>(t.view(), ball2_sorted, L, hL, per, rho_sorted,
-                                                    d_work);
+                                                    d_work); skid::note_launch();
+    return cudaGetLastError();
+}
+
+template <int G>
+static cudaError_t launch_field(const FieldArgs &a, int max_movers, cudaStream_t st)
+{
+    int perSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, field_kernel<G>, G_WARPS * 32, 0);
+    if (perSM < 1) perSM = 1;
+    int blocks = num_sms() * perSM;
+    int need = ((max_movers + G - 1) / G + G_WARPS - 1) / G_WARPS;
+    if (blocks > need) blocks = need;
+    if (blocks < 1) blocks = 1;
+    field_kernel<G><<<blocks, G_WARPS * 32, 0, st>>>(a); skid::note_launch();
     return cudaGetLastError();
 }
 
@@ -273,14 +292,11 @@ cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st)
     if (max_movers <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(a.d_work, 0, sizeof(int), st);
     if (e) return e;
-    int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, field_kernel, G_WARPS * 32, 0);
-    if (perSM < 1) perSM = 1;
-    int blocks = num_sms() * perSM;
-    int need = ((max_movers + SKID_LEAF - 1) / SKID_LEAF + G_WARPS - 1) / G_WARPS;
-    if (blocks > need) blocks = need;
-    field_kernel<<<blocks, G_WARPS * 32, 0, st>>>(a);
-    return cudaGetLastError();
+    switch (a.G) {
+    case 1: return launch_field<1>(a, max_movers, st);
+    case 8: return launch_field<8>(a, max_movers, st);
+    default: return launch_field<32>(a, max_movers, st);
+    }
 }
 
 }  // namespace skid

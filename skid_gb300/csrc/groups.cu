@@ -213,12 +213,12 @@ cudaError_t group_order(const int *grp, int n, int ng, SortScratch &ss, GroupSta
         (e = dalloc(ss.v1, n)) || (e = dalloc(G.members, n)) || (e = dalloc(G.start, ng)) ||
         (e = dalloc(G.count, ng)) || (e = dalloc(G.gof, n)))
         return e;
-    keys_from_groups<<<grid_for(n), 256, 0, st>>>(grp, n, ss.k0.p, ss.v0.p);
+    keys_from_groups<<<grid_for(n), 256, 0, st>>>(grp, n, ss.k0.p, ss.v0.p); skid::note_launch();
     if ((e = radix_sort(ss, n, bits_for(ng), st))) return e;
-    fill_int<<<grid_for(ng), 256, 0, st>>>(G.start.p, -1, ng);
+    fill_int<<<grid_for(ng), 256, 0, st>>>(G.start.p, -1, ng); skid::note_launch();
     group_bounds<<<grid_for(n), 256, 0, st>>>(ss.k0.p, ss.v0.p, n, ng, G.start.p, G.count.p,
-                                              G.members.p, G.gof.p);
-    group_counts<<<grid_for(ng), 256, 0, st>>>(G.start.p, G.count.p, ng);
+                                              G.members.p, G.gof.p); skid::note_launch();
+    group_counts<<<grid_for(ng), 256, 0, st>>>(G.start.p, G.count.p, ng); skid::note_launch();
     return cudaGetLastError();
 }
 
@@ -234,7 +234,7 @@ cudaError_t group_props(GroupState &G, const float4 *pos4, const float4 *vel4, c
     if (blocks < 1) blocks = 1;
     group_props_kernel<<<blocks, 256, 0, st>>>(G.start.p, G.count.p, G.members.p, G.nGroup, pos4,
                                                vel4, moved, L, hL, wrapHi, wrapLo, com ? 1 : 0,
-                                               keep_centre ? 1 : 0, G.rec.p);
+                                               keep_centre ? 1 : 0, G.rec.p); skid::note_launch();
     return cudaGetLastError();
 }
 
@@ -246,15 +246,15 @@ cudaError_t too_small(GroupState &G, int *grp, int n, int nmin, int *d_ng, SortS
     if ((e = dalloc(G.gtmp, ng)) || (e = dalloc(G.gtmp2, ng)) || (e = dalloc(G.map, ng)))
         return e;
     if ((e = dalloc(G.rec2, ng))) return e;
-    toosmall_flags<<<grid_for(ng), 256, 0, st>>>(G.rec.p, ng, nmin, G.gtmp.p);
+    toosmall_flags<<<grid_for(ng), 256, 0, st>>>(G.rec.p, ng, nmin, G.gtmp.p); skid::note_launch();
     if ((e = scan_exclusive(G.gtmp.p, G.gtmp2.p, ng, d_ng, ss, st))) return e;
     // rank[g] = position among kept groups; records move to slot rank+1
     toosmall_apply<<<grid_for(ng), 256, 0, st>>>(G.gtmp.p, G.gtmp2.p, ng, G.rec.p, G.rec2.p,
-                                                 G.map.p);
+                                                 G.map.p); skid::note_launch();
     if ((e = cudaMemcpyAsync(G.rec.p, G.rec2.p, ng * sizeof(skid_group), cudaMemcpyDeviceToDevice,
                              st)))
         return e;
-    remap_groups<<<grid_for(n), 256, 0, st>>>(grp, n, G.map.p);
+    remap_groups<<<grid_for(n), 256, 0, st>>>(grp, n, G.map.p); skid::note_launch();
     return cudaGetLastError();
 }
 
@@ -266,8 +266,8 @@ cudaError_t group_radius(GroupState &G, const int *grp, int n, const float4 *pos
     if ((e = dalloc(G.gtmp, ng))) return e;
     float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
     if ((e = cudaMemsetAsync(G.gtmp.p, 0, ng * sizeof(int), st))) return e;
-    radius_kernel<<<grid_for(n), 256, 0, st>>>(grp, n, pos4, G.rec.p, L, hL, (unsigned *)G.gtmp.p);
-    radius_store<<<grid_for(ng), 256, 0, st>>>((const unsigned *)G.gtmp.p, ng, G.rec.p);
+    radius_kernel<<<grid_for(n), 256, 0, st>>>(grp, n, pos4, G.rec.p, L, hL, (unsigned *)G.gtmp.p); skid::note_launch();
+    radius_store<<<grid_for(ng), 256, 0, st>>>((const unsigned *)G.gtmp.p, ng, G.rec.p); skid::note_launch();
     return cudaGetLastError();
 }
 

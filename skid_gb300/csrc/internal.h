@@ -63,6 +63,13 @@ struct Tree {
     }
 };
 
+// ---- launch accounting (sort.cu) ----
+// Every kernel launch calls note_launch(); launches enqueued while a stream is
+// being captured into a graph are not counted (the graph's replays are).
+void note_launch(int n = 1);
+long long launches_total();
+void set_capturing(bool on);
+
 // ---- sort.cu ----
 // Stable LSD radix sort of (key, value) pairs on the low `bits` bits.
 // Result lands in (k0, v0) of the scratch.
@@ -78,11 +85,14 @@ int num_sms();
 // that is given per-slot ball data.
 cudaError_t tree_build(Tree &t, const float4 *pts, int n, bool balls, SortScratch &s,
                        cudaStream_t st);
-// Recompute leaf and node boxes from pos (t.pos when null) and, when aux is
-// given, per-slot ball data (aux.x = ball2, aux.w = live-copy mask; slots
-// with an empty mask are left out).  d_n (device) overrides t.n.
+// Recompute leaf and node boxes from pos (t.pos when null).  With aux, ball
+// data per slot (aux.x = ball2) also builds the ball boxes and max ball2;
+// with ballw the ball2 is pos.w instead.  d_n (device) overrides t.n; with
+// d_dirty the refit runs only when *d_dirty is set, and clears it.
 cudaError_t tree_refit(Tree &t, const float4 *pos, const float4 *aux, const int *d_n,
-                       cudaStream_t st);
+                       cudaStream_t st, bool ballw = false, int *d_dirty = nullptr);
+// Node arrays for n already-ordered points (no sort).
+cudaError_t tree_shape(Tree &t, int n, bool balls);
 // Morton order of n points: sorted permutation lands in s.v0.
 cudaError_t morton_order(const float4 *pts, int n, SortScratch &s, cudaStream_t st);
 cudaError_t bbox_of(const float4 *pts, int n, unsigned *d_box6, cudaStream_t st);
@@ -98,23 +108,38 @@ cudaError_t knn_ball2(const Tree &t, int k, float3 L, bool per, float *ball2_sor
 cudaError_t density_gather(const Tree &t, const float *ball2_sorted, float3 L, bool per,
                            float *rho_sorted, int *d_work, cudaStream_t st);
 
-// Scatterers in tree (Morton) order, compacted as ScatterCut removes them.
-// aux = (fBall2, ih2, fNorm*m, live-copy mask bits).
-struct ScatState {
-    DBuf<float4> spos, saux, spos2, saux2;
-    DBuf<float> srho, srho2;
-    DBuf<int> sidx, sidx2;          // iOrder of each slot
-    DBuf<unsigned char> touched;    // reached an active mover (non-first passes)
-    DBuf<unsigned> tbits;           // copies that reached a mover (first pass)
+// Scatterer copies of the move phase (originals and periodic replicas), in
+// Morton order of the copy positions, compacted as ScatterCut removes them.
+//   cpos  = (x_c, y_c, z_c, fBall2)
+//   ccoef = (ih2, fNorm*m, rho, iOrder | 0x80000000 for the original)
+struct CopyState {
+    int cap = 0;
+    DBuf<float4> cpos, ccoef, cpos2, ccoef2;
+    DBuf<unsigned char> touched;    // reached an active mover this step
     DBuf<int> keep, kpos;
-    int *d_nS = nullptr;            // live scatterers (device)
-    int *d_nS2 = nullptr;
+    DBuf<unsigned> mask;            // build-time image masks
+    DBuf<int> cnt, off;             // build-time copy counts / offsets
+    int *d_n = nullptr;             // live copies (device)
+    int *d_n2 = nullptr;
     unsigned *d_floor = nullptr;    // ordered-uint min density (fScatDens)
-    int *d_live = nullptr;          // live copies after the cut
+    int *d_dirty = nullptr;         // copies changed since the last refit
+    cudaError_t alloc(int n)
+    {
+        cudaError_t e;
+        size_t m = n > 0 ? n : 1;
+        if ((e = dalloc(cpos, m)) || (e = dalloc(ccoef, m)) || (e = dalloc(cpos2, m)) ||
+            (e = dalloc(ccoef2, m)) || (e = dalloc(touched, m)) || (e = dalloc(keep, m)) ||
+            (e = dalloc(kpos, m)))
+            return e;
+        cap = (int)m;
+        return cudaSuccess;
+    }
 };
 
-// Movers: positions by mover index; `act` lists the active ones.
+// Movers: positions by mover index; `act` lists the active ones, sorted by
+// the Morton key of their current positions after every prune.
 struct MoverState {
+    int cap = 0;
     DBuf<float4> mpos, mold;
     DBuf<int> mio;                  // iOrder of each mover
     DBuf<int> act, act2, keep, kpos;
@@ -123,37 +148,44 @@ struct MoverState {
 };
 
 struct FieldArgs {
-    // scatterers (tree-sorted, compacted): pos (x,y,z,m), aux (b, ih2, fnorm*m, mask)
-    const float4 *spos;
-    const float4 *saux;
-    const float4 *blo, *bhi;     // ball boxes
-    const float4 *lo, *hi;       // point boxes (periodic image class at leaves)
+    const float4 *cpos, *ccoef;      // copies
+    const float4 *blo, *bhi;         // ball boxes of the copy tree
     int leafBase;
-    const int *d_nS;             // live scatterers
-    // movers
-    float4 *mpos;                // positions (w unused)
-    const int *act;              // active mover indices
+    const int *d_nC;                 // live copies
+    float4 *mpos;                    // mover positions (w unused)
+    const int *act;                  // active mover indices
     const int *d_nA;
-    float3 L, hL;
-    bool per;
-    float fStep;                 // 0: no move (field probe)
-    float3 wrapHi, wrapLo;       // float thresholds of kdMoveParticles' wrap
+    float fStep;                     // 0: no move (field probe)
+    float3 wrapHi, wrapLo;           // float thresholds of kdMoveParticles' wrap
     float3 period;
-    float *acc_out;              // optional [3*nA] field output (probe)
-    unsigned char *touched;      // per scatterer slot (non-initial passes)
-    unsigned *touched_bits;      // per scatterer slot image bits (initial pass)
+    float *acc_out;                  // optional [3*nA] field output (probe)
+    unsigned char *touched;          // per copy slot
     int *d_work;
     unsigned *d_status;
+    unsigned long long *stats;       // optional: nodes, leaves, candidate tests, hits
+    int G;                           // movers per warp: 32, 8 or 1
 };
 cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st);
 
 // ---- scatter.cu ----
-cudaError_t scatter_aux(const float4 *spos, const float *ball2_sorted, int n, float3 L,
-                        float3 boxlo, float3 boxhi, bool periodic, float4 *aux, int *d_extra,
-                        cudaStream_t st);
+// Copies of the ns scatterers (sorted order) with their densities; sets
+// *nCopies and fills C (Morton-sorted).
+cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rho, const int *sidx,
+                         int ns, float3 L, float3 boxlo, float3 boxhi, bool periodic,
+                         CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st);
 // After a move pass: density floor, cut, stable compaction, counts.
-cudaError_t scatter_cut(ScatState &s, bool initial, bool nocut, float *final_rho, SortScratch &ss,
+cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, SortScratch &ss,
                         cudaStream_t st);
-cudaError_t mover_prune(MoverState &m, float3 period, float fCvg, SortScratch &ss, cudaStream_t st);
+// Prune converged movers, then re-sort the active ones by Morton key.
+cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,
+                        SortScratch &ss, cudaStream_t st);
+
+inline int grid_for(int n, int threads = 256)
+{
+    int b = (n + threads - 1) / threads;
+    int cap = num_sms() * 8;
+    if (b > cap) b = cap;
+    return b < 1 ? 1 : b;
+}
 
 }  // namespace skid

@@ -170,7 +170,7 @@ cudaError_t knn_ball2(const Tree &t, int k, float3 L, bool per, float *ball2_sor
     }
     float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
     if ((e = cudaMemsetAsync(d_work, 0, sizeof(int), st))) return e;
-    knn_kernel<<<blocks, nw * 32, smem, st>>>(t.view(), k, L, hL, per, ball2_sorted, d_work, gh);
+    knn_kernel<<<blocks, nw * 32, smem, st>>>(t.view(), k, L, hL, per, ball2_sorted, d_work, gh); skid::note_launch();
     return cudaGetLastError();
 }
 

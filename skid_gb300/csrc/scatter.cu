@@ -1,16 +1,25 @@
-// Scatterer and mover bookkeeping between move steps.
+// Scatterer copies and mover bookkeeping for the move phase.
 //
-//  - scatter_aux: per scatterer the move-field coefficients and the set of
-//    its copies: the original (bit 13) plus every periodic image whose
-//    distance to the box is below fBall2 (the replicas of smooth1.c:283-332,
-//    INTERSECTNP kd.h:102-119, same float arithmetic).
+//  - copies: every scatterer plus each periodic image whose distance to the
+//    box is below fBall2 (the replica scatterers of smooth1.c:283-332, same
+//    float arithmetic as INTERSECTNP, kd.h:102-119).  A copy carries its own
+//    position x_c = fl(x + s L), so the move-field gather is a plain
+//    (non-periodic) ball test from the copy, like smBallGather
+//    (smooth1.c:338-384).  Slots hold
+//        cpos  = (x_c, y_c, z_c, fBall2)
+//        ccoef = (ih2, fNorm*m, rho, iOrder | original-bit)
+//    with ih2 = 4/fBall2 and fNorm = M_1_PI ih2^2 sqrt(ih2) m rounded like
+//    smooth1.c:447-448.
 //  - cut: the heuristic scatterer removal (smooth1.c:460-470, 387-405,
 //    509-513).  fScatDens = min density over copies that reached an active
 //    mover; copies below it go.  On the first step (dark-only input or -fic)
-//    copies that reached no mover count as density 0.  Surviving scatterers
-//    are compacted in place order, which keeps them Morton-sorted.
-//  - prune: kdPruneInactive (kd.c:735-793), stable.
+//    copies that reached no mover count as density 0.  Survivors are
+//    compacted in slot order, which keeps them Morton-sorted.
+//  - prune: kdPruneInactive (kd.c:735-793), stable, then the active movers
+//    are re-sorted by the Morton key of their current positions so that each
+//    warp's movers stay close together as the active set thins out.
 #include <cfloat>
+#include <cstring>
 
 #include "internal.h"
 
@@ -18,145 +27,173 @@ namespace skid {
 
 namespace {
 
-constexpr unsigned ORIG_BIT = 13;
+constexpr unsigned ORIG_FLAG = 0x80000000u;
 
-__global__ void aux_kernel(const float4 *__restrict__ spos, const float *__restrict__ ball2,
-                           int n, float3 L, float3 blo, float3 bhi, int periodic,
-                           float4 *__restrict__ aux, int *d_extra)
+__device__ __forceinline__ unsigned image_mask(float4 p, float b, float3 L, float3 blo, float3 bhi)
 {
-    int extra = 0;
+    unsigned m = 0;
+    for (int ix = -1; ix <= 1; ++ix)
+        for (int iy = -1; iy <= 1; ++iy)
+            for (int iz = -1; iz <= 1; ++iz) {
+                if (!(ix | iy | iz)) continue;
+                float x = fadd(p.x, fmul((float)ix, L.x));
+                float y = fadd(p.y, fmul((float)iy, L.y));
+                float z = fadd(p.z, fmul((float)iz, L.z));
+                float dx = fsub(blo.x, x), dx1 = fsub(x, bhi.x);
+                float dy = fsub(blo.y, y), dy1 = fsub(y, bhi.y);
+                float dz = fsub(blo.z, z), dz1 = fsub(z, bhi.z);
+                float f;
+                if (dx > 0.0f) f = fmul(dx, dx);
+                else if (dx1 > 0.0f) f = fmul(dx1, dx1);
+                else f = 0.0f;
+                if (dy > 0.0f) f = fadd(f, fmul(dy, dy));
+                else if (dy1 > 0.0f) f = fadd(f, fmul(dy1, dy1));
+                if (dz > 0.0f) f = fadd(f, fmul(dz, dz));
+                else if (dz1 > 0.0f) f = fadd(f, fmul(dz1, dz1));
+                if (f < b) m |= 1u << ((ix + 1) * 9 + (iy + 1) * 3 + (iz + 1));
+            }
+    return m;
+}
+
+__global__ void copy_count_kernel(const float4 *__restrict__ spos, const float *__restrict__ ball2,
+                                  int n, float3 L, float3 blo, float3 bhi, int periodic,
+                                  unsigned *__restrict__ masks, int *__restrict__ counts)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned m = periodic ? image_mask(spos[i], ball2[i], L, blo, bhi) : 0u;
+        masks[i] = m;
+        counts[i] = 1 + __popc(m);
+    }
+}
+
+__global__ void copy_write_kernel(const float4 *__restrict__ spos, const float *__restrict__ ball2,
+                                  const float *__restrict__ rho, const int *__restrict__ sidx,
+                                  const unsigned *__restrict__ masks, const int *__restrict__ off,
+                                  int n, float3 L, float4 *__restrict__ cpos,
+                                  float4 *__restrict__ ccoef)
+{
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 p = spos[i];
         float b = ball2[i];
-        unsigned m = 1u << ORIG_BIT;
-        if (periodic) {
-            for (int ix = -1; ix <= 1; ++ix)
-                for (int iy = -1; iy <= 1; ++iy)
-                    for (int iz = -1; iz <= 1; ++iz) {
-                        if (!(ix | iy | iz)) continue;
-                        float x = fadd(p.x, fmul((float)ix, L.x));
-                        float y = fadd(p.y, fmul((float)iy, L.y));
-                        float z = fadd(p.z, fmul((float)iz, L.z));
-                        float dx = fsub(blo.x, x), dx1 = fsub(x, bhi.x);
-                        float dy = fsub(blo.y, y), dy1 = fsub(y, bhi.y);
-                        float dz = fsub(blo.z, z), dz1 = fsub(z, bhi.z);
-                        float f;
-                        if (dx > 0.0f) f = fmul(dx, dx);
-                        else if (dx1 > 0.0f) f = fmul(dx1, dx1);
-                        else f = 0.0f;
-                        if (dy > 0.0f) f = fadd(f, fmul(dy, dy));
-                        else if (dy1 > 0.0f) f = fadd(f, fmul(dy1, dy1));
-                        if (dz > 0.0f) f = fadd(f, fmul(dz, dz));
-                        else if (dz1 > 0.0f) f = fadd(f, fmul(dz1, dz1));
-                        if (f < b) m |= 1u << ((ix + 1) * 9 + (iy + 1) * 3 + (iz + 1));
-                    }
-        }
-        // smooth1.c:447-448: ih2 = 4/fBall2 (float); fNorm = M_1_PI ih2^2 sqrt(ih2) m
         float ih2 = (float)(4.0 / (double)b);
         double dih2 = ih2;
         float fnm = (float)(M_1_PI * dih2 * dih2 * sqrt(dih2) * (double)p.w);
-        aux[i] = make_float4(b, ih2, fnm, __uint_as_float(m));
-        extra += __popc(m) - 1;
+        float r = rho[i];
+        unsigned io = (unsigned)sidx[i];
+        int o = off[i];
+        cpos[o] = make_float4(p.x, p.y, p.z, b);
+        ccoef[o] = make_float4(ih2, fnm, r, __uint_as_float(io | ORIG_FLAG));
+        unsigned m = masks[i];
+        int k = 1;
+        while (m) {
+            int bit = __ffs(m) - 1;
+            m &= m - 1;
+            int ix = bit / 9 - 1, iy = (bit / 3) % 3 - 1, iz = bit % 3 - 1;
+            float x = fadd(p.x, fmul((float)ix, L.x));
+            float y = fadd(p.y, fmul((float)iy, L.y));
+            float z = fadd(p.z, fmul((float)iz, L.z));
+            cpos[o + k] = make_float4(x, y, z, b);
+            ccoef[o + k] = make_float4(ih2, fnm, r, __uint_as_float(io));
+            ++k;
+        }
     }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) extra += __shfl_xor_sync(SKID_FULL, extra, o);
-    if ((threadIdx.x & 31) == 0 && extra) atomicAdd(d_extra, extra);
 }
 
-// Pass 1 of the cut: density floor over touched live copies.
-__global__ void floor_kernel(const float4 *__restrict__ aux, const float *__restrict__ rho,
-                             const unsigned char *__restrict__ touched,
-                             const unsigned *__restrict__ tbits, const int *d_n,
+__global__ void copy_keys_kernel(const float4 *__restrict__ cpos, int n, float3 lo, float3 inv,
+                                 uint64_t *keys, uint32_t *vals)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 q = cpos[i];
+        keys[i] = morton63(make_float3(q.x, q.y, q.z), lo, inv);
+        vals[i] = (uint32_t)i;
+    }
+}
+
+__global__ void copy_permute_kernel(const uint32_t *__restrict__ perm, int n,
+                                    const float4 *__restrict__ a, const float4 *__restrict__ b,
+                                    float4 *__restrict__ a2, float4 *__restrict__ b2)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t j = perm[i];
+        a2[i] = a[j];
+        b2[i] = b[j];
+    }
+}
+
+// Pass 1 of the cut: density floor over touched copies.
+__global__ void floor_kernel(const float4 *__restrict__ ccoef,
+                             const unsigned char *__restrict__ touched, const int *d_n,
                              unsigned *d_floor)
 {
     int n = *d_n;
     unsigned best = 0xffffffffu;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        unsigned alive = __float_as_uint(aux[i].w);
-        unsigned hit = tbits ? (tbits[i] & alive) : (touched[i] ? alive : 0u);
-        if (hit) best = min(best, f2ord(rho[i]));
-    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (touched[i]) best = min(best, f2ord(ccoef[i].z));
 #pragma unroll
     for (int o = 16; o; o >>= 1) best = min(best, __shfl_xor_sync(SKID_FULL, best, o));
     if ((threadIdx.x & 31) == 0 && best != 0xffffffffu) atomicMin(d_floor, best);
 }
 
-// Pass 2: new live masks, keep flags, zeroed first-step densities.
-__global__ void cut_kernel(float4 *__restrict__ aux, const float *__restrict__ rho,
-                           unsigned char *__restrict__ touched, unsigned *__restrict__ tbits,
-                           const int *__restrict__ sidx, const int *d_n, int cap,
-                           const unsigned *d_floor, int nocut, int *__restrict__ keep, int *d_live,
-                           float *__restrict__ final_rho)
+// Pass 2: keep flags, zeroed first-step densities, touched reset.
+__global__ void cut_kernel(const float4 *__restrict__ ccoef, unsigned char *__restrict__ touched,
+                           const int *d_n, int cap, const unsigned *d_floor, int initial,
+                           int nocut, int *__restrict__ keep, float *__restrict__ final_rho)
 {
     int n = *d_n;
     unsigned fl = *d_floor;
     float fScatDens = fl == 0xffffffffu ? 0.0f : ord2f(fl);
-    int live = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
         if (i >= n) { keep[i] = 0; continue; }
-        float4 a = aux[i];
-        unsigned alive = __float_as_uint(a.w);
-        unsigned tb = tbits ? tbits[i] : 0u;
-        unsigned na = alive;
+        float4 c = ccoef[i];
+        bool t = touched[i] != 0;
+        touched[i] = 0;
+        int k = 1;
         if (!nocut) {
-            if (tbits) {
-                if ((tb & (1u << ORIG_BIT)) == 0u && final_rho) final_rho[sidx[i]] = 0.0f;
-                if (fScatDens > 0.0f) na = rho[i] >= fScatDens ? (alive & tb) : 0u;
+            if (initial) {
+                unsigned bits = __float_as_uint(c.w);
+                if (!t && (bits & ORIG_FLAG) && final_rho) final_rho[bits & ~ORIG_FLAG] = 0.0f;
+                // a copy that reached no mover counts as density 0 (smooth1.c:463-470)
+                float r = t ? c.z : 0.0f;
+                k = r >= fScatDens;
             } else {
-                na = rho[i] >= fScatDens ? alive : 0u;
+                k = c.z >= fScatDens;
             }
         }
-        if (tbits) tbits[i] = 0u;
-        else touched[i] = 0;
-        a.w = __uint_as_float(na);
-        aux[i] = a;
-        keep[i] = na != 0u;
-        live += __popc(na);
+        keep[i] = k;
     }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) live += __shfl_xor_sync(SKID_FULL, live, o);
-    if ((threadIdx.x & 31) == 0 && live) atomicAdd(d_live, live);
 }
 
 // Stable compaction into the spare arrays, skipped when nothing was cut.
-__global__ void compact_scat_kernel(const int *__restrict__ keep, const int *__restrict__ pos,
-                                    const int *d_n, const int *d_n2,
-                                    const float4 *__restrict__ spos,
-                                    const float4 *__restrict__ aux, const float *__restrict__ rho,
-                                    const int *__restrict__ sidx, float4 *__restrict__ spos2,
-                                    float4 *__restrict__ aux2, float *__restrict__ rho2,
-                                    int *__restrict__ sidx2)
+__global__ void compact_copies_kernel(const int *__restrict__ keep, const int *__restrict__ pos,
+                                      const int *d_n, const int *d_n2,
+                                      const float4 *__restrict__ cpos,
+                                      const float4 *__restrict__ ccoef, float4 *__restrict__ cpos2,
+                                      float4 *__restrict__ ccoef2)
 {
     int n = *d_n;
     if (*d_n2 == n) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!keep[i]) continue;
         int j = pos[i];
-        spos2[j] = spos[i];
-        aux2[j] = aux[i];
-        rho2[j] = rho[i];
-        sidx2[j] = sidx[i];
+        cpos2[j] = cpos[i];
+        ccoef2[j] = ccoef[i];
     }
 }
 
-// Copy the compacted arrays back and publish the new count.  Runs as one
-// grid after the compaction, so a captured graph always reads the primary
-// arrays.
-__global__ void copyback_scat_kernel(int *d_n, const int *d_n2, float4 *__restrict__ spos,
-                                     float4 *__restrict__ aux, float *__restrict__ rho,
-                                     int *__restrict__ sidx, const float4 *__restrict__ spos2,
-                                     const float4 *__restrict__ aux2,
-                                     const float *__restrict__ rho2,
-                                     const int *__restrict__ sidx2)
+// Copy the compacted arrays back and mark the tree dirty.  A captured graph
+// therefore always reads the primary arrays.
+__global__ void copyback_copies_kernel(const int *d_n, const int *d_n2, float4 *__restrict__ cpos,
+                                       float4 *__restrict__ ccoef,
+                                       const float4 *__restrict__ cpos2,
+                                       const float4 *__restrict__ ccoef2, int *d_dirty)
 {
     int n2 = *d_n2;
     if (n2 == *d_n) return;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += gridDim.x * blockDim.x) {
-        spos[j] = spos2[j];
-        aux[j] = aux2[j];
-        rho[j] = rho2[j];
-        sidx[j] = sidx2[j];
+        cpos[j] = cpos2[j];
+        ccoef[j] = ccoef2[j];
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_dirty = 1;
 }
 
 __global__ void prune_flag_kernel(const float4 *__restrict__ mpos, const float4 *__restrict__ mold,
@@ -180,92 +217,130 @@ __global__ void prune_flag_kernel(const float4 *__restrict__ mpos, const float4 
     }
 }
 
-__global__ void prune_compact_kernel(const int *__restrict__ keep, const int *__restrict__ pos,
+__global__ void init_keys_kernel(int cap, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
+        keys[i] = ~0ull;
+        vals[i] = 0u;
+    }
+}
+
+// Survivors get rOld reset (kd.c:785-789) and the Morton key of their
+// current position at their compacted slot; empty slots keep keys that sort
+// last.
+__global__ void prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ pos,
                                      const int *d_nA, const int *__restrict__ act,
-                                     int *__restrict__ act2, const float4 *__restrict__ mpos,
-                                     float4 *__restrict__ mold)
+                                     const float4 *__restrict__ mpos, float4 *__restrict__ mold,
+                                     float3 lo, float3 inv, uint64_t *__restrict__ keys,
+                                     uint32_t *__restrict__ vals)
 {
     int n = *d_nA;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!keep[i]) continue;
         int m = act[i];
-        act2[pos[i]] = m;
-        mold[m] = mpos[m];
+        float4 p = mpos[m];
+        mold[m] = p;
+        int j = pos[i];
+        keys[j] = morton63(make_float3(p.x, p.y, p.z), lo, inv);
+        vals[j] = (uint32_t)m;
     }
 }
 
-__global__ void copyback_act_kernel(int *d_nA, const int *d_nA2, int *__restrict__ act,
-                                    const int *__restrict__ act2)
+__global__ void act_from_sorted(const uint32_t *__restrict__ vals, const int *d_n2,
+                                int *__restrict__ act)
 {
-    int n2 = *d_nA2;
+    int n2 = *d_n2;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += gridDim.x * blockDim.x)
-        act[j] = act2[j];
+        act[j] = (int)vals[j];
 }
 
 __global__ void set_count_kernel(int *dst, const int *src) { *dst = *src; }
 
-inline int grid_for(int n, int threads = 256)
+float ord_to_float(unsigned u)
 {
-    int b = (n + threads - 1) / threads;
-    int cap = num_sms() * 8;
-    if (b > cap) b = cap;
-    return b < 1 ? 1 : b;
+    unsigned v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &v, 4);
+    return f;
 }
 
 }  // namespace
 
-cudaError_t scatter_aux(const float4 *spos, const float *ball2_sorted, int n, float3 L,
-                        float3 boxlo, float3 boxhi, bool periodic, float4 *aux, int *d_extra,
-                        cudaStream_t st)
+cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rho, const int *sidx,
+                         int ns, float3 L, float3 boxlo, float3 boxhi, bool periodic,
+                         CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st)
 {
-    cudaError_t e = cudaMemsetAsync(d_extra, 0, sizeof(int), st);
-    if (e || n <= 0) return e;
-    aux_kernel<<<grid_for(n), 256, 0, st>>>(spos, ball2_sorted, n, L, boxlo, boxhi,
-                                            periodic ? 1 : 0, aux, d_extra);
+    cudaError_t e;
+    if ((e = dalloc(C.mask, ns)) || (e = dalloc(C.cnt, ns)) || (e = dalloc(C.off, ns)))
+        return e;
+    copy_count_kernel<<<grid_for(ns), 256, 0, st>>>(spos, ball2, ns, L, boxlo, boxhi, periodic ? 1 : 0, C.mask.p, C.cnt.p); skid::note_launch();
+    if ((e = scan_exclusive(C.cnt.p, C.off.p, ns, C.d_n, ss, st))) return e;
+    int nc = 0;
+    if ((e = cudaMemcpyAsync(&nc, C.d_n, sizeof(int), cudaMemcpyDeviceToHost, st))) return e;
+    if ((e = cudaStreamSynchronize(st))) return e;
+    if ((e = C.alloc(nc))) return e;
+    copy_write_kernel<<<grid_for(ns), 256, 0, st>>>(spos, ball2, rho, sidx, C.mask.p, C.off.p, ns, L, C.cpos2.p, C.ccoef2.p); skid::note_launch();
+    // Morton order of the copy positions (replicas lie just outside the box)
+    if ((e = dalloc(ss.k0, nc)) || (e = dalloc(ss.k1, nc)) || (e = dalloc(ss.v0, nc)) ||
+        (e = dalloc(ss.v1, nc)) || (e = dalloc(ss.box, 8)))
+        return e;
+    if ((e = bbox_of(C.cpos2.p, nc, ss.box.p, st))) return e;
+    unsigned hb[6];
+    if ((e = cudaMemcpyAsync(hb, ss.box.p, sizeof(hb), cudaMemcpyDeviceToHost, st))) return e;
+    if ((e = cudaStreamSynchronize(st))) return e;
+    float3 lo = make_float3(ord_to_float(hb[0]), ord_to_float(hb[1]), ord_to_float(hb[2]));
+    float3 hi = make_float3(ord_to_float(hb[3]), ord_to_float(hb[4]), ord_to_float(hb[5]));
+    float ext = fmaxf(fmaxf(hi.x - lo.x, hi.y - lo.y), fmaxf(hi.z - lo.z, 1e-30f));
+    float s = 2097151.0f / ext;
+    copy_keys_kernel<<<grid_for(nc), 256, 0, st>>>(C.cpos2.p, nc, lo, make_float3(s, s, s), ss.k0.p, ss.v0.p); skid::note_launch();
+    if ((e = radix_sort(ss, nc, 63, st))) return e;
+    copy_permute_kernel<<<grid_for(nc), 256, 0, st>>>(ss.v0.p, nc, C.cpos2.p, C.ccoef2.p, C.cpos.p, C.ccoef.p); skid::note_launch();
+    if ((e = cudaMemsetAsync(C.touched.p, 0, C.cap, st))) return e;
+    if ((e = cudaMemsetAsync(C.d_dirty, 0, sizeof(int), st))) return e;
+    *nCopies = nc;
     return cudaGetLastError();
 }
 
-cudaError_t scatter_cut(ScatState &s, bool initial, bool nocut, float *final_rho, SortScratch &ss,
+cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, SortScratch &ss,
                         cudaStream_t st)
 {
     cudaError_t e;
-    int cap = (int)s.spos.n;
-    if ((e = cudaMemsetAsync(s.d_floor, 0xff, sizeof(unsigned), st))) return e;
-    if ((e = cudaMemsetAsync(s.d_live, 0, sizeof(int), st))) return e;
+    int cap = C.cap;
+    if ((e = cudaMemsetAsync(C.d_floor, 0xff, sizeof(unsigned), st))) return e;
     int g = grid_for(cap);
-    floor_kernel<<<g, 256, 0, st>>>(s.saux.p, s.srho.p, s.touched.p, initial ? s.tbits.p : nullptr,
-                                    s.d_nS, s.d_floor);
-    cut_kernel<<<g, 256, 0, st>>>(s.saux.p, s.srho.p, s.touched.p, initial ? s.tbits.p : nullptr,
-                                  s.sidx.p, s.d_nS, cap, s.d_floor, nocut ? 1 : 0, s.keep.p,
-                                  s.d_live, final_rho);
+    floor_kernel<<<g, 256, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, C.d_floor); skid::note_launch();
+    cut_kernel<<<g, 256, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, cap, C.d_floor, initial ? 1 : 0, nocut ? 1 : 0, C.keep.p, final_rho); skid::note_launch();
     if ((e = cudaGetLastError())) return e;
     if (nocut) return cudaSuccess;
-    // stable compaction of the scatterers that keep a live copy
-    if ((e = scan_exclusive(s.keep.p, s.kpos.p, cap, s.d_nS2, ss, st))) return e;
-    compact_scat_kernel<<<g, 256, 0, st>>>(s.keep.p, s.kpos.p, s.d_nS, s.d_nS2, s.spos.p, s.saux.p,
-                                           s.srho.p, s.sidx.p, s.spos2.p, s.saux2.p, s.srho2.p,
-                                           s.sidx2.p);
-    copyback_scat_kernel<<<g, 256, 0, st>>>(s.d_nS, s.d_nS2, s.spos.p, s.saux.p, s.srho.p, s.sidx.p,
-                                            s.spos2.p, s.saux2.p, s.srho2.p, s.sidx2.p);
-    set_count_kernel<<<1, 1, 0, st>>>(s.d_nS, s.d_nS2);
+    if ((e = scan_exclusive(C.keep.p, C.kpos.p, cap, C.d_n2, ss, st))) return e;
+    compact_copies_kernel<<<g, 256, 0, st>>>(C.keep.p, C.kpos.p, C.d_n, C.d_n2, C.cpos.p, C.ccoef.p, C.cpos2.p, C.ccoef2.p); skid::note_launch();
+    copyback_copies_kernel<<<g, 256, 0, st>>>(C.d_n, C.d_n2, C.cpos.p, C.ccoef.p, C.cpos2.p, C.ccoef2.p, C.d_dirty); skid::note_launch();
+    set_count_kernel<<<1, 1, 0, st>>>(C.d_n, C.d_n2); skid::note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t mover_prune(MoverState &m, float3 period, float fCvg, SortScratch &ss, cudaStream_t st)
+cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,
+                        SortScratch &ss, cudaStream_t st)
 {
     cudaError_t e;
-    int cap = (int)m.act.n;
+    int cap = m.cap;
+    // sort scratch for cap keys (allocated on the first, uncaptured call)
+    if ((e = dalloc(ss.k0, cap)) || (e = dalloc(ss.k1, cap)) || (e = dalloc(ss.v0, cap)) ||
+        (e = dalloc(ss.v1, cap)))
+        return e;
     float3 hP = make_float3((float)(0.5 * (double)period.x), (float)(0.5 * (double)period.y),
                             (float)(0.5 * (double)period.z));
     float fCvg2 = fCvg * fCvg;
     int g = grid_for(cap);
-    prune_flag_kernel<<<g, 256, 0, st>>>(m.mpos.p, m.mold.p, m.act.p, m.d_nA, cap, hP, fCvg2,
-                                         m.keep.p);
+    prune_flag_kernel<<<g, 256, 0, st>>>(m.mpos.p, m.mold.p, m.act.p, m.d_nA, cap, hP, fCvg2, m.keep.p); skid::note_launch();
     if ((e = scan_exclusive(m.keep.p, m.kpos.p, cap, m.d_nA2, ss, st))) return e;
-    prune_compact_kernel<<<g, 256, 0, st>>>(m.keep.p, m.kpos.p, m.d_nA, m.act.p, m.act2.p, m.mpos.p,
-                                            m.mold.p);
-    copyback_act_kernel<<<g, 256, 0, st>>>(m.d_nA, m.d_nA2, m.act.p, m.act2.p);
-    set_count_kernel<<<1, 1, 0, st>>>(m.d_nA, m.d_nA2);
+    init_keys_kernel<<<g, 256, 0, st>>>(cap, ss.k0.p, ss.v0.p); skid::note_launch();
+    prune_scatter_kernel<<<g, 256, 0, st>>>(m.keep.p, m.kpos.p, m.d_nA, m.act.p, m.mpos.p, m.mold.p, keylo, keyinv, ss.k0.p, ss.v0.p); skid::note_launch();
+    // an even number of digit passes leaves the result in (k0, v0), so a
+    // captured graph replays consistently
+    if ((e = radix_sort(ss, cap, 64, st))) return e;
+    act_from_sorted<<<g, 256, 0, st>>>(ss.v0.p, m.d_nA2, m.act.p); skid::note_launch();
+    set_count_kernel<<<1, 1, 0, st>>>(m.d_nA, m.d_nA2); skid::note_launch();
     return cudaGetLastError();
 }
 

@@ -4,9 +4,25 @@
 // the digit-major count table, (3) a stable scatter that ranks keys inside
 // the tile with warp match + per-warp digit counts.  Tiles are 4096 keys
 // (256 threads x 16 rounds, round-major so tile order = input order).
+#include <atomic>
+
 #include "internal.h"
 
 namespace skid {
+
+namespace {
+std::atomic<long long> g_launches{0};
+thread_local bool g_capturing = false;
+}  // namespace
+
+void note_launch(int n)
+{
+    if (!g_capturing) g_launches += n;
+}
+
+long long launches_total() { return g_launches.load(); }
+
+void set_capturing(bool on) { g_capturing = on; }
 
 namespace {
 
@@ -66,32 +82,6 @@ __global__ void rs_scatter(const uint64_t *__restrict__ kin, const uint32_t *__r
             run[tid] += s;
         }
         __syncthreads();
-    }
-}
-
-// Single-block exclusive scan of up to a few million uint32 (sequential
-// chunks per thread).
-__global__ void scan_one_block_u32(uint32_t *data, int m)
-{
-    __shared__ uint32_t part[1024];
-    int t = threadIdx.x, T = blockDim.x;
-    int per = (m + T - 1) / T;
-    int b = t * per, e = min(b + per, m);
-    uint32_t s = 0;
-    for (int i = b; i < e; ++i) s += data[i];
-    part[t] = s;
-    __syncthreads();
-    for (int o = 1; o < T; o <<= 1) {
-        uint32_t x = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += x;
-        __syncthreads();
-    }
-    uint32_t run = part[t] - s;
-    for (int i = b; i < e; ++i) {
-        uint32_t x = data[i];
-        data[i] = run;
-        run += x;
     }
 }
 
@@ -205,10 +195,11 @@ cudaError_t radix_sort(SortScratch &s, int n, int bits, cudaStream_t st)
     cudaError_t e = dalloc(s.hist, (size_t)256 * nTiles);
     if (e) return e;
     for (int shift = 0; shift < bits; shift += 8) {
-        rs_histogram<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, n, shift, nTiles, s.hist.p);
-        scan_one_block_u32<<<1, 1024, 0, st>>>(s.hist.p, 256 * nTiles);
+        rs_histogram<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, n, shift, nTiles, s.hist.p); skid::note_launch();
+        e = scan_exclusive((const int *)s.hist.p, (int *)s.hist.p, 256 * nTiles, nullptr, s, st);
+        if (e) return e;
         rs_scatter<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, s.v0.p, s.k1.p, s.v1.p, n, shift, nTiles,
-                                                  s.hist.p);
+                                                  s.hist.p); skid::note_launch();
         std::swap(s.k0, s.k1);
         std::swap(s.v0, s.v1);
     }
@@ -226,9 +217,9 @@ cudaError_t scan_exclusive(const int *in, int *out, int n, int *d_total, SortScr
     if (nb > 512 * 16) return cudaErrorInvalidValue;  // > 33 M entries
     cudaError_t e = dalloc(s.blk, (size_t)nb);
     if (e) return e;
-    scan_tile_sums<<<nb, SC_THREADS, 0, st>>>(in, n, s.blk.p);
-    scan_blocks<<<1, 512, 0, st>>>(s.blk.p, nb, d_total);
-    scan_apply<<<nb, SC_THREADS, 0, st>>>(in, out, n, s.blk.p);
+    scan_tile_sums<<<nb, SC_THREADS, 0, st>>>(in, n, s.blk.p); skid::note_launch();
+    scan_blocks<<<1, 512, 0, st>>>(s.blk.p, nb, d_total); skid::note_launch();
+    scan_apply<<<nb, SC_THREADS, 0, st>>>(in, out, n, s.blk.p); skid::note_launch();
     return cudaGetLastError();
 }
 

@@ -69,24 +69,29 @@ __global__ void gather_sorted(const float4 *__restrict__ p, const uint32_t *__re
 // ball2 (sorted order) builds ball boxes when given; aux (sorted order, x =
 // ball2, w = live-copy mask bits) is the alternative source for refits.
 __global__ void upward_kernel(const float4 *__restrict__ pos, const float *__restrict__ ball2,
-                              const float4 *__restrict__ aux, int n_host, const int *d_n,
+                              const float4 *__restrict__ aux, int ballw, int n_host, const int *d_n,
                               int leafBase, float4 *lo, float4 *hi, float4 *blo, float4 *bhi,
-                              int *flag)
+                              int *flag, const int *d_dirty)
 {
     int leaf = blockIdx.x * blockDim.x + threadIdx.x;
     if (leaf >= leafBase) return;
+    if (d_dirty && !*d_dirty) return;
     int n = d_n ? *d_n : n_host;
     float4 l = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX);
     float4 h = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
     float4 bl = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f);
     float4 bh = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
-    bool balls = (ball2 != nullptr) || (aux != nullptr);
+    // max ball2 (lo.w) needs ball data; ball boxes also need allocated arrays
+    bool hasb = (ball2 != nullptr) || (aux != nullptr) || ballw;
+    bool balls = hasb && blo != nullptr && bhi != nullptr;
     int b = leaf * SKID_LEAF, e = min(b + SKID_LEAF, n);
     for (int i = b; i < e; ++i) {
         float4 q = pos[i];
         float b2 = 0.0f;
         bool live = true;
-        if (aux) {
+        if (ballw) {
+            b2 = q.w;
+        } else if (aux) {
             float4 a = aux[i];
             b2 = a.x;
             live = __float_as_uint(a.w) != 0u;
@@ -96,13 +101,13 @@ __global__ void upward_kernel(const float4 *__restrict__ pos, const float *__res
         if (!live) continue;
         l.x = fminf(l.x, q.x); l.y = fminf(l.y, q.y); l.z = fminf(l.z, q.z);
         h.x = fmaxf(h.x, q.x); h.y = fmaxf(h.y, q.y); h.z = fmaxf(h.z, q.z);
+        if (hasb) l.w = fmaxf(l.w, b2);
         if (balls) {
             // ball radius rounded up so the box contains every d2 < b2 point
             float r = sqrtf(b2) * (1.0f + 1e-6f) + 1e-30f;
             r += 4.8e-7f * (fabsf(q.x) + fabsf(q.y) + fabsf(q.z) + r);
             bl.x = fminf(bl.x, q.x - r); bl.y = fminf(bl.y, q.y - r); bl.z = fminf(bl.z, q.z - r);
             bh.x = fmaxf(bh.x, q.x + r); bh.y = fmaxf(bh.y, q.y + r); bh.z = fmaxf(bh.z, q.z + r);
-            l.w = fmaxf(l.w, b2);
         }
     }
     int node = leafBase + leaf;
@@ -140,7 +145,7 @@ cudaError_t bbox_of(const float4 *pts, int n, unsigned *d_box6, cudaStream_t st)
     if (e) return e;
     int blocks = min((n + 255) / 256, num_sms() * 4);
     if (blocks < 1) blocks = 1;
-    bbox_kernel<<<blocks, 256, 0, st>>>(pts, n, d_box6);
+    bbox_kernel<<<blocks, 256, 0, st>>>(pts, n, d_box6); skid::note_launch();
     return cudaGetLastError();
 }
 
@@ -169,7 +174,7 @@ cudaError_t tree_build(Tree &t, const float4 *pts, int n, bool balls, SortScratc
     if (n > 0) {
         int blocks = min((n + 255) / 256, num_sms() * 8);
         if ((e = morton_order(pts, n, s, st))) return e;
-        gather_sorted<<<blocks, 256, 0, st>>>(pts, s.v0.p, n, t.pos.p, t.perm.p);
+        gather_sorted<<<blocks, 256, 0, st>>>(pts, s.v0.p, n, t.pos.p, t.perm.p); skid::note_launch();
     }
     return tree_refit(t, nullptr, nullptr, nullptr, st);
 }
@@ -184,21 +189,37 @@ cudaError_t morton_order(const float4 *pts, int n, SortScratch &s, cudaStream_t 
     unsigned *dbox = s.box.p;
     if ((e = bbox_of(pts, n, dbox, st))) return e;
     int blocks = min((n + 255) / 256, num_sms() * 8);
-    morton_kernel<<<blocks, 256, 0, st>>>(pts, n, dbox, s.k0.p, s.v0.p);
+    morton_kernel<<<blocks, 256, 0, st>>>(pts, n, dbox, s.k0.p, s.v0.p); skid::note_launch();
     return radix_sort(s, n, 63, st);
 }
 
 cudaError_t tree_refit(Tree &t, const float4 *pos, const float4 *aux, const int *d_n,
-                       cudaStream_t st)
+                       cudaStream_t st, bool ballw, int *d_dirty)
 {
     cudaError_t e = cudaMemsetAsync(t.flag.p, 0, 2 * (size_t)t.leafBase * sizeof(int), st);
     if (e) return e;
     int threads = 128;
     int blocks = (t.leafBase + threads - 1) / threads;
-    upward_kernel<<<blocks, threads, 0, st>>>(pos ? pos : t.pos.p, nullptr, aux, t.n, d_n,
-                                              t.leafBase, t.lo.p, t.hi.p, t.blo.p, t.bhi.p,
-                                              t.flag.p);
-    return cudaGetLastError();
+    bool nb = t.blo.n < 2 * (size_t)t.leafBase || t.bhi.n < 2 * (size_t)t.leafBase;
+    upward_kernel<<<blocks, threads, 0, st>>>(pos ? pos : t.pos.p, nullptr, aux, ballw ? 1 : 0,
+                                              t.n, d_n, t.leafBase, t.lo.p, t.hi.p,
+                                              nb ? nullptr : t.blo.p, nb ? nullptr : t.bhi.p,
+                                              t.flag.p, d_dirty); skid::note_launch();
+    if (d_dirty) e = cudaMemsetAsync(d_dirty, 0, sizeof(int), st);
+    return e ? e : cudaGetLastError();
+}
+
+cudaError_t tree_shape(Tree &t, int n, bool balls)
+{
+    cudaError_t e;
+    t.n = n;
+    t.nLeaf = (n + SKID_LEAF - 1) / SKID_LEAF;
+    t.leafBase = leaf_base_for(n);
+    size_t nodes = 2 * (size_t)t.leafBase;
+    if ((e = dalloc(t.lo, nodes)) || (e = dalloc(t.hi, nodes)) || (e = dalloc(t.flag, nodes)))
+        return e;
+    if (balls && ((e = dalloc(t.blo, nodes)) || (e = dalloc(t.bhi, nodes)))) return e;
+    return cudaSuccess;
 }
 
 }  // namespace skid

@@ -430,7 +430,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     float3 hP = make_float3((float)(0.5 * (double)P.period.x), (float)(0.5 * (double)P.period.y),
                             (float)(0.5 * (double)P.period.z));
     prep_members<<<grid_for(nslots), 256, 0, st>>>(G.members.p, gof, nslots, pos4, vel4, G.rec.p,
-                                                   hP, U.qr.p, U.qv.p);
+                                                   hP, U.qr.p, U.qv.p); skid::note_launch();
     if ((e = cudaMemcpyAsync(U.qid.p, G.members.p, nslots * sizeof(int), cudaMemcpyDeviceToDevice,
                              st)))
         return e;
@@ -439,7 +439,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     float3 hL = make_float3(0.5f * P.period.x, 0.5f * P.period.y, 0.5f * P.period.z);
     scoop_kernel<<<grid_for(ng), 256, 0, st>>>(ut.view(), U.usoft.p, G.rec.p, G.count.p, ng, P.nmax,
                                               fBall2, P.period, hL, P.per, 0, U.scnt.p, nullptr,
-                                              nullptr, nullptr);
+                                              nullptr, nullptr); skid::note_launch();
     if ((e = scan_exclusive(U.scnt.p, U.soff.p, ng, U.cnt.p, ss, st))) return e;
     int nscoop = 0;
     if ((e = cudaMemcpyAsync(&nscoop, U.cnt.p, sizeof(int), cudaMemcpyDeviceToHost, st))) return e;
@@ -449,9 +449,9 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     if (nscoop > 0)
         scoop_kernel<<<grid_for(ng), 256, 0, st>>>(ut.view(), U.usoft.p, G.rec.p, G.count.p, ng,
                                                   P.nmax, fBall2, P.period, hL, P.per, 1, U.scnt.p,
-                                                  U.soff.p, U.slist.p, U.ssoft.p);
+                                                  U.soff.p, U.slist.p, U.ssoft.p); skid::note_launch();
     // potential work items (group, tile)
-    pot_ntiles<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, U.nt.p);
+    pot_ntiles<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, U.nt.p); skid::note_launch();
     if ((e = scan_exclusive(U.nt.p, U.toff.p, ng, U.cnt.p + 1, ss, st))) return e;
     int nitems = 0;
     if ((e = cudaMemcpyAsync(&nitems, U.cnt.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st)))
@@ -459,11 +459,11 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     if ((e = cudaStreamSynchronize(st))) return e;
     if ((e = dalloc(U.items, nitems > 0 ? nitems : 1))) return e;
     if (nitems > 0) {
-        pot_items<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, U.toff.p, U.items.p);
+        pot_items<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, U.toff.p, U.items.p); skid::note_launch();
         int blocks = nitems < num_sms() * 16 ? nitems : num_sms() * 16;
         pot_kernel<<<blocks, POT_TILE, 0, st>>>(U.items.p, U.cnt.p + 1, G.start.p, G.count.p, U.qr.p,
                                                 U.qv.p, U.soff.p, U.scnt.p, U.slist.p, U.ssoft.p,
-                                                P.G, P.plummer, P.scale, U.pot.p);
+                                                P.G, P.plummer, P.scale, U.pot.p); skid::note_launch();
     }
     // removal loop, one block per group
     RemoveArgs A;
@@ -491,7 +491,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     A.nounbind = P.nounbind;
     if ((e = cudaMemsetAsync(d_unbound, 0, sizeof(int), st))) return e;
     int blocks = ng - 1 < num_sms() * 8 ? ng - 1 : num_sms() * 8;
-    if (blocks > 0) remove_kernel<<<blocks, RM_THREADS, 0, st>>>(A);
+    if (blocks > 0) remove_kernel<<<blocks, RM_THREADS, 0, st>>>(A); skid::note_launch();
     return cudaGetLastError();
 }
 

@@ -42,7 +42,8 @@ class Timings(C.Structure):
     _fields_ = [("density_ms", C.c_float), ("moving_ms", C.c_float), ("fof_ms", C.c_float),
                 ("micro_ms", C.c_float), ("groups_ms", C.c_float), ("unbind_ms", C.c_float),
                 ("toosmall_ms", C.c_float), ("gather_launches", C.c_longlong),
-                ("kernel_launches", C.c_longlong)]
+                ("kernel_launches", C.c_longlong), ("field_ms", C.c_double),
+                ("field_bytes", C.c_double)]
 
 
 GROUP_DTYPE = np.dtype([("nMembers", "<i4"), ("fMass", "<f4"), ("rel", "<f4", 3),
@@ -80,6 +81,9 @@ SIGNATURES = {
     "skid_get_moved": [_V, _F],
     "skid_get_final_density": [_V, _F],
     "skid_get_timings": [_V, C.POINTER(Timings)],
+    "skid_stream": [_V, C.POINTER(C.c_void_p)],
+    "skid_restart": [_V],
+    "skid_field_stats": [_V, C.c_int, C.POINTER(C.c_ulonglong)],
     "skid_knn_ball2": [_V, C.c_int, _F, C.c_int, _F],
     "skid_field": [_V, C.c_int, _F, _F],
     "skid_fof_points": [_V, C.c_int, _F, C.c_float, _I, _I],
@@ -103,13 +107,16 @@ def load(path: str = LIB_PATH):
             f.restype = C.c_int
         lib.skid_strerror.argtypes = [C.c_int]
         lib.skid_strerror.restype = C.c_char_p
+        lib.skid_last_cuda_error.argtypes = [C.c_void_p]
+        lib.skid_last_cuda_error.restype = C.c_char_p
         _lib = lib
     return _lib
 
 
 def exported_symbols(path: str = LIB_PATH):
     lib = C.CDLL(path)
-    return {name for name in list(SIGNATURES) + ["skid_strerror"] if hasattr(lib, name)}
+    return {name for name in list(SIGNATURES) + ["skid_strerror", "skid_last_cuda_error"]
+            if hasattr(lib, name)}
 
 
 def _f(a):
@@ -149,7 +156,10 @@ class Context:
     def _call(self, name, *args):
         rc = getattr(self.lib, name)(*args)
         if rc != 0:
-            raise SkidError(rc, name)
+            where = name
+            if rc == -3 and getattr(self, "h", None):
+                where += " [" + self.lib.skid_last_cuda_error(self.h).decode() + "]"
+            raise SkidError(rc, where)
         return rc
 
     def close(self):
@@ -180,6 +190,21 @@ class Context:
         self._call("skid_set_particles", self.h, snap.n_gas, snap.n_dark, snap.n_star,
                    float(snap.time), _f(self._pos), _f(self._vel), _f(self._mass), _f(self._soft),
                    _f(self._temp))
+
+    def restart(self):
+        """Back to the freshly loaded state, particles kept on the device."""
+        self._call("skid_restart", self.h)
+
+    def field_stats(self, enable=True):
+        """Counts so far (nodes, leaves, tests, hits); then restart counting."""
+        out = (C.c_ulonglong * 4)()
+        self._call("skid_field_stats", self.h, int(enable), out)
+        return tuple(int(x) for x in out)
+
+    def stream_ptr(self) -> int:
+        s = C.c_void_p()
+        self._call("skid_stream", self.h, C.byref(s))
+        return s.value or 0
 
     def scatter_active(self, bGasAndDark=False, bGasOnly=False) -> int:
         n = C.c_int()

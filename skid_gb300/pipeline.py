@@ -42,7 +42,10 @@ def _f32(x) -> float:
 
 
 def run(snap: tipsy.Snapshot, opts: Options, ctx: gpu.Context | None = None, log=None,
-        want_density: bool | None = None, want_moved: bool | None = None) -> Result:
+        want_density: bool | None = None, want_moved: bool | None = None,
+        upload: bool = True) -> Result:
+    """upload=False re-runs on the particles already on the context's device
+    (skid_restart) instead of copying the snapshot again."""
     lines = []
 
     def say(s):
@@ -57,7 +60,10 @@ def run(snap: tipsy.Snapshot, opts: Options, ctx: gpu.Context | None = None, log
     t0 = time.perf_counter()
     try:
         say(f"nDark:{snap.n_dark} nGas:{snap.n_gas} nStar:{snap.n_star}")
-        ctx.set_particles(snap)
+        if upload:
+            ctx.set_particles(snap)
+        else:
+            ctx.restart()
         in_type = (DARK if snap.n_dark else 0) | (GAS if snap.n_gas else 0) | (STAR if snap.n_star else 0)
         counts = {}
         rho = moved = None
