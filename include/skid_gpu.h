@@ -38,6 +38,7 @@ extern "C" {
 #define SKID_EOVERFLOW -5   /* an internal capacity was exceeded            */
 #define SKID_ENODEV -6      /* no usable sm_103 device                      */
 #define SKID_ESTATE -7      /* call made in the wrong pipeline state        */
+#define SKID_ETOOLARGE -8   /* request exceeds a fixed (static) capacity     */
 
 #define SKID_SOFT_PLUMMER 1 /* kd.h:24 */
 #define SKID_SOFT_SPLINE 2  /* kd.h:25 */
@@ -186,6 +187,29 @@ int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
 /* The context's CUDA stream (a cudaStream_t), for callers that time or
  * order their own work against the library's (no reference counterpart). */
 int skid_stream(skid_ctx *ctx, void **stream);
+
+/* ---- Allocation-free entry point. ---- */
+
+/* Limits of skid_knn_ball2_noalloc's static scratch. */
+#define SKID_NOALLOC_MAX_POINTS 65536
+#define SKID_NOALLOC_MAX_K 256
+
+/* k-th nearest-neighbour squared distance (self included) of each of n
+ * points among the same points, like skid_knn_ball2, for callers that cannot
+ * allocate device memory (a framework that owns the device allocator; a loop
+ * that cannot afford cudaMalloc's implicit synchronisation).  No reference
+ * counterpart.  d_pos (float[3n]) and d_ball2 (float[n]) are DEVICE pointers
+ * owned by the caller; period[3] is host memory (FLT_MAX: not periodic);
+ * stream is a cudaStream_t (NULL: the default stream) and the call returns
+ * once the work is queued on it.  Every intermediate lives in one
+ * file-scope device array of about 5 MB that each GPU loading the library
+ * keeps until exit; nothing is allocated or freed.  n above
+ * SKID_NOALLOC_MAX_POINTS or k above SKID_NOALLOC_MAX_K returns
+ * SKID_ETOOLARGE.  The first call on a device looks up the array's address
+ * there (make it before any stream capture).  Calls share the array: calls
+ * whose work overlaps on the GPU race. */
+int skid_knn_ball2_noalloc(const float *d_pos, int n, int k, const float period[3],
+                           float *d_ball2, void *stream);
 
 /* ---- Stage probes with explicit inputs (parity tests, adjoint checks). ---- */
 

@@ -327,6 +327,7 @@ const char *skid_strerror(int code)
     case SKID_EOVERFLOW: return "internal capacity exceeded";
     case SKID_ENODEV: return "no usable sm_103 device";
     case SKID_ESTATE: return "call made in the wrong pipeline state";
+    case SKID_ETOOLARGE: return "request exceeds a fixed capacity";
     }
     return "unknown error";
 }
