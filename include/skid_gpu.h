@@ -184,6 +184,13 @@ int skid_get_timings(skid_ctx *ctx, skid_timings *t);
  * the counts so far; the counters then restart from zero. */
 int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
 
+/* Tuning knobs (no reference counterpart).  Names:
+ *   "field_movers_per_warp"  0 = by active count (default), or 32, 8, 1
+ *   "field_g32_min"          active movers at or above which 32 per warp
+ *   "field_g8_min"           active movers at or above which 8 per warp
+ * Returns SKID_EINVAL for an unknown name or value. */
+int skid_set_option(skid_ctx *ctx, const char *name, double value);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that time or
  * order their own work against the library's (no reference counterpart). */
 int skid_stream(skid_ctx *ctx, void **stream);

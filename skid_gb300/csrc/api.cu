@@ -787,6 +787,25 @@ int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4)
     return 0;
 }
 
+int skid_set_option(skid_ctx *ctx, const char *name, double value)
+{
+    if (!ctx || !name) return SKID_EINVAL;
+    int v = (int)value;
+    if (!strcmp(name, "field_movers_per_warp")) {
+        if (v != 0 && v != 1 && v != 8 && v != 32) return SKID_EINVAL;
+        ctx->opt_G = v;
+    } else if (!strcmp(name, "field_g32_min")) {
+        if (v < 0) return SKID_EINVAL;
+        ctx->opt_g32_min = v;
+    } else if (!strcmp(name, "field_g8_min")) {
+        if (v < 0) return SKID_EINVAL;
+        ctx->opt_g8_min = v;
+    } else {
+        return SKID_EINVAL;
+    }
+    return 0;
+}
+
 int skid_stream(skid_ctx *ctx, void **stream)
 {
     if (!ctx || !stream) return SKID_EINVAL;

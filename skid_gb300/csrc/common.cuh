@@ -113,9 +113,8 @@ __device__ __forceinline__ void set_status(unsigned *st, unsigned bit) { atomicO
 __device__ __forceinline__ int next_node(int c)
 {
     // SETNEXT (kd.h:11-15): the next node in depth-first order after the
-    // subtree of c.
-    while (c & 1) c >>= 1;
-    return c + 1;
+    // subtree of c -- drop the trailing one bits, then step right.
+    return (c >> (__ffs(~c) - 1)) + 1;
 }
 
 struct TreeView {

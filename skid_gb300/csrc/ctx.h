@@ -200,10 +200,14 @@ struct skid_ctx {
         return ldexpf(1.0f, S);
     }
     int enqueue_step(float fStep, bool initial, bool nocut, int slot, int G);
+    // Crossovers measured on GB300 with the 2^21-particle workload: per-step
+    // move-field time is lowest with 32 movers per warp above ~450k active
+    // movers, 8 per warp down to ~24k, and one per warp below.
+    int opt_G = 0, opt_g32_min = 450000, opt_g8_min = 24000;
     int movers_per_warp() const
     {
-        // 32 movers per warp while the active set is dense; fewer as it thins
-        return nActive >= 32768 ? 32 : (nActive >= 2048 ? 8 : 1);
+        if (opt_G) return opt_G;
+        return nActive >= opt_g32_min ? 32 : (nActive >= opt_g8_min ? 8 : 1);
     }
     void drop_graphs()
     {

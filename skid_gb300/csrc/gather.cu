@@ -154,6 +154,21 @@ field_kernel(FieldArgs a)
         int mi = a.act[valid ? slot : item * G];
         float4 yp = a.mpos[mi];
         float3 y = make_float3(yp.x, yp.y, yp.z);
+        // bounding box of the warp's movers, for the per-leaf candidate prefilter
+        float3 wlo = valid ? y : make_float3(FLT_MAX, FLT_MAX, FLT_MAX);
+        float3 whi = valid ? y : make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            wlo.x = fminf(wlo.x, __shfl_xor_sync(SKID_FULL, wlo.x, o));
+            wlo.y = fminf(wlo.y, __shfl_xor_sync(SKID_FULL, wlo.y, o));
+            wlo.z = fminf(wlo.z, __shfl_xor_sync(SKID_FULL, wlo.z, o));
+            whi.x = fmaxf(whi.x, __shfl_xor_sync(SKID_FULL, whi.x, o));
+            whi.y = fmaxf(whi.y, __shfl_xor_sync(SKID_FULL, whi.y, o));
+            whi.z = fmaxf(whi.z, __shfl_xor_sync(SKID_FULL, whi.z, o));
+        }
+        // candidates a lane may test: every L-th one starting at its sub-index
+        const unsigned mine = G == 32 ? SKID_FULL
+                              : (G == 8 ? (0x11111111u << sub) : (1u << sub));
         float ax = 0.0f, ay = 0.0f, az = 0.0f;
         int cp = 1;
         for (;;) {
@@ -173,19 +188,28 @@ field_kernel(FieldArgs a)
                 }
                 __syncwarp();
                 ++st_leaves;
+                // prefilter: lane j keeps candidate j if its ball (radius
+                // rounded up) reaches the movers' box; the exact test below
+                // decides, so this only skips candidates that cannot hit
+                bool rel = false;
+                if (lane < cnt) {
+                    float4 c = cpos_s[w][lane];
+                    float r = sqrtf(c.w) * (1.0f + 2e-6f) +
+                              1e-6f * (fabsf(c.x) + fabsf(c.y) + fabsf(c.z)) + 1e-30f;
+                    rel = c.x + r >= wlo.x && c.x - r <= whi.x && c.y + r >= wlo.y &&
+                          c.y - r <= whi.y && c.z + r >= wlo.z && c.z - r <= whi.z;
+                }
+                const unsigned R = __ballot_sync(SKID_FULL, rel) & mine;
                 unsigned mask = 0;
                 if (want) {
-#pragma unroll
-                    for (int i = 0; i < G; ++i) {
-                        int j = sub + i * L;
-                        if (j < cnt) {
-                            float4 c = cpos_s[w][j];
-                            // smBallGather's test (smooth1.c:365-369), from the copy
-                            float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
-                            if (d2 < c.w) mask |= 1u << j;
-                        }
+                    for (unsigned m = R; m; m &= m - 1) {
+                        int j = __ffs(m) - 1;
+                        float4 c = cpos_s[w][j];
+                        // smBallGather's test (smooth1.c:365-369), from the copy
+                        float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
+                        if (d2 < c.w) mask |= 1u << j;
                     }
-                    st_tests += (unsigned)min(G, max(0, (cnt - sub + L - 1) / L));
+                    st_tests += __popc(R);
                 }
                 st_hits += __popc(mask);
                 for (unsigned m = mask; m; m &= m - 1) {

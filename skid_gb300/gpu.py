@@ -84,6 +84,7 @@ SIGNATURES = {
     "skid_stream": [_V, C.POINTER(C.c_void_p)],
     "skid_restart": [_V],
     "skid_field_stats": [_V, C.c_int, C.POINTER(C.c_ulonglong)],
+    "skid_set_option": [_V, C.c_char_p, C.c_double],
     "skid_knn_ball2": [_V, C.c_int, _F, C.c_int, _F],
     "skid_field": [_V, C.c_int, _F, _F],
     "skid_fof_points": [_V, C.c_int, _F, C.c_float, _I, _I],
@@ -194,6 +195,9 @@ class Context:
     def restart(self):
         """Back to the freshly loaded state, particles kept on the device."""
         self._call("skid_restart", self.h)
+
+    def set_option(self, name: str, value: float):
+        self._call("skid_set_option", self.h, name.encode(), float(value))
 
     def field_stats(self, enable=True):
         """Counts so far (nodes, leaves, tests, hits); then restart counting."""
