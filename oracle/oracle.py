@@ -90,6 +90,8 @@ def lib():
         _lib.or_run.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_int, C.c_double,
                                 f, f, f, f, f, i, C.POINTER(Group), C.c_int, f, f, f,
                                 C.POINTER(Result)]
+        _lib.or_run_unbind.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_int, f, f, f, f,
+                                       i, f, C.POINTER(Group), C.c_int, C.POINTER(Result)]
     return _lib
 
 
@@ -175,10 +177,7 @@ def d2(q, c, period=None):
     return float(lib().or_d2(_fp(q), _fp(c), _fp(_period(period))))
 
 
-def run(snap, flags, verbose=False, max_iter=0, stop_after=0):
-    """Run the whole pipeline on a Snapshot with skid-style options (a
-    ``skid_gb300.options.Options``).  Returns a dict of arrays.  stop_after=1
-    stops after the group centres (FoF groups), 2 after unbinding."""
+def _params(flags, verbose=False, max_iter=0, stop_after=0):
     from skid_gb300.options import Options
     o = flags if isinstance(flags, Options) else Options.parse(flags)
     p = Params()
@@ -198,6 +197,25 @@ def run(snap, flags, verbose=False, max_iter=0, stop_after=0):
     p.maxIter = max_iter or o.maxIter
     p.verbose = int(verbose)
     p.stopAfter = int(stop_after)
+    return o, p
+
+
+def _groups(groups, ng):
+    return {
+        "nMembers": np.array([groups[g].nMembers for g in range(ng)], np.int64),
+        "fMass": np.array([groups[g].fMass for g in range(ng)], np.float32),
+        "rCenter": np.array([list(groups[g].rCenter) for g in range(ng)], np.float32),
+        "vcm": np.array([list(groups[g].vcm) for g in range(ng)], np.float32),
+        "rBound": np.array([list(groups[g].rBound) for g in range(ng)], np.float32),
+        "fRadius": np.array([groups[g].fRadius for g in range(ng)], np.float32),
+    }
+
+
+def run(snap, flags, verbose=False, max_iter=0, stop_after=0):
+    """Run the whole pipeline on a Snapshot with skid-style options (a
+    ``skid_gb300.options.Options``).  Returns a dict of arrays.  stop_after=1
+    stops after the group centres (FoF groups), 2 after unbinding."""
+    o, p = _params(flags, verbose, max_iter, stop_after)
     n = snap.n
     pos = np.ascontiguousarray(snap.pos, np.float32)
     vel = np.ascontiguousarray(snap.vel, np.float32)
@@ -216,16 +234,33 @@ def run(snap, flags, verbose=False, max_iter=0, stop_after=0):
                       _fp(rho), _fp(ball2), _fp(moved), C.byref(res))
     if rc:
         raise ValueError(f"oracle run failed: {rc}")
-    ng = res.nGroup + 1
-    gr = {
-        "nMembers": np.array([groups[g].nMembers for g in range(ng)], np.int64),
-        "fMass": np.array([groups[g].fMass for g in range(ng)], np.float32),
-        "rCenter": np.array([list(groups[g].rCenter) for g in range(ng)], np.float32),
-        "vcm": np.array([list(groups[g].vcm) for g in range(ng)], np.float32),
-        "rBound": np.array([list(groups[g].rBound) for g in range(ng)], np.float32),
-        "fRadius": np.array([groups[g].fRadius for g in range(ng)], np.float32),
-    }
+    gr = _groups(groups, res.nGroup + 1)
     return {"grp": grp, "groups": gr, "rho": rho, "ball2": ball2, "moved": moved,
             "nScatterInit": res.nScatterInit, "nExtraScat": res.nExtraScat,
             "nMove": res.nMove, "nIter": res.nIter, "nGroupFoF": res.nGroupFoF,
             "nUnbound": res.nUnbound, "nGroup": res.nGroup, "nScatFinal": res.nScatFinal}
+
+
+def run_unbind(snap, flags, grp, centers=None, verbose=False, stop_after=0):
+    """Unbind-only mode (-unbind): grp holds the input group ids by iOrder,
+    centers is None (centre of mass) or an array (nGroup-1, 6) of rCenter and
+    vcm from a .gtp file.  stop_after=2 stops after unbinding (no too-small)."""
+    o, p = _params(flags, verbose, 0, stop_after)
+    pos = np.ascontiguousarray(snap.pos, np.float32)
+    vel = np.ascontiguousarray(snap.vel, np.float32)
+    mass = np.ascontiguousarray(snap.mass, np.float32)
+    soft = np.ascontiguousarray(snap.soft, np.float32)
+    g = np.array(grp, np.int32)
+    cap = int(g.max(initial=0)) + 2
+    groups = (Group * cap)()
+    cptr = None
+    if centers is not None:
+        c = np.ascontiguousarray(centers, np.float32).reshape(-1, 6)
+        cptr = _fp(c)
+    res = Result()
+    rc = lib().or_run_unbind(C.byref(p), snap.n_gas, snap.n_dark, snap.n_star, _fp(pos), _fp(vel),
+                             _fp(mass), _fp(soft), _ip(g), cptr, groups, cap, C.byref(res))
+    if rc:
+        raise ValueError(f"oracle unbind-only run failed: {rc}")
+    return {"grp": g, "groups": _groups(groups, res.nGroup + 1), "nGroupFoF": res.nGroupFoF,
+            "nUnbound": res.nUnbound, "nGroup": res.nGroup}

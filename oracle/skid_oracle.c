@@ -888,6 +888,131 @@ static void scoop_visit(void *vctx, int j)
     }
 }
 
+/* Unbinding, too-small and group radii (kd.c:1299-1466, 1251-1293,
+ * 1627-1644) over groups G[0..nGroup) whose members grp[] names; shared by
+ * the whole pipeline and the unbind-only mode.  Takes ownership of G. */
+static int finish_run(const or_params *P, int inType, int n, const float *pos, const float *vel,
+                      const float *mass, float *sft, int *grp, or_group *G, int nGroup,
+                      or_group *groups, int cap_groups, or_result *res)
+{
+    /* 9. unbinding (kd.c:1299-1466) */
+    if (P->bEps) for (int i = 0; i < n; ++i) sft[i] = P->fEps;
+    res->nGroupFoF = nGroup - 1;
+    if (P->verbose) printf("Groups before Unbind:%d\n", nGroup - 1);
+    gm_t *order = (gm_t *)malloc((size_t)(n ? n : 1) * sizeof(gm_t));
+    for (int i = 0; i < n; ++i) { order[i].g = grp[i]; order[i].io = i; }
+    qsort(order, (size_t)n, sizeof(gm_t), cmp_gm);
+    int n0 = G[0].nMembers;
+    int *ung = (int *)malloc((size_t)(n0 ? n0 : 1) * sizeof(int));
+    for (int i = 0; i < n0; ++i) ung[i] = order[i].io;
+    ktree st;
+    kt_build(&st, pos, ung, n0);
+    float hx = (float)(0.5 * P->period[0]), hy = (float)(0.5 * P->period[1]),
+          hz = (float)(0.5 * P->period[2]);
+    int nUnbind = 0;
+    int start = n0;
+    int maxn = 1;
+    for (int g = 1; g < nGroup; ++g) if (G[g].nMembers > maxn) maxn = G[g].nMembers;
+    float *qr = (float *)malloc((size_t)maxn * 3 * sizeof(float));
+    float *qv = (float *)malloc((size_t)maxn * 3 * sizeof(float));
+    float *qm = (float *)malloc((size_t)maxn * sizeof(float));
+    float *qs = (float *)malloc((size_t)maxn * sizeof(float));
+    int *qid = (int *)malloc((size_t)maxn * sizeof(int));
+    double *pot = (double *)malloc((size_t)maxn * sizeof(double));
+    int *removed = (int *)malloc((size_t)maxn * sizeof(int));
+    float fScoop2 = P->fScoop * P->fScoop;
+    for (int g = 1; g < nGroup; ++g) {
+        int gn = G[g].nMembers;
+        int s0 = start;
+        start += gn;
+        if (gn >= P->nMaxMembers) continue;
+        for (int i = 0; i < gn; ++i) {
+            int io = order[s0 + i].io;
+            float dx = wrap_h(pos[3 * (size_t)io + 0] - G[g].rel[0], hx);
+            float dy = wrap_h(pos[3 * (size_t)io + 1] - G[g].rel[1], hy);
+            float dz = wrap_h(pos[3 * (size_t)io + 2] - G[g].rel[2], hz);
+            qr[3 * i + 0] = dx; qr[3 * i + 1] = dy; qr[3 * i + 2] = dz;
+            for (int d = 0; d < 3; ++d) qv[3 * i + d] = vel[3 * (size_t)io + d];
+            qm[i] = mass[io];
+            qs[i] = sft[io];
+            qid[i] = io;
+        }
+        /* kdCellPot (grav.c:8-36) */
+        for (int i = 0; i < gn; ++i) pot[i] = 0.0;
+        for (int i = 0; i < gn - 1; ++i) {
+            for (int j = i + 1; j < gn; ++j) {
+                float dx = qr[3 * i + 0] - qr[3 * j + 0];
+                float dy = qr[3 * i + 1] - qr[3 * j + 1];
+                float dz = qr[3 * i + 2] - qr[3 * j + 2];
+                float d2 = (dx * dx + dy * dy) + dz * dz;
+                float dir = pair_pot(d2, qs[i] + qs[j], P->iSoftType);
+                pot[i] += (float)(P->G * qm[j] * dir);
+                pot[j] += (float)(P->G * qm[i] * dir);
+            }
+        }
+        /* kdAddScoopPot: always applied (kd.c:1379-1384 precedence) */
+        if (n0 > 0) {
+            scoop_ctx c = {pos, mass, sft, {G[g].rel[0], G[g].rel[1], G[g].rel[2]}, P->period,
+                           gn, qr, qs, pot, P->G, P->iSoftType};
+            range_rec(&st, 0, G[g].rCenter, fScoop2, P->period, 1, fScoop2, scoop_visit, &c);
+        }
+        float vout[3], bout[3], mout;
+        int left = or_unbind_group(P, inType, gn, qr, qv, qm, qs, qid, pot, G[g].rel,
+                                   vout, &mout, bout, removed);
+        int nrm = gn - left;
+        for (int r = 0; r < nrm; ++r) grp[removed[r]] = 0;
+        nUnbind += nrm;
+        G[g].nMembers = left;
+        G[0].nMembers += nrm;
+        G[g].fMass = mout;
+        for (int d = 0; d < 3; ++d) { G[g].vcm[d] = vout[d]; G[g].rBound[d] = bout[d]; }
+    }
+    kt_free(&st);
+    free(qr); free(qv); free(qm); free(qs); free(qid); free(pot); free(removed); free(ung);
+    free(order);
+    res->nUnbound = nUnbind;
+    if (P->verbose) printf("Number of particles Unbound:%d\n", nUnbind);
+    if (P->stopAfter == 2) {
+        res->nGroup = nGroup - 1;
+        for (int g = 0; g < nGroup && g < cap_groups; ++g) groups[g] = G[g];
+        free(G);
+        return 0;
+    }
+    /* 10. too small (kd.c:1251-1293) */
+    int *map = (int *)malloc((size_t)nGroup * sizeof(int));
+    int ng2 = 1;
+    map[0] = 0;
+    for (int g = 1; g < nGroup; ++g) {
+        if (G[g].nMembers < P->nMinMembers || G[g].nMembers == 0) { map[g] = 0; continue; }
+        map[g] = ng2;
+        G[ng2] = G[g];
+        ++ng2;
+    }
+    for (int i = 0; i < n; ++i) grp[i] = map[grp[i]];
+    free(map);
+    /* radius about the density centre (kd.c:1627-1644) */
+    for (int g = 1; g < ng2; ++g) G[g].fRadius = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        int g = grp[i];
+        if (!g) continue;
+        float fRad = 0.0f;
+        for (int d = 0; d < 3; ++d) {
+            float del = pos[3 * (size_t)i + d] - G[g].rCenter[d];
+            if (del > 0.5 * P->period[d]) del -= P->period[d];
+            if (del <= -0.5 * P->period[d]) del += P->period[d];
+            fRad += del * del;
+        }
+        fRad = (float)sqrt((double)fRad);
+        if (fRad > G[g].fRadius) G[g].fRadius = fRad;
+    }
+    res->nGroup = ng2 - 1;
+    if (P->verbose) printf("Number of Groups:%d\n", ng2 - 1);
+    for (int g = 0; g < ng2 && g < cap_groups; ++g) groups[g] = G[g];
+    free(G);
+    fflush(stdout);
+    return 0;
+}
+
 int or_run(const or_params *P, int nGas, int nDark, int nStar, double time,
            const float *pos, const float *vel, const float *mass, const float *soft,
            const float *temp, int *grp, or_group *groups, int cap_groups, float *rho_out,
@@ -1064,126 +1189,70 @@ int or_run(const or_params *P, int nGas, int nDark, int nStar, double time,
         free(S.rho); free(S.alive); free(S.zeroed);
         return 0;
     }
-    /* 9. unbinding (kd.c:1299-1466) */
-    if (P->bEps) for (int i = 0; i < n; ++i) sft[i] = P->fEps;
-    res->nGroupFoF = nGroup - 1;
-    if (P->verbose) printf("Groups before Unbind:%d\n", nGroup - 1);
-    gm_t *order = (gm_t *)malloc((size_t)(n ? n : 1) * sizeof(gm_t));
-    for (int i = 0; i < n; ++i) { order[i].g = grp[i]; order[i].io = i; }
-    qsort(order, (size_t)n, sizeof(gm_t), cmp_gm);
-    int n0 = G[0].nMembers;
-    int *ung = (int *)malloc((size_t)(n0 ? n0 : 1) * sizeof(int));
-    for (int i = 0; i < n0; ++i) ung[i] = order[i].io;
-    ktree st;
-    kt_build(&st, pos, ung, n0);
-    float hx = (float)(0.5 * P->period[0]), hy = (float)(0.5 * P->period[1]),
-          hz = (float)(0.5 * P->period[2]);
-    int nUnbind = 0;
-    int start = n0;
-    int maxn = 1;
-    for (int g = 1; g < nGroup; ++g) if (G[g].nMembers > maxn) maxn = G[g].nMembers;
-    float *qr = (float *)malloc((size_t)maxn * 3 * sizeof(float));
-    float *qv = (float *)malloc((size_t)maxn * 3 * sizeof(float));
-    float *qm = (float *)malloc((size_t)maxn * sizeof(float));
-    float *qs = (float *)malloc((size_t)maxn * sizeof(float));
-    int *qid = (int *)malloc((size_t)maxn * sizeof(int));
-    double *pot = (double *)malloc((size_t)maxn * sizeof(double));
-    int *removed = (int *)malloc((size_t)maxn * sizeof(int));
-    float fScoop2 = P->fScoop * P->fScoop;
-    for (int g = 1; g < nGroup; ++g) {
-        int gn = G[g].nMembers;
-        int s0 = start;
-        start += gn;
-        if (gn >= P->nMaxMembers) continue;
-        for (int i = 0; i < gn; ++i) {
-            int io = order[s0 + i].io;
-            float dx = wrap_h(pos[3 * (size_t)io + 0] - G[g].rel[0], hx);
-            float dy = wrap_h(pos[3 * (size_t)io + 1] - G[g].rel[1], hy);
-            float dz = wrap_h(pos[3 * (size_t)io + 2] - G[g].rel[2], hz);
-            qr[3 * i + 0] = dx; qr[3 * i + 1] = dy; qr[3 * i + 2] = dz;
-            for (int d = 0; d < 3; ++d) qv[3 * i + d] = vel[3 * (size_t)io + d];
-            qm[i] = mass[io];
-            qs[i] = sft[io];
-            qid[i] = io;
-        }
-        /* kdCellPot (grav.c:8-36) */
-        for (int i = 0; i < gn; ++i) pot[i] = 0.0;
-        for (int i = 0; i < gn - 1; ++i) {
-            for (int j = i + 1; j < gn; ++j) {
-                float dx = qr[3 * i + 0] - qr[3 * j + 0];
-                float dy = qr[3 * i + 1] - qr[3 * j + 1];
-                float dz = qr[3 * i + 2] - qr[3 * j + 2];
-                float d2 = (dx * dx + dy * dy) + dz * dz;
-                float dir = pair_pot(d2, qs[i] + qs[j], P->iSoftType);
-                pot[i] += (float)(P->G * qm[j] * dir);
-                pot[j] += (float)(P->G * qm[i] * dir);
-            }
-        }
-        /* kdAddScoopPot: always applied (kd.c:1379-1384 precedence) */
-        if (n0 > 0) {
-            scoop_ctx c = {pos, mass, sft, {G[g].rel[0], G[g].rel[1], G[g].rel[2]}, P->period,
-                           gn, qr, qs, pot, P->G, P->iSoftType};
-            range_rec(&st, 0, G[g].rCenter, fScoop2, P->period, 1, fScoop2, scoop_visit, &c);
-        }
-        float vout[3], bout[3], mout;
-        int left = or_unbind_group(P, inType, gn, qr, qv, qm, qs, qid, pot, G[g].rel,
-                                   vout, &mout, bout, removed);
-        int nrm = gn - left;
-        for (int r = 0; r < nrm; ++r) grp[removed[r]] = 0;
-        nUnbind += nrm;
-        G[g].nMembers = left;
-        G[0].nMembers += nrm;
-        G[g].fMass = mout;
-        for (int d = 0; d < 3; ++d) { G[g].vcm[d] = vout[d]; G[g].rBound[d] = bout[d]; }
-    }
-    kt_free(&st);
-    free(qr); free(qv); free(qm); free(qs); free(qid); free(pot); free(removed); free(ung);
-    free(order);
-    res->nUnbound = nUnbind;
-    if (P->verbose) printf("Number of particles Unbound:%d\n", nUnbind);
-    if (P->stopAfter == 2) {
-        res->nGroup = nGroup - 1;
-        for (int g = 0; g < nGroup && g < cap_groups; ++g) groups[g] = G[g];
-        free(G);
-        free(mgrp); free(mio); free(mr); free(mold); free(ar); free(act); free(acc);
-        free(spos); free(smass); free(sb2); free(srho); free(rho); free(sidx); free(sft);
-        free(S.rho); free(S.alive); free(S.zeroed);
-        return 0;
-    }
-    /* 10. too small (kd.c:1251-1293) */
-    int *map = (int *)malloc((size_t)nGroup * sizeof(int));
-    int ng2 = 1;
-    map[0] = 0;
-    for (int g = 1; g < nGroup; ++g) {
-        if (G[g].nMembers < P->nMinMembers || G[g].nMembers == 0) { map[g] = 0; continue; }
-        map[g] = ng2;
-        G[ng2] = G[g];
-        ++ng2;
-    }
-    for (int i = 0; i < n; ++i) grp[i] = map[grp[i]];
-    free(map);
-    /* radius about the density centre (kd.c:1627-1644) */
-    for (int g = 1; g < ng2; ++g) G[g].fRadius = 0.0f;
-    for (int i = 0; i < n; ++i) {
-        int g = grp[i];
-        if (!g) continue;
-        float fRad = 0.0f;
-        for (int d = 0; d < 3; ++d) {
-            float del = pos[3 * (size_t)i + d] - G[g].rCenter[d];
-            if (del > 0.5 * P->period[d]) del -= P->period[d];
-            if (del <= -0.5 * P->period[d]) del += P->period[d];
-            fRad += del * del;
-        }
-        fRad = (float)sqrt((double)fRad);
-        if (fRad > G[g].fRadius) G[g].fRadius = fRad;
-    }
-    res->nGroup = ng2 - 1;
-    if (P->verbose) printf("Number of Groups:%d\n", ng2 - 1);
-    for (int g = 0; g < ng2 && g < cap_groups; ++g) groups[g] = G[g];
-    free(G);
+    int rc = finish_run(P, inType, n, pos, vel, mass, sft, grp, G, nGroup, groups, cap_groups, res);
     free(mgrp); free(mio); free(mr); free(mold); free(ar); free(act); free(acc);
     free(spos); free(smass); free(sb2); free(srho); free(rho); free(sidx); free(sft);
     free(S.rho); free(S.alive); free(S.zeroed);
-    fflush(stdout);
-    return 0;
+    return rc;
+}
+
+/* Unbind-only mode (main.c:348-372): kdInGroup (kd.c:920-962) reads the
+ * group ids, kdInitpGroup (kd.c:969-1005) sums the float masses in iOrder
+ * and leaves rel at the largest-iOrder member, kdReadCenter (kd.c:1083-1196)
+ * takes rCenter and vcm from the .gtp records (centers: 6 floats per group
+ * 1..nGroup-1, rCenter then vcm) or, with centers NULL, the float
+ * mass-weighted centre and velocity.  Then unbinding and too-small as in
+ * or_run.  grp[n] is read and rewritten. */
+int or_run_unbind(const or_params *P, int nGas, int nDark, int nStar, const float *pos,
+                  const float *vel, const float *mass, const float *soft, int *grp,
+                  const float *centers, or_group *groups, int cap_groups, or_result *res)
+{
+    int n = nGas + nDark + nStar;
+    memset(res, 0, sizeof(*res));
+    int inType = (nDark ? OR_DARK : 0) | (nGas ? OR_GAS : 0) | (nStar ? OR_STAR : 0);
+    int nGroup = 1;
+    for (int i = 0; i < n; ++i) {
+        if (grp[i] < 0) return -1;
+        if (grp[i] + 1 > nGroup) nGroup = grp[i] + 1;
+    }
+    or_group *G = (or_group *)calloc((size_t)nGroup, sizeof(or_group));
+    for (int i = 0; i < n; ++i) {
+        int g = grp[i];
+        G[g].nMembers++;
+        if (!g) continue;
+        G[g].fMass += mass[i];
+        for (int d = 0; d < 3; ++d) G[g].rel[d] = pos[3 * (size_t)i + d];
+    }
+    if (centers) {
+        for (int g = 1; g < nGroup; ++g)
+            for (int d = 0; d < 3; ++d) {
+                G[g].rCenter[d] = centers[6 * (size_t)(g - 1) + d];
+                G[g].vcm[d] = centers[6 * (size_t)(g - 1) + 3 + d];
+            }
+    } else {
+        for (int i = 0; i < n; ++i) {
+            int g = grp[i];
+            if (!g) continue;
+            for (int d = 0; d < 3; ++d) {
+                float del = pos[3 * (size_t)i + d] - G[g].rel[d];
+                if (del > 0.5 * P->period[d]) del -= P->period[d];
+                if (del <= -0.5 * P->period[d]) del += P->period[d];
+                G[g].rCenter[d] += mass[i] * del;
+                G[g].vcm[d] += mass[i] * vel[3 * (size_t)i + d];
+            }
+        }
+        for (int g = 1; g < nGroup; ++g)
+            for (int d = 0; d < 3; ++d) {
+                G[g].rCenter[d] /= G[g].fMass;
+                G[g].rCenter[d] += G[g].rel[d];
+                if (G[g].rCenter[d] > P->center[d] + 0.5 * P->period[d]) G[g].rCenter[d] -= P->period[d];
+                if (G[g].rCenter[d] <= P->center[d] - 0.5 * P->period[d]) G[g].rCenter[d] += P->period[d];
+                G[g].vcm[d] /= G[g].fMass;
+            }
+    }
+    float *sft = (float *)malloc((size_t)(n ? n : 1) * sizeof(float));
+    memcpy(sft, soft, (size_t)n * sizeof(float));
+    int rc = finish_run(P, inType, n, pos, vel, mass, sft, grp, G, nGroup, groups, cap_groups, res);
+    free(sft);
+    return rc;
 }

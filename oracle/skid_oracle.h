@@ -108,6 +108,13 @@ int or_run(const or_params *par, int nGas, int nDark, int nStar, double time,
            int *grp, or_group *groups, int cap_groups, float *rho, float *ball2,
            float *moved, or_result *res);
 
+/* Unbind-only mode: grp[n] (read and rewritten) holds the input group ids;
+ * centers is NULL or 6 floats (rCenter, vcm) per group 1..max id. */
+int or_run_unbind(const or_params *par, int nGas, int nDark, int nStar,
+                  const float *pos, const float *vel, const float *mass,
+                  const float *soft, int *grp, const float *centers,
+                  or_group *groups, int cap_groups, or_result *res);
+
 /* Unbinding of one group given its members (kd.c:1329-1460).  q arrays are in
  * the group's member order; returns the number of members left. */
 int or_unbind_group(const or_params *par, int inType, int n,

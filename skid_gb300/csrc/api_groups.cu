@@ -153,7 +153,7 @@ int skid_set_groups(skid_ctx *ctx, const int *grp, int nGroup, const skid_group 
     ctx->G.nGroup = nGroup;
     CK(group_order(ctx->grp.p, n, nGroup, ctx->ss, ctx->G, st));
     CK(group_props(ctx->G, ctx->pos4.p, ctx->vel4.p, ctx->pos4.p, ctx->L, ctx->wrap_hi(),
-                   ctx->wrap_lo(), centers == nullptr, false, st));
+                   ctx->wrap_lo(), centers == nullptr, true, st));
     if (centers) {
         DBuf<skid_group> &tmp = ctx->G.rec2;
         if (dalloc(tmp, nGroup)) return ctx->fail(SKID_ENOMEM);

@@ -92,7 +92,7 @@ cudaError_t fof_run(Tree &t, const float4 *pts, int np, const int *mio, int nior
 cudaError_t group_order(const int *grp, int n, int ng, SortScratch &ss, GroupState &G,
                         cudaStream_t st);
 cudaError_t group_props(GroupState &G, const float4 *pos4, const float4 *vel4, const float4 *moved,
-                        float3 L, float3 wrapHi, float3 wrapLo, bool com, bool keep_centre,
+                        float3 L, float3 wrapHi, float3 wrapLo, bool com, bool rel_last,
                         cudaStream_t st);
 cudaError_t too_small(GroupState &G, int *grp, int n, int nmin, int *d_ng, SortScratch &ss,
                       cudaStream_t st);

@@ -5,11 +5,12 @@
 //    kdGroupOrder (kd.c:1205-1245).
 //  - group_props: kdInitpGroup (kd.c:969-1005) + kdCalcCenter
 //    (kd.c:1013-1075): members, mass, reference point rel (the smallest-iOrder
-//    member; the reference takes the last in its array order -- any member
-//    gives the same centre up to rounding), density centre = rel + mean of the
-//    wrapped moved offsets, mass-weighted mean velocity.  With `com` set it is
-//    kdReadCenter's fallback (kd.c:1160-1192): mass-weighted centre of the
-//    input positions.
+//    member after a move; any member gives the same centre up to rounding),
+//    density centre = rel + mean of the wrapped moved offsets, mass-weighted
+//    mean velocity.  With `com` set it is kdReadCenter's fallback
+//    (kd.c:1160-1192): mass-weighted centre of the input positions.  With
+//    `rel_last` rel is the largest-iOrder member, as kdInitpGroup leaves it
+//    when the groups are read from a file (its loop runs in iOrder there).
 //  - too_small: kdTooSmall (kd.c:1251-1293), order-preserving renumbering.
 //  - group_radius: max distance of current members from the centre
 //    (kdWriteGroup, kd.c:1627-1644).
@@ -65,7 +66,7 @@ __global__ void group_props_kernel(const int *__restrict__ start, const int *__r
                                    const int *__restrict__ members, int ng,
                                    const float4 *__restrict__ pos4, const float4 *__restrict__ vel4,
                                    const float4 *__restrict__ moved, float3 L, float3 hL,
-                                   float3 wrapHi, float3 wrapLo, int com, int keep_centre,
+                                   float3 wrapHi, float3 wrapLo, int com, int rel_last,
                                    skid_group *__restrict__ rec)
 {
     int lane = threadIdx.x & 31;
@@ -86,7 +87,7 @@ __global__ void group_props_kernel(const int *__restrict__ start, const int *__r
             }
             continue;
         }
-        float4 rp = pos4[members[s]];
+        float4 rp = pos4[members[rel_last ? s + c - 1 : s]];
         float rel[3] = {rp.x, rp.y, rp.z};
         double m = 0.0, cs[3] = {0, 0, 0}, vs[3] = {0, 0, 0};
         for (int k = s + lane; k < s + c; k += 32) {
@@ -120,15 +121,13 @@ __global__ void group_props_kernel(const int *__restrict__ start, const int *__r
             float Ld[3] = {L.x, L.y, L.z};
             for (int d = 0; d < 3; ++d) {
                 r.rel[d] = rel[d];
-                if (!keep_centre) {
-                    float cc = (float)cs[d];
-                    cc = com ? cc / fm : cc / (float)c;
-                    cc = fadd(cc, rel[d]);
-                    if (cc > wh[d]) cc = fsub(cc, Ld[d]);
-                    if (cc <= wl[d]) cc = fadd(cc, Ld[d]);
-                    r.rCenter[d] = cc;
-                    r.vcm[d] = (float)vs[d] / fm;
-                }
+                float cc = (float)cs[d];
+                cc = com ? cc / fm : cc / (float)c;
+                cc = fadd(cc, rel[d]);
+                if (cc > wh[d]) cc = fsub(cc, Ld[d]);
+                if (cc <= wl[d]) cc = fadd(cc, Ld[d]);
+                r.rCenter[d] = cc;
+                r.vcm[d] = (float)vs[d] / fm;
                 r.rBound[d] = 0.0f;
             }
             r.fRadius = 0.0f;
@@ -223,7 +222,7 @@ cudaError_t group_order(const int *grp, int n, int ng, SortScratch &ss, GroupSta
 }
 
 cudaError_t group_props(GroupState &G, const float4 *pos4, const float4 *vel4, const float4 *moved,
-                        float3 L, float3 wrapHi, float3 wrapLo, bool com, bool keep_centre,
+                        float3 L, float3 wrapHi, float3 wrapLo, bool com, bool rel_last,
                         cudaStream_t st)
 {
     cudaError_t e;
@@ -234,7 +233,7 @@ cudaError_t group_props(GroupState &G, const float4 *pos4, const float4 *vel4, c
     if (blocks < 1) blocks = 1;
     group_props_kernel<<<blocks, 256, 0, st>>>(G.start.p, G.count.p, G.members.p, G.nGroup, pos4,
                                                vel4, moved, L, hL, wrapHi, wrapLo, com ? 1 : 0,
-                                               keep_centre ? 1 : 0, G.rec.p); skid::note_launch();
+                                               rel_last ? 1 : 0, G.rec.p); skid::note_launch();
     return cudaGetLastError();
 }
 

@@ -1,0 +1,308 @@
+/*
+ * TIPSY input and skid output files (see tipsy_io.h).
+ */
+#include "tipsy_io.h"
+
+#include <errno.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define GAS_FLOATS 12
+#define DARK_FLOATS 9
+#define STAR_FLOATS 11
+
+static uint32_t bswap32(uint32_t v)
+{
+    return (v >> 24) | ((v >> 8) & 0xff00u) | ((v << 8) & 0xff0000u) | (v << 24);
+}
+
+static int host_is_little(void)
+{
+    uint32_t one = 1;
+    return *(unsigned char *)&one == 1;
+}
+
+/* Read count 4-byte words (floats or ints); XDR words are big-endian. */
+static int read_words(FILE *fp, void *dst, size_t count, int big)
+{
+    if (fread(dst, 4, count, fp) != count) return -1;
+    if (big == host_is_little()) {
+        uint32_t *w = (uint32_t *)dst;
+        for (size_t i = 0; i < count; ++i) w[i] = bswap32(w[i]);
+    }
+    return 0;
+}
+
+static int write_words(FILE *fp, const void *src, size_t count, int big)
+{
+    if (big != host_is_little()) return fwrite(src, 4, count, fp) == count ? 0 : -1;
+    const uint32_t *w = (const uint32_t *)src;
+    for (size_t i = 0; i < count; ++i) {
+        uint32_t v = bswap32(w[i]);
+        if (fwrite(&v, 4, 1, fp) != 1) return -1;
+    }
+    return 0;
+}
+
+static int read_header(FILE *fp, int standard, double *time, int cnt[5])
+{
+    unsigned char raw[32];
+    if (fread(raw, 1, 32, fp) != 32) return -1;
+    uint64_t t;
+    memcpy(&t, raw, 8);
+    if (standard == host_is_little()) {
+        uint64_t r = 0;
+        for (int i = 0; i < 8; ++i) r = (r << 8) | ((t >> (8 * i)) & 0xff);
+        t = r;
+    }
+    memcpy(time, &t, 8);
+    for (int i = 0; i < 5; ++i) {
+        uint32_t v;
+        memcpy(&v, raw + 8 + 4 * i, 4);
+        if (standard == host_is_little()) v = bswap32(v);
+        cnt[i] = (int)v;
+    }
+    return 0;
+}
+
+static int write_header(FILE *fp, int standard, double time, int nbodies, int nsph, int ndark,
+                        int nstar)
+{
+    unsigned char raw[32];
+    memset(raw, 0, sizeof(raw));
+    uint64_t t;
+    memcpy(&t, &time, 8);
+    if (standard == host_is_little()) {
+        uint64_t r = 0;
+        for (int i = 0; i < 8; ++i) r = (r << 8) | ((t >> (8 * i)) & 0xff);
+        t = r;
+    }
+    memcpy(raw, &t, 8);
+    int v[6] = {nbodies, 3, nsph, ndark, nstar, 0};
+    for (int i = 0; i < 6; ++i) {
+        uint32_t w = (uint32_t)v[i];
+        if (standard == host_is_little()) w = bswap32(w);
+        memcpy(raw + 8 + 4 * i, &w, 4);
+    }
+    return fwrite(raw, 1, 32, fp) == 32 ? 0 : -1;
+}
+
+int tipsy_read(FILE *fp, int standard, snapshot *s, char *err, size_t errlen)
+{
+    memset(s, 0, sizeof(*s));
+    int cnt[5];
+    if (read_header(fp, standard, &s->time, cnt)) {
+        snprintf(err, errlen, "truncated TIPSY header");
+        return -1;
+    }
+    /* cnt: nbodies, ndim, nsph, ndark, nstar */
+    s->nGas = cnt[2];
+    s->nDark = cnt[3];
+    s->nStar = cnt[4];
+    if (s->nGas < 0 || s->nDark < 0 || s->nStar < 0 ||
+        (long long)s->nGas + s->nDark + s->nStar > (1ll << 28)) {
+        snprintf(err, errlen, "bad particle counts in TIPSY header (%d gas, %d dark, %d star)",
+                 s->nGas, s->nDark, s->nStar);
+        return -1;
+    }
+    int n = s->n = s->nGas + s->nDark + s->nStar;
+    size_t m = n > 0 ? (size_t)n : 1;
+    s->pos = malloc(3 * m * sizeof(float));
+    s->vel = malloc(3 * m * sizeof(float));
+    s->mass = malloc(m * sizeof(float));
+    s->soft = malloc(m * sizeof(float));
+    s->temp = calloc(m, sizeof(float));
+    if (!s->pos || !s->vel || !s->mass || !s->soft || !s->temp) {
+        tipsy_free(s);
+        snprintf(err, errlen, "out of host memory");
+        return -1;
+    }
+    float rec[GAS_FLOATS];
+    for (int i = 0; i < n; ++i) {
+        int type = i < s->nGas ? 0 : (i < s->nGas + s->nDark ? 1 : 2);
+        int nf = type == 0 ? GAS_FLOATS : (type == 1 ? DARK_FLOATS : STAR_FLOATS);
+        if (read_words(fp, rec, (size_t)nf, standard)) {
+            snprintf(err, errlen, "truncated TIPSY particle records (particle %d of %d)", i, n);
+            tipsy_free(s);
+            return -1;
+        }
+        /* gas: mass pos[3] vel[3] rho temp hsmooth metals phi
+         * dark: mass pos[3] vel[3] eps phi
+         * star: mass pos[3] vel[3] metals tform eps phi */
+        s->mass[i] = rec[0];
+        for (int d = 0; d < 3; ++d) {
+            s->pos[3 * (size_t)i + d] = rec[1 + d];
+            s->vel[3 * (size_t)i + d] = rec[4 + d];
+        }
+        if (type == 0) {
+            s->temp[i] = rec[8];
+            s->soft[i] = rec[9];
+        } else if (type == 1) {
+            s->soft[i] = rec[7];
+        } else {
+            s->soft[i] = rec[9];
+        }
+    }
+    return 0;
+}
+
+void tipsy_free(snapshot *s)
+{
+    free(s->pos);
+    free(s->vel);
+    free(s->mass);
+    free(s->soft);
+    free(s->temp);
+    memset(s, 0, sizeof(*s));
+}
+
+int tipsy_write_gtp(const char *path, int standard, double time, int nGroup, const float *mass,
+                    const float *pos, const float *vel, const float *radius)
+{
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return -1;
+    int rc = write_header(fp, standard, time, nGroup, 0, 0, nGroup);
+    for (int g = 0; g < nGroup && !rc; ++g) {
+        float rec[STAR_FLOATS];
+        rec[0] = mass[g];
+        for (int d = 0; d < 3; ++d) {
+            rec[1 + d] = pos[3 * (size_t)g + d];
+            rec[4 + d] = vel[3 * (size_t)g + d];
+        }
+        rec[7] = 0.0f;           /* metals */
+        rec[8] = (float)time;    /* tform */
+        rec[9] = radius[g];      /* eps */
+        rec[10] = 0.0f;          /* phi */
+        rc = write_words(fp, rec, STAR_FLOATS, standard);
+    }
+    if (fclose(fp)) rc = -1;
+    return rc;
+}
+
+int tipsy_read_gtp(const char *path, int standard, int *nStar, float **mass, float **pos,
+                   float **vel, char *err, size_t errlen)
+{
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return 0;
+    double t;
+    int cnt[5];
+    if (read_header(fp, standard, &t, cnt) || cnt[2] < 0 || cnt[3] < 0 || cnt[4] < 0) {
+        snprintf(err, errlen, "%s: bad TIPSY header", path);
+        fclose(fp);
+        return -1;
+    }
+    /* skip gas and dark records (kd.c:1121-1128) */
+    if (fseek(fp, (long)cnt[2] * GAS_FLOATS * 4 + (long)cnt[3] * DARK_FLOATS * 4, SEEK_CUR)) {
+        snprintf(err, errlen, "%s: truncated", path);
+        fclose(fp);
+        return -1;
+    }
+    int ns = cnt[4];
+    size_t m = ns > 0 ? (size_t)ns : 1;
+    *mass = malloc(m * sizeof(float));
+    *pos = malloc(3 * m * sizeof(float));
+    *vel = malloc(3 * m * sizeof(float));
+    for (int i = 0; i < ns; ++i) {
+        float rec[STAR_FLOATS];
+        if (read_words(fp, rec, STAR_FLOATS, standard)) {
+            snprintf(err, errlen, "%s: truncated star records", path);
+            fclose(fp);
+            return -1;
+        }
+        (*mass)[i] = rec[0];
+        for (int d = 0; d < 3; ++d) {
+            (*pos)[3 * (size_t)i + d] = rec[1 + d];
+            (*vel)[3 * (size_t)i + d] = rec[4 + d];
+        }
+    }
+    fclose(fp);
+    *nStar = ns;
+    return 1;
+}
+
+/* Fast decimal output for the large text files. */
+static char *put_int(char *p, int v)
+{
+    char tmp[16];
+    int k = 0;
+    unsigned u = v < 0 ? (unsigned)(-(long long)v) : (unsigned)v;
+    if (v < 0) *p++ = '-';
+    do { tmp[k++] = (char)('0' + u % 10); u /= 10; } while (u);
+    while (k) *p++ = tmp[--k];
+    *p++ = '\n';
+    return p;
+}
+
+int write_grp(const char *path, int n, const int *grp)
+{
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -1;
+    size_t cap = 1 << 20;
+    char *buf = malloc(cap + 32);
+    char *p = buf;
+    p = put_int(p, n);
+    for (int i = 0; i < n; ++i) {
+        p = put_int(p, grp[i]);
+        if ((size_t)(p - buf) > cap) { fwrite(buf, 1, (size_t)(p - buf), fp); p = buf; }
+    }
+    fwrite(buf, 1, (size_t)(p - buf), fp);
+    free(buf);
+    return fclose(fp) ? -1 : 0;
+}
+
+int write_den(const char *path, int n, const float *rho)
+{
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -1;
+    fprintf(fp, "%d\n", n);
+    for (int i = 0; i < n; ++i) fprintf(fp, "%.10g\n", rho[i]);
+    return fclose(fp) ? -1 : 0;
+}
+
+int write_ray(const char *path, const snapshot *s, const float *moved, const int *moved_flag,
+              const float period[3])
+{
+    FILE *fp = fopen(path, "w");
+    if (!fp) return -1;
+    fprintf(fp, "%d\n", s->n);
+    for (int d = 0; d < 3; ++d) {
+        float h = (float)(0.5 * (double)period[d]);
+        for (int i = 0; i < s->n; ++i) {
+            if (!moved_flag[i]) {
+                fprintf(fp, "0\n");
+                continue;
+            }
+            float dx = moved[3 * (size_t)i + d] - s->pos[3 * (size_t)i + d];
+            if (dx > h) dx -= 2 * h;
+            if (dx <= -h) dx += 2 * h;
+            fprintf(fp, "%g\n", dx);
+        }
+    }
+    return fclose(fp) ? -1 : 0;
+}
+
+int read_grp(const char *path, int **grp, char *err, size_t errlen)
+{
+    FILE *fp = fopen(path, "r");
+    if (!fp) {
+        snprintf(err, errlen, "ERROR: Could not open file:%s", path);
+        return -1;
+    }
+    int n = 0;
+    if (fscanf(fp, "%d", &n) != 1 || n < 0) {
+        snprintf(err, errlen, "%s: bad particle count", path);
+        fclose(fp);
+        return -1;
+    }
+    *grp = malloc((size_t)(n > 0 ? n : 1) * sizeof(int));
+    for (int i = 0; i < n; ++i) {
+        if (fscanf(fp, "%d", &(*grp)[i]) != 1) {
+            snprintf(err, errlen, "%s: truncated after %d of %d ids", path, i, n);
+            fclose(fp);
+            return -1;
+        }
+    }
+    fclose(fp);
+    return n;
+}

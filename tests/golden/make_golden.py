@@ -5,7 +5,12 @@
 The reference binary is oracle/_ref/skid (built from the reference sources by
 oracle/build_ref.sh).  Each case stores its input snapshot (native TIPSY),
 the flags, the reference's stdout lines and its output files
-(.grp/.gtp/.den/.stat/.ray as the flags ask).  The fixtures are what the GPU
+(.grp/.gtp/.den/.stat/.ray as the flags ask).  The unbind-only cases
+(-unbind) reuse another case's input snapshot ("input_from") and take that
+case's reference .grp (and .gtp, when "with_gtp") as their group input,
+stored beside them as in.grp / in.gtp.  The reference writes the native
+TIPSY header's four pad bytes uninitialised, so a regenerated ref.gtp can
+differ from the stored one in bytes 28-31 only.  The fixtures are what the GPU
 tests compare against on machines where the reference is not present.
 """
 import json
@@ -49,6 +54,16 @@ CASES = {
 }
 
 
+# name: (source case, with_gtp, flags); "-unbind" names the stored in.grp
+UNBIND_CASES = {
+    "dark4k_unbind_gtp": ("dark4k_nu", True,
+                          ["-tau", "0.02", "-m", "8", "-p", "1", "-H", H1, "-unbind", "in",
+                           "-stats"]),
+    "mixed6k_unbind_com": ("mixed6k", False,
+                           ["-tau", "0.02", "-m", "8", "-p", "1", "-H", H1, "-unbind", "in.grp"]),
+}
+
+
 def make_input(name):
     n, nh, dex, r200, frac, seed, gas_frac, n_star, _ = CASES[name]
     spec = synth.HaloSpec(n, nh, dex, (5.0, 15.0), r200, frac, seed, gas_frac=gas_frac)
@@ -87,6 +102,38 @@ def main():
         with open(os.path.join(d, "case.json"), "w") as f:
             json.dump(meta, f, indent=1)
         print(name, snap.n, [l for l in lines if not l.startswith(("Ittr", "Micro"))])
+    for name, (src, with_gtp, flags) in UNBIND_CASES.items():
+        d = os.path.join(HERE, name)
+        sd = os.path.join(HERE, src)
+        os.makedirs(d, exist_ok=True)
+        shutil.copy(os.path.join(sd, "ref.grp"), os.path.join(d, "in.grp"))
+        if with_gtp:
+            shutil.copy(os.path.join(sd, "ref.gtp"), os.path.join(d, "in.gtp"))
+        elif os.path.exists(os.path.join(d, "in.gtp")):
+            os.remove(os.path.join(d, "in.gtp"))
+        with open(os.path.join(sd, "case.json")) as f:
+            smeta = json.load(f)
+        with tempfile.TemporaryDirectory() as tmp:
+            for ext in ("grp", "gtp"):
+                if os.path.exists(os.path.join(d, "in." + ext)):
+                    shutil.copy(os.path.join(d, "in." + ext), os.path.join(tmp, "in." + ext))
+            with open(os.path.join(sd, "input.bin"), "rb") as f:
+                r = subprocess.run([ref, *flags, "-o", "ref"], stdin=f, cwd=tmp,
+                                   capture_output=True, text=True, check=True)
+            outs = []
+            for ext in ("grp", "gtp", "stat"):
+                p = os.path.join(tmp, "ref." + ext)
+                if os.path.exists(p):
+                    shutil.copy(p, os.path.join(d, "ref." + ext))
+                    outs.append(ext)
+        lines = [l for l in r.stdout.splitlines()
+                 if not l.startswith(("SKID", "   ")) and "Time" not in l]
+        meta = {"flags": flags, "n": smeta["n"], "n_gas": smeta["n_gas"],
+                "n_dark": smeta["n_dark"], "n_star": smeta["n_star"], "outputs": outs,
+                "stdout": lines, "input_from": src, "warnings": r.stderr.splitlines()}
+        with open(os.path.join(d, "case.json"), "w") as f:
+            json.dump(meta, f, indent=1)
+        print(name, smeta["n"], lines)
 
 
 if __name__ == "__main__":

@@ -18,7 +18,8 @@ def load(name):
     d = os.path.join(GOLDEN, name)
     with open(os.path.join(d, "case.json")) as f:
         meta = json.load(f)
-    snap = tipsy.read_tipsy(os.path.join(d, "input.bin"))
+    src = os.path.join(GOLDEN, meta["input_from"]) if "input_from" in meta else d
+    snap = tipsy.read_tipsy(os.path.join(src, "input.bin"))
     ref = {"grp": tipsy.read_grp(os.path.join(d, "ref.grp")),
            "gtp": tipsy.read_gtp(os.path.join(d, "ref.gtp"))}
     if "den" in meta["outputs"]:
@@ -26,6 +27,8 @@ def load(name):
     if "stat" in meta["outputs"]:
         ref["stat"] = tipsy.read_stat(os.path.join(d, "ref.stat"))
     opts = Options.parse(meta["flags"])
+    if opts.bUnbindOnly:
+        opts.achGroup = os.path.join(d, opts.achGroup)
     counts = {}
     for line in meta["stdout"]:
         for key, tag in (("nExtraScat", "nExtraScat:"), ("nGroupFoF", "Groups before Unbind:"),
@@ -36,9 +39,29 @@ def load(name):
     return snap, opts, ref, counts, meta
 
 
-def check_catalogue(grp, groups, ref, opts, min_agree=0.999, tol_pos=2e-5):
+def unbind_inputs(opts):
+    """Group ids and (n-1, 6) centres (rCenter, vcm; None without a .gtp) of
+    an unbind-only case, read the way kdInGroup/kdReadCenter read them."""
+    base = opts.achGroup[:-4] if opts.achGroup.endswith(".grp") else opts.achGroup
+    grp = tipsy.read_grp(base + ".grp")
+    centers = None
+    if os.path.exists(base + ".gtp"):
+        star = tipsy.read_gtp(base + ".gtp", standard=opts.bStandard)
+        centers = np.concatenate([star["pos"], star["vel"]], axis=1).astype(np.float32)
+    return grp, centers
+
+
+def check_catalogue(grp, groups, ref, opts, min_agree=0.999, tol_pos=None):
     """Per-particle agreement, same groups above -m, and matched .gtp records.
-    groups: dict-like with fMass, rCenter, vcm, fRadius indexed by group id."""
+    groups: dict-like with fMass, rCenter, vcm, fRadius indexed by group id.
+
+    A density centre is the mean of the members' final moved positions, and
+    each of those is only defined to within the last step's size: summing
+    the move field in another order (the reference sums in tree order, the
+    GPU per lane) changes where a particle stops by a fraction of fStep.  The
+    default centre tolerance is therefore 2 % of fStep."""
+    if tol_pos is None:
+        tol_pos = 0.02 * opts.fStep
     m = compare.match_groups(ref["grp"], grp)
     assert m.agreement >= min_agree, f"agreement {m.agreement:.5f}"
     assert m.same_groups(), f"unmatched groups ref={m.unmatched_a} new={m.unmatched_b}"

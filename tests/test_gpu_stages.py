@@ -60,7 +60,10 @@ def test_unbind_isolated(gpu_ready, name):
     from skid_gb300 import gpu
     snap, opts, ref, counts, meta = gc.load(name)
     r1 = oracle.run(snap, opts, stop_after=1)
-    r2 = oracle.run(snap, opts, stop_after=2)
+    # the groups go in as in unbind-only mode (each group's reference point is
+    # then its largest-iOrder member), so the oracle runs that mode too
+    centers = np.concatenate([r1["groups"]["rCenter"][1:], r1["groups"]["vcm"][1:]], axis=1)
+    r2 = oracle.run_unbind(snap, opts, r1["grp"], centers, stop_after=2)
     ng = r1["nGroupFoF"]
     cen = np.zeros(ng + 1, gpu.GROUP_DTYPE)
     cen["rCenter"] = r1["groups"]["rCenter"]

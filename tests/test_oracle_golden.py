@@ -9,6 +9,14 @@ from tests import golden_cases as gc
 @pytest.mark.parametrize("name", gc.names())
 def test_oracle_matches_reference(name):
     snap, opts, ref, counts, meta = gc.load(name)
+    if opts.bUnbindOnly:
+        grp, centers = gc.unbind_inputs(opts)
+        r = oracle.run_unbind(snap, opts, grp, centers)
+        gc.check_catalogue(r["grp"], r["groups"], ref, opts)
+        assert r["nGroupFoF"] == counts["nGroupFoF"]
+        assert r["nUnbound"] == counts["nUnbound"]
+        assert r["nGroup"] == counts["nGroup"]
+        return
     r = oracle.run(snap, opts)
     gc.check_catalogue(r["grp"], r["groups"], ref, opts)
     if "nExtraScat" in counts:
