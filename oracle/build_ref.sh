@@ -4,7 +4,9 @@
 # the binaries are the oracle's reference leg and never part of the product.
 #
 #   oracle/_ref/skid       reference skid, as shipped
-#   oracle/_ref/skid_nsp   built by build_ref_nsp.sh (patched oracle for -nsp)
+#   oracle/_ref/skid_nsp   patched oracle for -nsp (every scatterer kept; see
+#                          oracle/nsp_shim.c), built without editing or
+#                          copying a reference source file
 #
 # The only missing dependency is SunRPC/tirpc XDR; oracle/xdr_shim provides
 # the handful of XDR routines the reference calls.  -ffp-contract=off keeps
@@ -26,3 +28,17 @@ gcc $CFLAGS -o "$OUT/skid" \
     "$REF/cosmo.c" "$REF/romberg.c" "$REF/runge.c" \
     "$HERE/xdr_shim/xdr_shim.c" -lm
 echo "build_ref: built $OUT/skid"
+# -nsp oracle: smooth1.c as a shared object (-fPIC leaves its global
+# functions interposable, so its call to ScatterCut goes through the PLT);
+# the executable exports its own ScatterCut from nsp_shim.c (-rdynamic) and
+# the dynamic linker binds the call there.  main.c alone is compiled with
+# bAllowInitialCut renamed to the shim's nsp_no_initial_cut.
+TMPO=$(mktemp -d)
+trap 'rm -rf "$TMPO"' EXIT
+gcc $CFLAGS -fPIC -fno-inline -shared -o "$OUT/libsmooth1_nsp.so" "$REF/smooth1.c"
+gcc $CFLAGS -DbAllowInitialCut=nsp_no_initial_cut -c -o "$TMPO/main_nsp.o" "$REF/main.c"
+gcc $CFLAGS -rdynamic -o "$OUT/skid_nsp" "$TMPO/main_nsp.o" \
+    "$REF/kd.c" "$REF/grav.c" "$REF/cosmo.c" "$REF/romberg.c" "$REF/runge.c" \
+    "$HERE/xdr_shim/xdr_shim.c" "$HERE/nsp_shim.c" \
+    -L"$OUT" -lsmooth1_nsp -Wl,-rpath,'$ORIGIN' -lm
+echo "build_ref: built $OUT/skid_nsp"

@@ -3,7 +3,8 @@
     python tests/golden/make_golden.py [path/to/reference/skid]
 
 The reference binary is oracle/_ref/skid (built from the reference sources by
-oracle/build_ref.sh).  Each case stores its input snapshot (native TIPSY),
+oracle/build_ref.sh); cases with -nsp, which v1.4.1 lacks, run the patched
+oracle/_ref/skid_nsp (every scatterer kept) without the flag.  Each case stores its input snapshot (native TIPSY),
 the flags, the reference's stdout lines and its output files
 (.grp/.gtp/.den/.stat/.ray as the flags ask).  The unbind-only cases
 (-unbind) reuse another case's input snapshot ("input_from") and take that
@@ -51,6 +52,9 @@ CASES = {
                             "-e", "0.002", "-maxgroup", "300", "-H", H1, "-stats"]),
     "dark4k_nu": (4096, 8, 1.5, 0.08, 0.6, 107, 0.0, 0,
                   ["-tau", "0.02", "-s", "32", "-m", "8", "-p", "1", "-nu", "-H", H1]),
+    "dark6k_nsp": (6144, 12, 1.5, 0.07, 0.6, 108, 0.0, 0,
+                   ["-tau", "0.016", "-s", "64", "-m", "8", "-p", "1", "-nsp", "-O", "0.3",
+                    "-Lambda", "0.7", "-H", H3, "-den", "-stats"]),
 }
 
 
@@ -85,9 +89,13 @@ def main():
         os.makedirs(d, exist_ok=True)
         inp = os.path.join(d, "input.bin")
         synth.write_snapshot(inp, snap)
+        exe, rflags = ref, flags
+        if "-nsp" in flags:
+            exe = os.path.join(os.path.dirname(ref), "skid_nsp")
+            rflags = [f for f in flags if f != "-nsp"]
         with tempfile.TemporaryDirectory() as tmp:
             with open(inp, "rb") as f:
-                r = subprocess.run([ref, *flags, "-o", "ref"], stdin=f, cwd=tmp,
+                r = subprocess.run([exe, *rflags, "-o", "ref"], stdin=f, cwd=tmp,
                                    capture_output=True, text=True, check=True)
             outs = []
             for ext in ("grp", "gtp", "den", "stat", "ray"):

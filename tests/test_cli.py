@@ -70,7 +70,7 @@ def _flags_for(meta, case_dir):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["dark4k_periodic", "mixed6k", "dark8k_lcdm", "dark4k_unbind_gtp",
+@pytest.mark.parametrize("name", ["dark4k_periodic", "mixed6k", "dark8k_lcdm", "dark6k_nsp", "dark4k_unbind_gtp",
                                   "mixed6k_unbind_com"])
 def test_cli_vs_reference(gpu_ready, cli, tmp_path, name):
     from skid_gb300 import tipsy
