@@ -195,6 +195,43 @@ int skid_set_option(skid_ctx *ctx, const char *name, double value);
  * order their own work against the library's (no reference counterpart). */
 int skid_stream(skid_ctx *ctx, void **stream);
 
+/* ---- Adjoints (no reference counterpart). ---- */
+
+#define SKID_ADJ_RECOMPUTE 0   /* find the neighbour pairs by walking the tree again */
+#define SKID_ADJ_STORED 1      /* gather every ball's members once and reuse the lists */
+#define SKID_ADJ_AUTO 2        /* stored while the lists fit in a quarter of the free
+                                  device memory, else recomputed */
+
+/* Gradient of L = sum_i w_i rho_i (rho the symmetric SPH density of
+ * skid_density, smooth1.c:132-276) with respect to the scatterer positions,
+ * the neighbour sets of skid_density held fixed: pair terms in both balls
+ * that hold a pair, plus each smoothing length's dependence on its k-th
+ * neighbour (h_i = |x_i - x_K(i)|/2).  w[n] by iOrder (non-scatterers'
+ * entries unused); dLdx[3n] by iOrder (0 for non-scatterers).  FP32
+ * arithmetic and accumulation.  SKID_ADJ_STORED keeps n_scatter*(nSmooth+16)
+ * indices on the device until the next skid_density; SKID_ADJ_RECOMPUTE
+ * stores nothing.  Needs nSmooth >= 2.  Call after skid_density (any later
+ * stage). */
+int skid_density_adjoint(skid_ctx *ctx, const float *w, float *dLdx, int mode);
+
+/* Query-position adjoint of the density field of the live scatterer copies,
+ * rho_f(y) = sum_c m_c W(|y - x_c|, h_c): dLdy[3i] = w[i] grad rho_f(y_i)
+ * for nm points y (mpos[3nm]).  The move field of smAccDensity
+ * (smooth1.c:436-508) is -grad rho_f: the move kernel is this adjoint with a
+ * unit cotangent, fused with the step. */
+int skid_field_adjoint(skid_ctx *ctx, int nm, const float *mpos, const float *w, float *dLdy);
+
+/* Potential energy of groups and its gradient.  For the nSel groups sel[]
+ * (ids of the grouping made by skid_group_centers or skid_set_groups; call
+ * before skid_unbind), E[s] = -1/2 sum_{i != j in g} G m_i m_j
+ * psi(r_ij, eps_i + eps_j) with kdCellPot's pair potential (grav.c:8-36,
+ * grav.h:11-31) on coordinates relative to the group's reference point
+ * (kd.c:1338-1352); FP32 pair sums, FP64 group totals.  With dLdx non-NULL,
+ * dLdx[3n] (by iOrder) receives sum_s v[s] dE[s]/dx (0 outside the selected
+ * groups). */
+int skid_potential_adjoint(skid_ctx *ctx, int iSoftType, float G, int nSel, const int *sel,
+                           const float *v, double *E, float *dLdx);
+
 /* ---- Allocation-free entry point. ---- */
 
 /* Limits of skid_knn_ball2_noalloc's static scratch. */

@@ -90,6 +90,9 @@ def lib():
         _lib.or_run.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_int, C.c_double,
                                 f, f, f, f, f, i, C.POINTER(Group), C.c_int, f, f, f,
                                 C.POINTER(Result)]
+        _lib.or_density_adjoint_check.argtypes = [C.c_int, f, f, f, C.c_int, f, C.c_int, i,
+                                                  C.c_double, d, d, d, i]
+        _lib.or_field_grad_check.argtypes = [C.c_int, f, f, f, f, C.c_int, f, C.c_double, d, d, d]
         _lib.or_run_unbind.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_int, f, f, f, f,
                                        i, f, C.POINTER(Group), C.c_int, C.POINTER(Result)]
     return _lib
@@ -264,3 +267,37 @@ def run_unbind(snap, flags, grp, centers=None, verbose=False, stop_after=0):
         raise ValueError(f"oracle unbind-only run failed: {rc}")
     return {"grp": g, "groups": _groups(groups, res.nGroup + 1), "nGroupFoF": res.nGroupFoF,
             "nUnbound": res.nUnbound, "nGroup": res.nGroup}
+
+
+def density_adjoint_check(pos, mass, w, k, period, sel, h=1e-6):
+    """FP64 gradient of L = sum w_i rho_i at particles sel: (analytic, central
+    differences of step h, sum of |term|), neighbour sets held fixed."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    mass = np.ascontiguousarray(mass, np.float32)
+    w = np.ascontiguousarray(w, np.float32)
+    sel = np.ascontiguousarray(sel, np.int32)
+    an = np.empty((len(sel), 3))
+    fd = np.empty((len(sel), 3))
+    ab = np.empty(len(sel))
+    ok = C.c_int(0)
+    rc = lib().or_density_adjoint_check(len(pos), _fp(pos), _fp(mass), _fp(w), int(k),
+                                        _fp(_period(period)), len(sel), _ip(sel), h, _dp(an),
+                                        _dp(fd), _dp(ab), C.byref(ok))
+    if rc:
+        raise ValueError(f"density adjoint check failed: {rc} (lists_ok={ok.value})")
+    return an, fd, ab
+
+
+def field_grad_check(spos, smass, sball2, period, ypos, h=1e-6):
+    """FP64 gradient of the density field at ypos: (analytic, central
+    differences, sum of |term|)."""
+    spos = np.ascontiguousarray(spos, np.float32)
+    smass = np.ascontiguousarray(smass, np.float32)
+    sball2 = np.ascontiguousarray(sball2, np.float32)
+    ypos = np.ascontiguousarray(ypos, np.float32)
+    an = np.empty((len(ypos), 3))
+    fd = np.empty((len(ypos), 3))
+    ab = np.empty(len(ypos))
+    lib().or_field_grad_check(len(spos), _fp(spos), _fp(smass), _fp(sball2), _fp(_period(period)),
+                              len(ypos), _fp(ypos), h, _dp(an), _dp(fd), _dp(ab))
+    return an, fd, ab

@@ -1256,3 +1256,244 @@ int or_run_unbind(const or_params *P, int nGas, int nDark, int nStar, const floa
     free(sft);
     return rc;
 }
+
+/* ------------------------------------------------------------------ */
+/* FP64 references for the adjoint checks (no reference counterpart:  */
+/* skid never differentiates its density).                             */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    int *v;
+    int n, cap;
+} ivec;
+
+static void ivec_push(ivec *a, int x)
+{
+    if (a->n == a->cap) {
+        a->cap = a->cap ? 2 * a->cap : 256;
+        a->v = (int *)realloc(a->v, (size_t)a->cap * sizeof(int));
+    }
+    a->v[a->n++] = x;
+}
+
+static void list_visit(void *ctx, int j) { ivec_push((ivec *)ctx, j); }
+
+/* M4 kernel profile f(q), f'(q), for q < 2 (0 beyond). */
+static void m4(double q, double *f, double *fp)
+{
+    if (q < 1.0) {
+        *f = 1.0 - 1.5 * q * q + 0.75 * q * q * q;
+        *fp = -3.0 * q + 2.25 * q * q;
+    } else if (q < 2.0) {
+        double t = 2.0 - q;
+        *f = 0.25 * t * t * t;
+        *fp = -0.75 * t * t;
+    } else {
+        *f = 0.0;
+        *fp = 0.0;
+    }
+}
+
+static double dmin_image(double d, float L)
+{
+    if (L < 0.25f * FLT_MAX) {
+        if (d > 0.5 * L) d -= L;
+        if (d < -0.5 * L) d += L;
+    }
+    return d;
+}
+
+typedef struct {
+    int n;
+    const double *X;     /* 3n */
+    const float *mass, *w, *period;
+    const int *off, *nbr, *kth;   /* ball lists (CSR, self included), k-th neighbour */
+} dens_sys;
+
+static double ddist(const dens_sys *S, int i, int j, double u[3])
+{
+    double r2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        u[d] = dmin_image(S->X[3 * (size_t)i + d] - S->X[3 * (size_t)j + d], S->period[d]);
+        r2 += u[d] * u[d];
+    }
+    return sqrt(r2);
+}
+
+/* S_i = sum_{j in B(i)} P_ij W(r_ij, h_i), h_i = |x_i - x_K(i)| / 2. */
+static double row_sum(const dens_sys *S, int i)
+{
+    double u[3];
+    double h = 0.5 * ddist(S, i, S->kth[i], u);
+    double s = 0.0;
+    for (int k = S->off[i]; k < S->off[i + 1]; ++k) {
+        int j = S->nbr[k];
+        double r = ddist(S, i, j, u), f, fp;
+        m4(r / h, &f, &fp);
+        double P = 0.5 * ((double)S->w[i] * S->mass[j] + (double)S->w[j] * S->mass[i]);
+        s += P * f / (M_PI * h * h * h);
+    }
+    return s;
+}
+
+/* d S_i / d x_p (analytic, FP64); adds sum |term| to *abs. */
+static void row_grad(const dens_sys *S, int i, int p, double g[3], double *abs)
+{
+    double u[3];
+    int K = S->kth[i];
+    double rK = ddist(S, i, K, u);
+    double uK[3] = {u[0], u[1], u[2]};   /* x_i - x_K */
+    double h = 0.5 * rK;
+    double H = 0.0;
+    for (int k = S->off[i]; k < S->off[i + 1]; ++k) {
+        int j = S->nbr[k];
+        double r = ddist(S, i, j, u), f, fp;
+        double q = r / h;
+        m4(q, &f, &fp);
+        double P = 0.5 * ((double)S->w[i] * S->mass[j] + (double)S->w[j] * S->mass[i]);
+        H += -P * (3.0 * f + q * fp) / (M_PI * h * h * h * h);
+        if (r > 0.0 && (i == p || j == p)) {
+            double c = P * fp / (M_PI * h * h * h * h) / r;   /* dW/dr / r */
+            double sg = (i == p) ? 1.0 : -1.0;              /* d r / d x_p */
+            double t2 = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                g[d] += sg * c * u[d];
+                t2 += c * u[d] * c * u[d];
+            }
+            *abs += sqrt(t2);
+        }
+    }
+    /* h_i = |x_i - x_K| / 2: d h / d x_i = (x_i - x_K)/(4 h), d h / d x_K = -(...) */
+    if (i == p || K == p) {
+        double sg = (i == p) ? 1.0 : -1.0;
+        double t2 = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            double t = sg * H * uK[d] / (4.0 * h);
+            g[d] += t;
+            t2 += t * t;
+        }
+        *abs += sqrt(t2);
+    }
+}
+
+int or_density_adjoint_check(int n, const float *pos, const float *mass, const float *w, int k,
+                             const float period[3], int nsel, const int *sel, double hfd,
+                             double *grad_an, double *grad_fd, double *absterm, int *lists_ok)
+{
+    if (k < 2 || k > n) return -1;
+    float *ball2 = (float *)malloc((size_t)n * sizeof(float));
+    or_knn_ball2(n, pos, k, period, ball2);
+    ktree t;
+    kt_build(&t, pos, NULL, n);
+    int *off = (int *)malloc(((size_t)n + 1) * sizeof(int));
+    int *kth = (int *)malloc((size_t)n * sizeof(int));
+    ivec all = {0, 0, 0};
+    int ok = 1;
+    for (int i = 0; i < n; ++i) {
+        off[i] = all.n;
+        const float *q = pos + 3 * (size_t)i;
+        float fr2 = nextafterf(ball2[i], INFINITY);
+        range_rec(&t, 0, q, (double)ball2[i] * (1.0 + 1e-5) + 1e-30, period, 1, fr2, list_visit, &all);
+        kth[i] = -1;
+        for (int a = off[i]; a < all.n; ++a) {
+            int j = all.v[a];
+            if (j != i && or_d2(q, pos + 3 * (size_t)j, period) == ball2[i] && (kth[i] < 0 || j < kth[i]))
+                kth[i] = j;
+        }
+        if (kth[i] < 0) ok = 0;
+    }
+    off[n] = all.n;
+    kt_free(&t);
+    *lists_ok = ok;
+    if (!ok) {
+        free(ball2); free(off); free(kth); free(all.v);
+        return -2;
+    }
+    /* rows containing each particle */
+    int *roff = (int *)calloc((size_t)n + 1, sizeof(int));
+    for (int a = 0; a < all.n; ++a) roff[all.v[a] + 1]++;
+    for (int i = 0; i < n; ++i) roff[i + 1] += roff[i];
+    int *rows = (int *)malloc((size_t)(all.n ? all.n : 1) * sizeof(int));
+    int *fill = (int *)malloc((size_t)n * sizeof(int));
+    memcpy(fill, roff, (size_t)n * sizeof(int));
+    for (int i = 0; i < n; ++i)
+        for (int a = off[i]; a < off[i + 1]; ++a) rows[fill[all.v[a]]++] = i;
+    double *X = (double *)malloc(3 * (size_t)n * sizeof(double));
+    for (size_t a = 0; a < 3 * (size_t)n; ++a) X[a] = pos[a];
+    dens_sys S = {n, X, mass, w, period, off, all.v, kth};
+    for (int s = 0; s < nsel; ++s) {
+        int p = sel[s];
+        double g[3] = {0, 0, 0}, ab = 0.0;
+        /* rows that depend on x_p: p's own and every row whose ball holds p
+         * (which includes every row with K(i) == p) */
+        for (int a = roff[p]; a < roff[p + 1]; ++a) row_grad(&S, rows[a], p, g, &ab);
+        int own = 0;
+        for (int a = roff[p]; a < roff[p + 1]; ++a) own |= rows[a] == p;
+        if (!own) row_grad(&S, p, p, g, &ab);
+        for (int d = 0; d < 3; ++d) {
+            grad_an[3 * (size_t)s + d] = g[d];
+            double x0 = X[3 * (size_t)p + d], up = 0.0, dn = 0.0;
+            X[3 * (size_t)p + d] = x0 + hfd;
+            for (int a = roff[p]; a < roff[p + 1]; ++a) up += row_sum(&S, rows[a]);
+            if (!own) up += row_sum(&S, p);
+            X[3 * (size_t)p + d] = x0 - hfd;
+            for (int a = roff[p]; a < roff[p + 1]; ++a) dn += row_sum(&S, rows[a]);
+            if (!own) dn += row_sum(&S, p);
+            X[3 * (size_t)p + d] = x0;
+            grad_fd[3 * (size_t)s + d] = (up - dn) / (2.0 * hfd);
+        }
+        absterm[s] = ab;
+    }
+    free(X); free(fill); free(rows); free(roff);
+    free(ball2); free(off); free(kth); free(all.v);
+    return 0;
+}
+
+/* Density field rho_f(y) = sum_j m_j W(|y - x_j|, h_j) of ns scatterers
+ * (nearest periodic image, h_j^2 = ball2_j / 4), FP64: its gradient at nq
+ * points analytically and by central differences of step hfd, and the sum
+ * of |term| per point. */
+int or_field_grad_check(int ns, const float *spos, const float *smass, const float *sball2,
+                        const float period[3], int nq, const float *ypos, double hfd,
+                        double *grad_an, double *grad_fd, double *absterm)
+{
+    for (int q = 0; q < nq; ++q) {
+        double y[3] = {ypos[3 * (size_t)q], ypos[3 * (size_t)q + 1], ypos[3 * (size_t)q + 2]};
+        double g[3] = {0, 0, 0}, ab = 0.0, fp_[3] = {0, 0, 0}, fm_[3] = {0, 0, 0};
+        for (int j = 0; j < ns; ++j) {
+            double h = 0.5 * sqrt((double)sball2[j]);
+            double u[3], r2 = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                u[d] = dmin_image(y[d] - spos[3 * (size_t)j + d], period[d]);
+                r2 += u[d] * u[d];
+            }
+            if (r2 >= 4.0 * h * h * (1.0 + 1e-6)) continue;
+            double r = sqrt(r2), f, fp;
+            double c0 = smass[j] / (M_PI * h * h * h);
+            m4(r / h, &f, &fp);
+            if (r > 0.0) {
+                double c = c0 * fp / h / r, t2 = 0.0;
+                for (int d = 0; d < 3; ++d) {
+                    g[d] += c * u[d];
+                    t2 += c * u[d] * c * u[d];
+                }
+                ab += sqrt(t2);
+            }
+            for (int d = 0; d < 3; ++d) {
+                for (int sgn = 0; sgn < 2; ++sgn) {
+                    double v[3] = {u[0], u[1], u[2]};
+                    v[d] += sgn ? -hfd : hfd;
+                    double rr = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]), ff, ffp;
+                    m4(rr / h, &ff, &ffp);
+                    if (sgn) fm_[d] += c0 * ff; else fp_[d] += c0 * ff;
+                }
+            }
+        }
+        for (int d = 0; d < 3; ++d) {
+            grad_an[3 * (size_t)q + d] = g[d];
+            grad_fd[3 * (size_t)q + d] = (fp_[d] - fm_[d]) / (2.0 * hfd);
+        }
+        absterm[q] = ab;
+    }
+    return 0;
+}

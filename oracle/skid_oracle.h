@@ -122,6 +122,23 @@ int or_unbind_group(const or_params *par, int inType, int n,
                     double *pot, const float rel[3], float outVcm[3],
                     float *outMass, float outBound[3], int *removed_ids);
 
+/* FP64 references for the adjoint checks.  Density: L = sum_i w_i rho_i
+ * with the kNN sets (and k-th neighbours) of pos held fixed; for the nsel
+ * particles sel[] the analytic gradient and central differences of step hfd
+ * (3 doubles each) and the sum of |term| (one double each).  lists_ok = 0 if
+ * some ball has no k-th neighbour at exactly fBall2 (returns -2). */
+int or_density_adjoint_check(int n, const float *pos, const float *mass,
+                             const float *w, int k, const float period[3],
+                             int nsel, const int *sel, double hfd,
+                             double *grad_an, double *grad_fd, double *absterm,
+                             int *lists_ok);
+/* Density field of ns scatterers at nq points: gradient, central
+ * differences, sum of |term|. */
+int or_field_grad_check(int ns, const float *spos, const float *smass,
+                        const float *sball2, const float period[3], int nq,
+                        const float *ypos, double hfd, double *grad_an,
+                        double *grad_fd, double *absterm);
+
 double or_exp2hub(double H0, double Omega0, double Lambda, double Quint,
                   double a);
 

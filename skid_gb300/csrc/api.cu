@@ -314,6 +314,44 @@ void skid_ctx::collect_field_times(int nslots)
 // ---------------------------------------------------------------------
 // C ABI
 
+// Move field at nm explicit positions from the current live copies, left in
+// probe_acc (the body of skid_field and skid_field_adjoint).
+static int field_probe(skid_ctx *ctx, int nm, const float *mpos)
+{
+    cudaStream_t st = ctx->st;
+    DBuf<float> &xyz = ctx->probe_f;
+    DBuf<float4> &p4 = ctx->probe_p4;
+    DBuf<int> &act = ctx->probe_i;
+    if (dalloc(xyz, 3 * (size_t)nm) || dalloc(p4, nm) || dalloc(act, nm + 2) ||
+        dalloc(ctx->probe_acc, 3 * (size_t)nm))
+        return ctx->fail(SKID_ENOMEM);
+    CK(cudaMemcpyAsync(xyz.p, mpos, 3 * (size_t)nm * sizeof(float), cudaMemcpyHostToDevice, st));
+    xyz_to_pos4<<<grid_for(nm), 256, 0, st>>>(xyz.p, nm, p4.p); skid::note_launch();
+    iota_kernel<<<grid_for(nm), 256, 0, st>>>(act.p, nm); skid::note_launch();
+    CK(cudaMemcpyAsync(act.p + nm, &nm, sizeof(int), cudaMemcpyHostToDevice, st));
+    FieldArgs a = ctx->field_args(0.0f, false, ctx->probe_acc.p);
+    a.mpos = p4.p;
+    a.act = act.p;
+    a.d_nA = act.p + nm;
+    a.G = 32;
+    a.stats = nullptr;
+    a.touched = ctx->probe_touched();
+    if (!a.touched) return ctx->fail(SKID_ENOMEM);
+    CK(field_move(a, nm, st));
+    return 0;
+}
+
+// dL/dy = w * grad rho_f = -w * (move field)
+__global__ void scale_field(float *acc, const float *__restrict__ w, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float s = -w[i];
+        acc[3 * (size_t)i] *= s;
+        acc[3 * (size_t)i + 1] *= s;
+        acc[3 * (size_t)i + 2] *= s;
+    }
+}
+
 extern "C" {
 
 const char *skid_strerror(int code)
@@ -836,28 +874,42 @@ int skid_field(skid_ctx *ctx, int nm, const float *mpos, float *acc)
 {
     if (!ctx || nm < 0 || !mpos || !acc) return SKID_EINVAL;
     if (ctx->stage < STAGE_DENSITY) return ctx->fail(SKID_ESTATE);
-    cudaStream_t st = ctx->st;
-    DBuf<float> &xyz = ctx->probe_f;
-    DBuf<float4> &p4 = ctx->probe_p4;
-    DBuf<int> &act = ctx->probe_i;
-    if (dalloc(xyz, 3 * (size_t)nm) || dalloc(p4, nm) || dalloc(act, nm + 2) ||
-        dalloc(ctx->probe_acc, 3 * (size_t)nm))
-        return ctx->fail(SKID_ENOMEM);
-    CK(cudaMemcpyAsync(xyz.p, mpos, 3 * (size_t)nm * sizeof(float), cudaMemcpyHostToDevice, st));
-    xyz_to_pos4<<<grid_for(nm), 256, 0, st>>>(xyz.p, nm, p4.p); skid::note_launch();
-    iota_kernel<<<grid_for(nm), 256, 0, st>>>(act.p, nm); skid::note_launch();
-    CK(cudaMemcpyAsync(act.p + nm, &nm, sizeof(int), cudaMemcpyHostToDevice, st));
-    FieldArgs a = ctx->field_args(0.0f, false, ctx->probe_acc.p);
-    a.mpos = p4.p;
-    a.act = act.p;
-    a.d_nA = act.p + nm;
-    a.G = 32;
-    a.stats = nullptr;
-    a.touched = ctx->probe_touched();
-    if (!a.touched) return ctx->fail(SKID_ENOMEM);
-    CK(field_move(a, nm, st));
+    if (int rc = field_probe(ctx, nm, mpos)) return rc;
     CK(cudaMemcpyAsync(acc, ctx->probe_acc.p, 3 * (size_t)nm * sizeof(float), cudaMemcpyDeviceToHost,
-                       st));
+                       ctx->st));
+    return ctx->sync_check();
+}
+
+int skid_field_adjoint(skid_ctx *ctx, int nm, const float *mpos, const float *w, float *dLdy)
+{
+    if (!ctx || nm < 0 || !mpos || !w || !dLdy) return SKID_EINVAL;
+    if (ctx->stage < STAGE_DENSITY) return ctx->fail(SKID_ESTATE);
+    if (int rc = field_probe(ctx, nm, mpos)) return rc;
+    cudaStream_t st = ctx->st;
+    if (dalloc(ctx->adj.win, nm > 0 ? nm : 1)) return ctx->fail(SKID_ENOMEM);
+    CK(cudaMemcpyAsync(ctx->adj.win.p, w, (size_t)nm * sizeof(float), cudaMemcpyHostToDevice, st));
+    scale_field<<<grid_for(nm), 256, 0, st>>>(ctx->probe_acc.p, ctx->adj.win.p, nm); skid::note_launch();
+    CK(cudaMemcpyAsync(dLdy, ctx->probe_acc.p, 3 * (size_t)nm * sizeof(float), cudaMemcpyDeviceToHost, st));
+    return ctx->sync_check();
+}
+
+int skid_density_adjoint(skid_ctx *ctx, const float *w, float *dLdx, int mode)
+{
+    if (!ctx || !w || !dLdx ||
+        (mode != SKID_ADJ_RECOMPUTE && mode != SKID_ADJ_STORED && mode != SKID_ADJ_AUTO))
+        return SKID_EINVAL;
+    if (ctx->stage < STAGE_DENSITY) return ctx->fail(SKID_ESTATE);
+    if (ctx->par.nSmooth < 2) return ctx->fail(SKID_EINVAL);
+    cudaStream_t st = ctx->st;
+    int n = ctx->n;
+    if (dalloc(ctx->adj.win, n > 0 ? n : 1)) return ctx->fail(SKID_ENOMEM);
+    CK(cudaMemcpyAsync(ctx->adj.win.p, w, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st));
+    cudaError_t e = density_adjoint(ctx->stree, ctx->sb2.p, ctx->sidx.p, ctx->adj.win.p, n, ctx->L,
+                                    ctx->per, mode, ctx->par.nSmooth, ctx->adj, ctx->d_scal + SC_WORK,
+                                    ctx->d_status, st);
+    if (e == cudaErrorMemoryAllocation) return ctx->fail(SKID_ENOMEM);
+    CK(e);
+    CK(cudaMemcpyAsync(dLdx, ctx->adj.out.p, 3 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
     return ctx->sync_check();
 }
 

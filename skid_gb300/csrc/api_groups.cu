@@ -165,6 +165,27 @@ int skid_set_groups(skid_ctx *ctx, const int *grp, int nGroup, const skid_group 
     return 0;
 }
 
+int skid_potential_adjoint(skid_ctx *ctx, int iSoftType, float G, int nSel, const int *sel,
+                           const float *v, double *E, float *dLdx)
+{
+    if (!ctx || nSel < 0 || (nSel > 0 && (!sel || !E)) || (dLdx && !v)) return SKID_EINVAL;
+    if (iSoftType != SKID_SOFT_PLUMMER && iSoftType != SKID_SOFT_SPLINE) return SKID_EINVAL;
+    if (ctx->stage != STAGE_GROUPS) return ctx->fail(SKID_ESTATE);
+    for (int s = 0; s < nSel; ++s)
+        if (sel[s] < 1 || sel[s] >= ctx->G.nGroup) return ctx->fail(SKID_EINVAL);
+    cudaStream_t st = ctx->st;
+    cudaError_t e = potential_adjoint(ctx->G, ctx->pos4.p, ctx->vel4.p, ctx->n, ctx->L, G,
+                                      iSoftType == SKID_SOFT_PLUMMER, nSel, sel, v, dLdx != nullptr,
+                                      ctx->adj, st);
+    if (e == cudaErrorMemoryAllocation) return ctx->fail(SKID_ENOMEM);
+    CK(e);
+    if (nSel) CK(cudaMemcpyAsync(E, ctx->adj.E.p, nSel * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (dLdx)
+        CK(cudaMemcpyAsync(dLdx, ctx->adj.out.p, 3 * (size_t)ctx->n * sizeof(float), cudaMemcpyDeviceToHost,
+                           st));
+    return ctx->sync_check();
+}
+
 int skid_set_soft(skid_ctx *ctx, float fEps)
 {
     if (!ctx) return SKID_EINVAL;

@@ -98,6 +98,24 @@ cudaError_t too_small(GroupState &G, int *grp, int n, int nmin, int *d_ng, SortS
                       cudaStream_t st);
 cudaError_t group_radius(GroupState &G, const int *grp, int n, const float4 *pos4, float3 L,
                          cudaStream_t st);
+// adjoint.cu
+struct AdjointState {
+    DBuf<float> win;            // cotangent by iOrder (or per query point)
+    DBuf<float> w, g, out;      // cotangent (tree order), gradient (tree order), gradient by iOrder
+    DBuf<int> nbr, ncnt;        // stored ball lists, `cap` per scatterer
+    int cap = 0;
+    bool lists = false;         // lists match the current density
+    DBuf<int2> items;           // potential work items (selection slot, tile)
+    DBuf<int> gsel;
+    DBuf<float> v;
+    DBuf<double> E;
+};
+cudaError_t density_adjoint(const Tree &t, const float *ball2_sorted, const int *sidx, const float *w_io,
+                            int n_io, float3 L, bool per, int mode, int k, AdjointState &A,
+                            int *d_work, unsigned *d_status, cudaStream_t st);
+cudaError_t potential_adjoint(const GroupState &G, const float4 *pos4, const float4 *vel4, int n,
+                              float3 period, float Gc, int plummer, int nSel, const int *h_sel,
+                              const float *h_v, bool want_grad, AdjointState &A, cudaStream_t st);
 // unbind.cu
 cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *pos4,
                        const float4 *vel4, Tree &ut, const UnbindParams &P, int *grp,
@@ -152,6 +170,7 @@ struct skid_ctx {
     skid::DBuf<float4> moved4;      // moved positions by iOrder
     skid::SortScratch ss;
     skid::DBuf<float> knn_heap;     // kNN heaps when k is too large for shared memory
+    skid::AdjointState adj;         // density / potential adjoints
 
     // outer-iteration CUDA graphs, one per movers-per-warp setting
     cudaGraphExec_t iter_graph[3] = {nullptr, nullptr, nullptr};
@@ -230,6 +249,7 @@ struct skid_ctx {
         stage = skid::STAGE_NONE;
         nScatInit = nExtraScat = nMove = nActive = 0;
         G.nGroup = 0;
+        adj.lists = false;
         tim = skid_timings{};
         cudaMemsetAsync(d_scal, 0, skid::SC_COUNT * sizeof(int), st);
         cudaMemsetAsync(d_fbytes, 0, 2 * sizeof(double), st);
@@ -291,6 +311,8 @@ struct skid_ctx {
         dfree(ss.box);
         dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);
         dfree(probe_t); dfree(knn_heap);
+        dfree(adj.win); dfree(adj.w); dfree(adj.g); dfree(adj.out); dfree(adj.nbr); dfree(adj.ncnt);
+        dfree(adj.items); dfree(adj.gsel); dfree(adj.v); dfree(adj.E);
         if (d_scal) cudaFree(d_scal);
         if (d_fbytes) cudaFree(d_fbytes);
         if (d_fstats) cudaFree(d_fstats);

@@ -18,6 +18,7 @@ SKID_ERRORS = {
     -1: "invalid argument", -2: "out of memory", -3: "CUDA runtime error",
     -4: "bounded device wait ran out", -5: "internal capacity exceeded",
     -6: "no usable sm_103 device", -7: "call made in the wrong pipeline state",
+    -8: "request exceeds a fixed capacity",
 }
 
 
@@ -88,7 +89,14 @@ SIGNATURES = {
     "skid_knn_ball2": [_V, C.c_int, _F, C.c_int, _F],
     "skid_field": [_V, C.c_int, _F, _F],
     "skid_fof_points": [_V, C.c_int, _F, C.c_float, _I, _I],
+    "skid_density_adjoint": [_V, _F, _F, C.c_int],
+    "skid_field_adjoint": [_V, C.c_int, _F, _F, _F],
+    "skid_potential_adjoint": [_V, C.c_int, C.c_float, C.c_int, _I, _F, _D, _F],
 }
+
+ADJ_RECOMPUTE = 0
+ADJ_STORED = 1
+ADJ_AUTO = 2
 
 _lib = None
 
@@ -315,6 +323,36 @@ class Context:
         acc = np.empty((len(mpos), 3), np.float32)
         self._call("skid_field", self.h, len(mpos), _f(mpos), _f(acc))
         return acc
+
+    def density_adjoint(self, w, mode=ADJ_RECOMPUTE):
+        """dL/dx (n, 3) by iOrder for L = sum_i w_i rho_i (after density())."""
+        w = _c32(w)
+        out = np.empty((len(w), 3), np.float32)
+        self._call("skid_density_adjoint", self.h, _f(w), _f(out), int(mode))
+        return out
+
+    def field_adjoint(self, ypos, w):
+        """w_i * grad rho_f(y_i), (nm, 3), over the live scatterer copies."""
+        ypos = _c32(ypos, (-1, 3))
+        w = _c32(w)
+        out = np.empty((len(ypos), 3), np.float32)
+        self._call("skid_field_adjoint", self.h, len(ypos), _f(ypos), _f(w), _f(out))
+        return out
+
+    def potential_adjoint(self, sel, v=None, G=1.0, soft_type=2, n=None):
+        """Potential energies E[s] of groups sel (FP64) and, with v, the
+        gradient of sum_s v[s] E[s] by iOrder (n, 3)."""
+        sel = np.ascontiguousarray(sel, np.int32)
+        E = np.zeros(len(sel), np.float64)
+        grad = None
+        vp = gp = None
+        if v is not None:
+            v = _c32(v)
+            grad = np.empty((self.n if n is None else n, 3), np.float32)
+            vp, gp = _f(v), _f(grad)
+        self._call("skid_potential_adjoint", self.h, int(soft_type), G, len(sel), _i(sel), vp,
+                   E.ctypes.data_as(_D), gp)
+        return E, grad
 
     def fof_points(self, pos, tau):
         pos = _c32(pos, (-1, 3))
