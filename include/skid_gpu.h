@@ -188,8 +188,27 @@ int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
  *   "field_movers_per_warp"  0 = by active count (default), or 32, 8, 1
  *   "field_g32_min"          active movers at or above which 32 per warp
  *   "field_g8_min"           active movers at or above which 8 per warp
+ *   "unbind_warp_max"        groups up to this size get one warp each in the
+ *                            removal loop: 0, 32, 64, 128, or -1 = autotuned
+ *                            (default: every candidate is timed on the first
+ *                            skid_unbind of the context, the fastest is kept)
+ *   "unbind_block"           threads per block for larger groups: 128, 256,
+ *                            512, 1024, or -1 = autotuned
+ *   "unbind_per_group"       1: one potential and one removal launch per group
+ *                            (the reference's serial loop, for comparison)
+ *   "unbind_retune"          forget the autotuned schedule
+ *   "field_unfused"          1: every move step runs the field as a separate
+ *                            gradient pass (field to memory, then a move
+ *                            kernel) instead of the fused adjoint-and-move
+ *                            kernel (for comparison; set before
+ *                            skid_init_move)
  * Returns SKID_EINVAL for an unknown name or value. */
 int skid_set_option(skid_ctx *ctx, const char *name, double value);
+
+/* Current value of a knob; for "unbind_warp_max" and "unbind_block" the
+ * schedule the last skid_unbind used, and "unbind_tune_candidates" the
+ * number of schedules the autotuner timed. */
+int skid_get_option(skid_ctx *ctx, const char *name, double *value);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that time or
  * order their own work against the library's (no reference counterpart). */

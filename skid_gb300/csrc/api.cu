@@ -295,7 +295,15 @@ int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int 
     CK(cudaStreamIsCapturing(st, &cs));
     unsigned evflags = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
     CK(cudaEventRecordWithFlags(fev[2 * slot], st, evflags));
-    CK(field_move(a, nMove, st));
+    if (opt_field_unfused) {
+        if (unfused_acc.n < 3 * (size_t)nMove) return fail(SKID_ESTATE);
+        a.fStep = 0.0f;
+        a.acc_out = unfused_acc.p;
+        CK(field_move(a, nMove, st));
+        CK(move_movers(a, unfused_acc.p, fStep, nMove, st));
+    } else {
+        CK(field_move(a, nMove, st));
+    }
     CK(cudaEventRecordWithFlags(fev[2 * slot + 1], st, evflags));
     CK(scatter_cut(C, initial, nocut, rho_final.p, ss, st));
     CK(tree_refit(ctree, C.cpos.p, nullptr, C.d_n, st, true, C.d_dirty));
@@ -616,6 +624,8 @@ int skid_init_move(skid_ctx *ctx, float fDensMin, float fTempMax, float fMassMax
     int n = ctx->n;
     cudaStream_t st = ctx->st;
     if (ctx->alloc_movers(n)) return ctx->fail(SKID_ENOMEM);
+    if (ctx->opt_field_unfused && dalloc(ctx->unfused_acc, 3 * (size_t)(n > 0 ? n : 1)))
+        return ctx->fail(SKID_ENOMEM);
     cut_criterion<<<grid_for(n), 256, 0, st>>>(ctx->pos4.p, ctx->rho.p, ctx->temp.p, n, ctx->nGas,
                                                ctx->nDark, ctx->inType, fDensMin, fTempMax,
                                                fMassMax, bGasAndDark, bGasOnly, ctx->M.keep.p); skid::note_launch();
@@ -838,9 +848,38 @@ int skid_set_option(skid_ctx *ctx, const char *name, double value)
     } else if (!strcmp(name, "field_g8_min")) {
         if (v < 0) return SKID_EINVAL;
         ctx->opt_g8_min = v;
+    } else if (!strcmp(name, "unbind_warp_max")) {
+        if (v != -1 && v != 0 && v != 32 && v != 64 && v != 128) return SKID_EINVAL;
+        ctx->opt_unbind_tw = v;
+    } else if (!strcmp(name, "unbind_block")) {
+        if (v != -1 && v != 128 && v != 256 && v != 512 && v != 1024) return SKID_EINVAL;
+        ctx->opt_unbind_bs = v;
+    } else if (!strcmp(name, "unbind_per_group")) {
+        ctx->opt_unbind_per_group = v != 0;
+    } else if (!strcmp(name, "field_unfused")) {
+        ctx->opt_field_unfused = v != 0;
+        ctx->drop_graphs();
+    } else if (!strcmp(name, "unbind_retune")) {
+        ctx->U.tuned_tw = ctx->U.tuned_bs = -1;
+        ctx->U.ntune = 0;
     } else {
         return SKID_EINVAL;
     }
+    return 0;
+}
+
+int skid_get_option(skid_ctx *ctx, const char *name, double *value)
+{
+    if (!ctx || !name || !value) return SKID_EINVAL;
+    if (!strcmp(name, "field_movers_per_warp")) *value = ctx->opt_G;
+    else if (!strcmp(name, "field_g32_min")) *value = ctx->opt_g32_min;
+    else if (!strcmp(name, "field_g8_min")) *value = ctx->opt_g8_min;
+    else if (!strcmp(name, "unbind_warp_max")) *value = ctx->U.used_tw;
+    else if (!strcmp(name, "unbind_block")) *value = ctx->U.used_bs;
+    else if (!strcmp(name, "unbind_per_group")) *value = ctx->opt_unbind_per_group;
+    else if (!strcmp(name, "unbind_tune_candidates")) *value = ctx->U.ntune;
+    else if (!strcmp(name, "field_unfused")) *value = ctx->opt_field_unfused;
+    else return SKID_EINVAL;
     return 0;
 }
 

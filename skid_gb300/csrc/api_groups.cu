@@ -237,6 +237,10 @@ int skid_unbind(skid_ctx *ctx, int iSoftType, float fScoop, int bGasAndDark, int
     P.subpot = ctx->inType == 1 || ctx->inType == 4;   // kd.c:1441
     P.nounbind = bNoUnbind != 0;
     P.scale = ctx->pot_scale(G);
+    P.n = ctx->n;
+    P.tw = ctx->opt_unbind_tw;
+    P.bs = ctx->opt_unbind_bs;
+    P.per_group = ctx->opt_unbind_per_group;
     CK(unbind_run(ctx->G, ctx->G.gof.p, ctx->n, ctx->pos4.p, ctx->vel4.p, ctx->utree, P, ctx->grp.p,
                   ctx->d_scal + SC_NUNB, ctx->ss, ctx->U, st));
     int nu = 0;

@@ -73,14 +73,24 @@ struct UnbindParams {
     float G, a, aH, opz, z;
     float scale;       // 2^S of the fixed-point potentials
     int plummer, subpot, nounbind;
+    int n;             // particles (size of grp)
+    int tw, bs;        // removal schedule: warp-per-group up to tw members, blocks of bs
+                       // threads above; -1 = autotuned
+    bool per_group;    // one potential and one removal launch per group
 };
 
 struct UnbindScratch {
     DBuf<float4> qr, qv, slist;
-    DBuf<long long> pot;
-    DBuf<int> qid, scnt, soff, nt, toff, cnt;
+    DBuf<long long> pot, pot_save;
+    DBuf<int> qid, scnt, soff, nt, toff, cnt, grp_save;
+    DBuf<uint32_t> order;
     DBuf<int2> items;
     DBuf<float> ssoft, usoft;
+    DBuf<skid_group> rec_save;
+    int tuned_tw = -1, tuned_bs = -1;   // autotuned removal schedule (kept per context)
+    int used_tw = -1, used_bs = -1;     // schedule of the last run
+    float tune_ms[16] = {};
+    int ntune = 0;
 };
 
 // fof.cu
@@ -223,6 +233,10 @@ struct skid_ctx {
     // move-field time is lowest with 32 movers per warp above ~450k active
     // movers, 8 per warp down to ~24k, and one per warp below.
     int opt_G = 0, opt_g32_min = 450000, opt_g8_min = 24000;
+    int opt_unbind_tw = -1, opt_unbind_bs = -1;   // -1: autotuned on the first skid_unbind
+    bool opt_unbind_per_group = false;
+    bool opt_field_unfused = false;                // field pass and move pass as separate kernels
+    skid::DBuf<float> unfused_acc;
     int movers_per_warp() const
     {
         if (opt_G) return opt_G;
@@ -306,7 +320,9 @@ struct skid_ctx {
         dfree(G.map); dfree(G.gtmp); dfree(G.gtmp2); dfree(G.gof); dfree(G.rec2);
         dfree(U.qr); dfree(U.qv); dfree(U.slist); dfree(U.pot); dfree(U.qid); dfree(U.scnt);
         dfree(U.soff); dfree(U.nt); dfree(U.toff); dfree(U.cnt); dfree(U.items); dfree(U.ssoft);
-        dfree(U.usoft); dfree(fof_minio); dfree(fof_flag); dfree(moved4);
+        dfree(unfused_acc);
+        dfree(U.usoft); dfree(U.pot_save); dfree(U.grp_save); dfree(U.order); dfree(U.rec_save);
+        dfree(fof_minio); dfree(fof_flag); dfree(moved4);
         dfree(ss.k0); dfree(ss.k1); dfree(ss.v0); dfree(ss.v1); dfree(ss.hist); dfree(ss.blk);
         dfree(ss.box);
         dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);

@@ -311,6 +311,45 @@ static cudaError_t launch_field(const FieldArgs &a, int max_movers, cudaStream_t
     return cudaGetLastError();
 }
 
+// The move alone (kdMoveParticles, kd.c:702-732) from a field written by
+// field_kernel with fStep = 0: the unfused form, a separate gradient pass.
+__global__ void move_kernel(FieldArgs a, const float *__restrict__ acc, float fStep, int cap)
+{
+    const int nA = *a.d_nA;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nA && slot < cap;
+         slot += gridDim.x * blockDim.x) {
+        int mi = a.act[slot];
+        if (mi < 0 || mi >= cap) {
+            set_status(a.d_status, ST_BADSTATE);
+            continue;
+        }
+        float4 yp = a.mpos[mi];
+        float3 y = make_float3(yp.x, yp.y, yp.z);
+        float ax = acc[3 * (size_t)slot], ay = acc[3 * (size_t)slot + 1], az = acc[3 * (size_t)slot + 2];
+        float s = d2of(ax, ay, az);
+        float ai = sqrtf(s);
+        ai = ai > 0.0f ? __fdiv_rn(fStep, ai) : 0.0f;
+        y.x = fsub(y.x, fmul(ai, ax));
+        y.y = fsub(y.y, fmul(ai, ay));
+        y.z = fsub(y.z, fmul(ai, az));
+        if (y.x > a.wrapHi.x) y.x = fsub(y.x, a.period.x);
+        if (y.x <= a.wrapLo.x) y.x = fadd(y.x, a.period.x);
+        if (y.y > a.wrapHi.y) y.y = fsub(y.y, a.period.y);
+        if (y.y <= a.wrapLo.y) y.y = fadd(y.y, a.period.y);
+        if (y.z > a.wrapHi.z) y.z = fsub(y.z, a.period.z);
+        if (y.z <= a.wrapLo.z) y.z = fadd(y.z, a.period.z);
+        a.mpos[mi] = make_float4(y.x, y.y, y.z, yp.w);
+    }
+}
+
+cudaError_t move_movers(const FieldArgs &a, const float *acc, float fStep, int max_movers,
+                        cudaStream_t st)
+{
+    if (max_movers <= 0) return cudaSuccess;
+    move_kernel<<<grid_for(max_movers), 256, 0, st>>>(a, acc, fStep, max_movers); note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st)
 {
     if (max_movers <= 0) return cudaSuccess;

@@ -166,6 +166,9 @@ struct FieldArgs {
     int G;                           // movers per warp: 32, 8 or 1
 };
 cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st);
+// The move step alone, from a field computed with fStep = 0 into acc.
+cudaError_t move_movers(const FieldArgs &a, const float *acc, float fStep, int max_movers,
+                        cudaStream_t st);
 
 // ---- scatter.cu ----
 // Copies of the ns scatterers (sorted order) with their densities; sets

@@ -19,11 +19,22 @@
 // potential exactly 0 (or its scoop part) and is unbound with E = 1/2 dv^2 >= 0.
 // Integer sums reproduce that exactly and in any order.
 //
-// Kernels: scoop lists (one thread per group walks the tree of ungrouped
-// particles), the all-pairs potential (one block per 128-member tile), and
-// the removal loop (one block per group, block-wide arg-max with
-// first-index ties).
+// Kernels, every group in one launch each:
+//  - scoop lists: one thread per group walks the tree of ungrouped particles;
+//  - potentials: work items are the upper-triangle tile pairs (I <= J) of
+//    every group, largest groups first; each pair's psi is evaluated once and
+//    added to both ends (the terms are exact integers, so the sums do not
+//    depend on the order);
+//  - removal: one persistent kernel takes groups largest first from a queue:
+//    groups above `tw` members get the whole block (BS threads, block-wide
+//    arg-max with first-index ties), smaller groups one warp each (warp
+//    shuffles only, no block barriers).
+// (tw, BS) is picked by timing the candidates on the first call (autotune),
+// or fixed through the context's options.  A per-group mode (one potential
+// and one removal launch per group, the reference's serial loop on the GPU)
+// serves as the unbatched comparison.
 #include <cfloat>
+#include <vector>
 
 #include "ctx.h"
 
@@ -31,8 +42,7 @@ namespace skid {
 
 namespace {
 
-constexpr int POT_TILE = 128;
-constexpr int RM_THREADS = 256;
+constexpr int POT_TILE = 128;   // power of two
 // Groups up to this size evaluate E exactly as the reference does (FP64
 // expression rounded to float, kd.c:1396-1399), so equal-energy members are
 // ordered by the reference's own rounding; larger groups use FP32 (GB300's
@@ -91,10 +101,12 @@ __global__ void scoop_kernel(TreeView t, const float *__restrict__ usoft,
                              int pass, int *__restrict__ cnt, const int *__restrict__ off,
                              float4 *__restrict__ list, float *__restrict__ lsoft)
 {
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x + 1; g < ng; g += gridDim.x * blockDim.x) {
+    // every entry is written, group 0 (the ungrouped particles) with 0: the
+    // counts are scanned into offsets as a whole
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
         int c = 0;
         int n = gcount[g];
-        if (n > 0 && n < nmax && t.n > 0) {
+        if (g > 0 && n > 0 && n < nmax && t.n > 0) {
             const float *cen = rec[g].rCenter;
             const float *rel = rec[g].rel;
             float3 q = make_float3(cen[0], cen[1], cen[2]);
@@ -134,83 +146,147 @@ __global__ void scoop_kernel(TreeView t, const float *__restrict__ usoft,
     }
 }
 
-__global__ void pot_items(const int *__restrict__ gcount, int ng, int nmax,
-                          const int *__restrict__ ioff, int2 *__restrict__ items)
-{
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x + 1; g < ng; g += gridDim.x * blockDim.x) {
-        int n = gcount[g];
-        if (n <= 0 || n >= nmax) continue;
-        int nt = (n + POT_TILE - 1) / POT_TILE;
-        for (int t = 0; t < nt; ++t) items[ioff[g] + t] = make_int2(g, t);
-    }
-}
 
-__global__ void pot_ntiles(const int *__restrict__ gcount, int ng, int nmax, int *__restrict__ nt)
+// ---- scheduling order: valid groups by descending size ----
+
+__global__ void sched_keys(const int *__restrict__ gcount, int ng, int nmax, uint64_t *keys,
+                           uint32_t *vals)
 {
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
         int n = gcount[g];
-        nt[g] = (g > 0 && n > 0 && n < nmax) ? (n + POT_TILE - 1) / POT_TILE : 0;
+        bool ok = g > 0 && n > 0 && n < nmax;
+        keys[g] = ok ? (uint64_t)(0x7fffffff - n) : 0xffffffffull;
+        vals[g] = (uint32_t)g;
     }
 }
 
-__global__ void __launch_bounds__(POT_TILE)
-pot_kernel(const int2 *__restrict__ items, const int *d_nitems, const int *__restrict__ gstart,
-           const int *__restrict__ gcount, const float4 *__restrict__ qr,
-           const float4 *__restrict__ qv, const int *__restrict__ soff,
-           const int *__restrict__ scnt, const float4 *__restrict__ slist,
-           const float *__restrict__ ssoft, float G, int plummer, float scale,
-           long long *__restrict__ pot)
+// cnt[0] = valid groups, cnt[1] = groups above tw members
+__global__ void sched_counts(const int *__restrict__ gcount, int ng, int nmax, int tw, int *cnt)
 {
-    __shared__ float4 sr[POT_TILE];
-    __shared__ float ss[POT_TILE];
-    int nitems = *d_nitems;
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        int2 w = items[it];
-        int g = w.x;
-        int s = gstart[g], n = gcount[g];
-        int i = w.y * POT_TILE + threadIdx.x;
-        bool valid = i < n;
-        float4 ri = valid ? qr[s + i] : make_float4(0, 0, 0, 0);
-        float ei = valid ? qv[s + i].w : 0.0f;
-        long long acc = 0;
-        for (int jb = 0; jb < n; jb += POT_TILE) {
-            __syncthreads();
-            int j = jb + threadIdx.x;
-            if (j < n) {
-                sr[threadIdx.x] = qr[s + j];
-                ss[threadIdx.x] = qv[s + j].w;
-            }
-            __syncthreads();
-            int cnt = min(POT_TILE, n - jb);
-            for (int k = 0; k < cnt; ++k) {
-                float4 rj = sr[k];
-                float d2 = d2of(fsub(ri.x, rj.x), fsub(ri.y, rj.y), fsub(ri.z, rj.z));
-                float dir = spline_pot(d2, fadd(ei, ss[k]), plummer);
-                float term = fmul(fmul(G, rj.w), dir);
-                acc += (jb + k != i) ? fx(term, scale) : 0ll;
-            }
+    int v = 0, b = 0;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+        int n = gcount[g];
+        if (g > 0 && n > 0 && n < nmax) {
+            ++v;
+            b += n > tw;
         }
-        // kdAddScoopPot: grav.c:112-127
-        int so = soff[g], sc = scnt[g];
-        for (int jb = 0; jb < sc; jb += POT_TILE) {
-            __syncthreads();
-            int j = jb + threadIdx.x;
-            if (j < sc) {
-                sr[threadIdx.x] = slist[so + j];
-                ss[threadIdx.x] = ssoft[so + j];
-            }
-            __syncthreads();
-            int cnt = min(POT_TILE, sc - jb);
-            for (int k = 0; k < cnt; ++k) {
-                float4 rj = sr[k];
-                float d2 = d2of(fsub(rj.x, ri.x), fsub(rj.y, ri.y), fsub(rj.z, ri.z));
-                float dir = spline_pot(d2, fadd(ss[k], ei), plummer);
-                acc += fx(fmul(fmul(G, rj.w), dir), scale);
-            }
-        }
-        if (valid) pot[s + i] = acc;
+    }
+    for (int o = 16; o; o >>= 1) {
+        v += __shfl_xor_sync(SKID_FULL, v, o);
+        b += __shfl_xor_sync(SKID_FULL, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(cnt, v);
+        atomicAdd(cnt + 1, b);
     }
 }
+
+// ---- potentials ----
+
+__global__ void pot_nitems(const uint32_t *__restrict__ order, const int *d_nvalid,
+                           const int *__restrict__ gcount, int ng, int *__restrict__ ni)
+{
+    int nv = *d_nvalid;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ng; k += gridDim.x * blockDim.x) {
+        int c = 0;
+        if (k < nv) {
+            int nt = (gcount[order[k]] + POT_TILE - 1) / POT_TILE;
+            c = nt * (nt + 1) / 2;
+        }
+        ni[k] = c;
+    }
+}
+
+__global__ void pot_fill(const uint32_t *__restrict__ order, const int *d_nvalid,
+                         const int *__restrict__ gcount, const int *__restrict__ ioff,
+                         int2 *__restrict__ items)
+{
+    int nv = *d_nvalid;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += gridDim.x * blockDim.x) {
+        int g = order[k];
+        int nt = (gcount[g] + POT_TILE - 1) / POT_TILE;
+        int o = ioff[k];
+        for (int I = 0; I < nt; ++I)
+            for (int J = I; J < nt; ++J) items[o++] = make_int2(g, (I << 16) | J);
+    }
+}
+
+// One tile pair (I, J) of one group per block iteration.  Off-diagonal
+// items take every (i in I, j in J); diagonal items every i < j in the tile,
+// plus the scoop terms of the tile's rows (kdAddScoopPot, grav.c:112-127).
+// At rotation step k thread t pairs its row with column (t + k) mod T, so a
+// column's shared accumulator is touched by one thread per step.
+__global__ void __launch_bounds__(POT_TILE)
+pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_host,
+               const int *__restrict__ gstart, const int *__restrict__ gcount,
+               const float4 *__restrict__ qr, const float4 *__restrict__ qv,
+               const int *__restrict__ soff, const int *__restrict__ scnt,
+               const float4 *__restrict__ slist, const float *__restrict__ ssoft, float G,
+               int plummer, float scale, long long *__restrict__ pot)
+{
+    constexpr int T = POT_TILE;
+    __shared__ float4 sr[T];
+    __shared__ float ss[T];
+    __shared__ unsigned long long acc_j[T];
+    const int t = threadIdx.x;
+    const int nitems = nitems_host >= 0 ? nitems_host : *d_nitems;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        int2 w = items[it];
+        int g = w.x, I = w.y >> 16, J = w.y & 0xffff;
+        int s = gstart[g], n = gcount[g];
+        int i = I * T + t;
+        bool vi = i < n;
+        float4 ri = vi ? qr[s + i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float ei = vi ? qv[s + i].w : 0.0f;
+        int j0 = J * T;
+        int nj = min(T, n - j0);
+        __syncthreads();
+        if (t < nj) {
+            sr[t] = qr[s + j0 + t];
+            ss[t] = qv[s + j0 + t].w;
+        }
+        acc_j[t] = 0ull;
+        __syncthreads();
+        long long acc = 0;
+        if (vi) {
+            int kmax = I != J ? T : T / 2 + 1;
+            for (int k = I != J ? 0 : 1; k < kmax; ++k) {
+                int jl = (t + k) & (T - 1);
+                if (jl >= nj) continue;
+                if (I == J && k == T / 2 && t >= T / 2) continue;   // each pair once
+                float4 rj = sr[jl];
+                float d2 = d2of(fsub(ri.x, rj.x), fsub(ri.y, rj.y), fsub(ri.z, rj.z));
+                float dir = spline_pot(d2, fadd(ei, ss[jl]), plummer);
+                acc += fx(fmul(fmul(G, rj.w), dir), scale);
+                atomicAdd(&acc_j[jl], (unsigned long long)fx(fmul(fmul(G, ri.w), dir), scale));
+            }
+        }
+        if (I == J) {
+            int so = soff[g], sc = scnt[g];
+            for (int jb = 0; jb < sc; jb += T) {
+                __syncthreads();
+                if (jb + t < sc) {
+                    sr[t] = slist[so + jb + t];
+                    ss[t] = ssoft[so + jb + t];
+                }
+                __syncthreads();
+                int cnt = min(T, sc - jb);
+                if (vi)
+                    for (int k = 0; k < cnt; ++k) {
+                        float4 rj = sr[k];
+                        float d2 = d2of(fsub(rj.x, ri.x), fsub(rj.y, ri.y), fsub(rj.z, ri.z));
+                        float dir = spline_pot(d2, fadd(ss[k], ei), plummer);
+                        acc += fx(fmul(fmul(G, rj.w), dir), scale);
+                    }
+            }
+        }
+        __syncthreads();
+        if (vi) atomicAdd((unsigned long long *)&pot[s + i], (unsigned long long)acc);
+        if (t < nj && acc_j[t]) atomicAdd((unsigned long long *)&pot[s + j0 + t], acc_j[t]);
+    }
+}
+
+// ---- removal ----
 
 struct ArgRed {
     float v;
@@ -253,169 +329,354 @@ struct RemoveArgs {
     float scale, inv_scale;         // 2^S, 2^-S
     float3 hP;
     int plummer, subpot, nounbind;
+    const uint32_t *order;          // valid groups, largest first
+    const int *d_cnt;               // [valid groups, groups above tw]
+    int *d_queue;
+    int single;                     // > 0: process only this group (per-group mode)
 };
 
-__global__ void __launch_bounds__(RM_THREADS) remove_kernel(RemoveArgs A)
+// E_i of kd.c:1392-1400: exact form (FP64 expression rounded to float, as the
+// reference computes it) or FP32 form for large groups.
+__device__ __forceinline__ float member_energy(bool exact, const RemoveArgs &A, float4 r, float4 v,
+                                               long long p, const double *dcm, const float *scm,
+                                               double inv_d, double opz_d)
 {
-    __shared__ ArgRed smax[RM_THREADS / 32], smin[RM_THREADS / 32];
-    __shared__ float4 s_r;      // removed particle (relative position, mass)
-    __shared__ float s_eps;
-    __shared__ float s_cm[6];   // rcm, vcm as floats
-    __shared__ int s_n, s_go, s_have, s_imin;
-    __shared__ double d_cm[6], d_mass;
-    int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    for (int g = blockIdx.x + 1; g < A.ng; g += gridDim.x) {
-        int s = A.gstart[g], n0 = A.gcount[g];
-        if (n0 <= 0 || n0 >= A.nmax) continue;
-        float4 *qr = A.qr + s;
-        float4 *qv = A.qv + s;
-        int *qid = A.qid + s;
-        long long *pot = A.pot + s;
-        // centre of mass and velocity (kd.c:1360-1375), FP64 sums of float products
-        double m = 0.0, c[6] = {0, 0, 0, 0, 0, 0};
-        for (int i = tid; i < n0; i += RM_THREADS) {
-            float4 r = qr[i], v = qv[i];
-            m += r.w;
-            c[0] += fmul(r.w, r.x); c[1] += fmul(r.w, r.y); c[2] += fmul(r.w, r.z);
-            c[3] += fmul(r.w, v.x); c[4] += fmul(r.w, v.y); c[5] += fmul(r.w, v.z);
-        }
+    if (exact) {
+        double fs = A.fShift, fc = A.fCosmo;
+        float dv0 = (float)(fs * ((double)v.x - dcm[3]) + fc * ((double)r.x - dcm[0]));
+        float dv1 = (float)(fs * ((double)v.y - dcm[4]) + fc * ((double)r.y - dcm[1]));
+        float dv2 = (float)(fs * ((double)v.z - dcm[5]) + fc * ((double)r.z - dcm[2]));
+        float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
+        return (float)(0.5 * (double)dd - ((double)p * inv_d) * opz_d);
+    }
+    float dv0 = A.fShift * (v.x - scm[3]) + A.fCosmo * (r.x - scm[0]);
+    float dv1 = A.fShift * (v.y - scm[4]) + A.fCosmo * (r.y - scm[1]);
+    float dv2 = A.fShift * (v.z - scm[5]) + A.fCosmo * (r.z - scm[2]);
+    float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
+    return 0.5f * dd - (__ll2float_rn(p) * A.inv_scale) * A.opz;
+}
+
+// kdSubPot (grav.c:44-59) of the removed particle rs on member (r, v).
+__device__ __forceinline__ long long sub_pot(const RemoveArgs &A, float4 rs, float es, float4 r,
+                                             float4 v, long long p)
+{
+    float d2 = d2of(fsub(rs.x, r.x), fsub(rs.y, r.y), fsub(rs.z, r.z));
+    float dir = spline_pot(d2, fadd(es, v.w), A.plummer);
+    return p - fx(fmul(fmul(A.G, rs.w), dir), A.scale);
+}
+
+// centre of mass: kd.c:1360-1375 (FP64 sums of float products)
+__device__ __forceinline__ void rcm_update(double &mass, double *dcm, float4 r, float4 v)
+{
+    mass -= r.w;
+    double f = (double)r.w / mass;
+    dcm[0] += f * (dcm[0] - r.x);
+    dcm[1] += f * (dcm[1] - r.y);
+    dcm[2] += f * (dcm[2] - r.z);
+    dcm[3] += f * (dcm[3] - v.x);
+    dcm[4] += f * (dcm[4] - v.y);
+    dcm[5] += f * (dcm[5] - v.z);
+}
+
+__device__ __forceinline__ void write_record(const RemoveArgs &A, int g, int n, double mass,
+                                             const double *dcm, float4 rb, int nrem)
+{
+    skid_group r = A.rec[g];
+    r.nMembers = n;
+    r.fMass = (float)mass;
+    r.vcm[0] = (float)dcm[3];
+    r.vcm[1] = (float)dcm[4];
+    r.vcm[2] = (float)dcm[5];
+    float hx = A.hP.x;   // kd.c:1452-1456 wraps every axis with hx
+    r.rBound[0] = wrap_h(fadd(rb.x, r.rel[0]), hx);
+    r.rBound[1] = wrap_h(fadd(rb.y, r.rel[1]), hx);
+    r.rBound[2] = wrap_h(fadd(rb.z, r.rel[2]), hx);
+    A.rec[g] = r;
+    if (nrem) atomicAdd(A.d_unbound, nrem);
+}
+
+// A small group, one warp: every lane keeps the FP64 centre itself (the same
+// values on every lane), lane 0 writes.
+__device__ void warp_group(const RemoveArgs &A, int g)
+{
+    const int lane = threadIdx.x & 31;
+    const int s = A.gstart[g], n0 = A.gcount[g];
+    float4 *qr = A.qr + s;
+    float4 *qv = A.qv + s;
+    int *qid = A.qid + s;
+    long long *pot = A.pot + s;
+    double m = 0.0, dcm[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = lane; i < n0; i += 32) {
+        float4 r = qr[i], v = qv[i];
+        m += r.w;
+        dcm[0] += fmul(r.w, r.x); dcm[1] += fmul(r.w, r.y); dcm[2] += fmul(r.w, r.z);
+        dcm[3] += fmul(r.w, v.x); dcm[4] += fmul(r.w, v.y); dcm[5] += fmul(r.w, v.z);
+    }
 #pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            m += __shfl_xor_sync(SKID_FULL, m, o);
-            for (int d = 0; d < 6; ++d) c[d] += __shfl_xor_sync(SKID_FULL, c[d], o);
+    for (int o = 16; o; o >>= 1) {
+        m += __shfl_xor_sync(SKID_FULL, m, o);
+        for (int d = 0; d < 6; ++d) dcm[d] += __shfl_xor_sync(SKID_FULL, dcm[d], o);
+    }
+    float scm[6];
+    for (int d = 0; d < 6; ++d) {
+        dcm[d] /= m;
+        scm[d] = (float)dcm[d];
+    }
+    const bool exact = n0 <= EXACT_E_MAX;
+    const double opz_d = 1.0 + (double)A.z, inv_d = 1.0 / (double)A.scale;
+    int n = n0, nrem = 0, imin = 0;
+    bool have = false;
+    float4 rs = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float es = 0.0f;
+    for (;;) {
+        ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
+        for (int i = lane; i < n; i += 32) {
+            float4 r = qr[i], v = qv[i];
+            long long p = pot[i];
+            if (have && A.subpot) {
+                p = sub_pot(A, rs, es, r, v, p);
+                pot[i] = p;
+            }
+            float E = member_energy(exact, A, r, v, p, dcm, scm, inv_d, opz_d);
+            if (E > mx.v) { mx.v = E; mx.i = i; }
+            if (E < mn.v) { mn.v = E; mn.i = i; }
         }
-        __syncthreads();
-        if (tid == 0) { d_mass = 0.0; for (int d = 0; d < 6; ++d) d_cm[d] = 0.0; }
-        __syncthreads();
+        mx = warp_argmax(mx);
+        mn = warp_argmin(mn);
+        // kd.c:1389-1409: fTotBig starts at -1, fTotMin at 1
+        imin = mn.v < 1.0f ? mn.i : 0;
+        if (!(mx.v >= 0.0f) || A.nounbind || n == 0) break;
+        const int ib = mx.i;
+        __syncwarp();
+        float4 r = qr[ib], v = qv[ib];
+        __syncwarp();   // every lane has read the removed member before lane 0 swaps it away
+        if (lane == 0) A.grp[qid[ib]] = 0;
+        ++nrem;
+        const int nn = n - 1;
+        if (nn == 0) {
+            m = 0.0;
+            dcm[3] = dcm[4] = dcm[5] = 0.0;
+            n = 0;
+            break;
+        }
+        rcm_update(m, dcm, r, v);
+        for (int d = 0; d < 6; ++d) scm[d] = (float)dcm[d];
         if (lane == 0) {
-            atomicAdd(&d_mass, m);
-            for (int d = 0; d < 6; ++d) atomicAdd(&d_cm[d], c[d]);
+            // swap with the last member (kd.c:1435-1440)
+            float4 rl = qr[nn], vl = qv[nn];
+            int il = qid[nn], ir = qid[ib];
+            long long pl = pot[nn], pb = pot[ib];
+            qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
+            qr[nn] = r; qv[nn] = v; qid[nn] = ir; pot[nn] = pb;
         }
+        __syncwarp();
+        rs = r;
+        es = v.w;
+        have = true;
+        n = nn;
+    }
+    __syncwarp();
+    if (lane == 0) write_record(A, g, n, m, dcm, qr[imin], nrem);
+    __syncwarp();
+}
+
+template <int BS>
+struct BlockShared {
+    ArgRed smax[BS / 32], smin[BS / 32];
+    float4 s_r;
+    float s_eps;
+    float s_cm[6];
+    int s_n, s_go, s_have, s_imin;
+    double d_cm[6], d_mass;
+    double part[BS / 32][7];
+};
+
+// A large group, the whole block.
+template <int BS>
+__device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
+{
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int s = A.gstart[g], n0 = A.gcount[g];
+    float4 *qr = A.qr + s;
+    float4 *qv = A.qv + s;
+    int *qid = A.qid + s;
+    long long *pot = A.pot + s;
+    double m = 0.0, c[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = tid; i < n0; i += BS) {
+        float4 r = qr[i], v = qv[i];
+        m += r.w;
+        c[0] += fmul(r.w, r.x); c[1] += fmul(r.w, r.y); c[2] += fmul(r.w, r.z);
+        c[3] += fmul(r.w, v.x); c[4] += fmul(r.w, v.y); c[5] += fmul(r.w, v.z);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        m += __shfl_xor_sync(SKID_FULL, m, o);
+        for (int d = 0; d < 6; ++d) c[d] += __shfl_xor_sync(SKID_FULL, c[d], o);
+    }
+    __syncthreads();
+    if (lane == 0) {
+        S.part[w][0] = m;
+        for (int d = 0; d < 6; ++d) S.part[w][1 + d] = c[d];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // warp partials in warp order: the same sums on every run
+        double t[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < BS / 32; ++k)
+            for (int d = 0; d < 7; ++d) t[d] += S.part[k][d];
+        S.d_mass = t[0];
+        for (int d = 0; d < 6; ++d) {
+            S.d_cm[d] = t[1 + d] / t[0];
+            S.s_cm[d] = (float)S.d_cm[d];
+        }
+        S.s_n = n0;
+        S.s_have = 0;
+        S.s_go = 1;
+    }
+    __syncthreads();
+    int nrem = 0;
+    const bool exact = n0 <= EXACT_E_MAX;
+    const double opz_d = 1.0 + (double)A.z, inv_d = 1.0 / (double)A.scale;
+    for (;;) {
+        const int n = S.s_n;
+        const bool have = S.s_have != 0;
+        const float4 rs = S.s_r;
+        const float es = S.s_eps;
+        double dcm[6];
+        float scm[6];
+        for (int d = 0; d < 6; ++d) { dcm[d] = S.d_cm[d]; scm[d] = S.s_cm[d]; }
+        ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
+        for (int i = tid; i < n; i += BS) {
+            float4 r = qr[i], v = qv[i];
+            long long p = pot[i];
+            if (have && A.subpot) {
+                p = sub_pot(A, rs, es, r, v, p);
+                pot[i] = p;
+            }
+            float E = member_energy(exact, A, r, v, p, dcm, scm, inv_d, opz_d);
+            if (E > mx.v) { mx.v = E; mx.i = i; }
+            if (E < mn.v) { mn.v = E; mn.i = i; }
+        }
+        mx = warp_argmax(mx);
+        mn = warp_argmin(mn);
+        if (lane == 0) { S.smax[w] = mx; S.smin[w] = mn; }
         __syncthreads();
         if (tid == 0) {
-            for (int d = 0; d < 6; ++d) {
-                d_cm[d] /= d_mass;
-                s_cm[d] = (float)d_cm[d];
+            ArgRed a = S.smax[0], b = S.smin[0];
+            for (int k = 1; k < BS / 32; ++k) {
+                ArgRed x = S.smax[k], y = S.smin[k];
+                if (x.v > a.v || (x.v == a.v && x.i < a.i)) a = x;
+                if (y.v < b.v || (y.v == b.v && y.i < b.i)) b = y;
             }
-            s_n = n0;
-            s_have = 0;
-            s_go = 1;
-        }
-        __syncthreads();
-        int nrem = 0;
-        const bool exact = n0 <= EXACT_E_MAX;
-        const double opz_d = 1.0 + (double)A.z;
-        const double inv_d = 1.0 / (double)A.scale;
-        while (true) {
-            int n = s_n;
-            bool have = s_have != 0;
-            float4 rs = s_r;
-            float es = s_eps;
-            float cm0 = s_cm[0], cm1 = s_cm[1], cm2 = s_cm[2];
-            float vm0 = s_cm[3], vm1 = s_cm[4], vm2 = s_cm[5];
-            double dc0 = d_cm[0], dc1 = d_cm[1], dc2 = d_cm[2];
-            double dv0m = d_cm[3], dv1m = d_cm[4], dv2m = d_cm[5];
-            ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
-            for (int i = tid; i < n; i += RM_THREADS) {
-                float4 r = qr[i], v = qv[i];
-                long long p = pot[i];
-                if (have && A.subpot) {
-                    // kdSubPot (grav.c:44-59)
-                    float d2 = d2of(fsub(rs.x, r.x), fsub(rs.y, r.y), fsub(rs.z, r.z));
-                    float dir = spline_pot(d2, fadd(es, v.w), A.plummer);
-                    p -= fx(fmul(fmul(A.G, rs.w), dir), A.scale);
-                    pot[i] = p;
-                }
-                float E;
-                if (exact) {
-                    double fs = A.fShift, fc = A.fCosmo;
-                    float dv0 = (float)(fs * ((double)v.x - dv0m) + fc * ((double)r.x - dc0));
-                    float dv1 = (float)(fs * ((double)v.y - dv1m) + fc * ((double)r.y - dc1));
-                    float dv2 = (float)(fs * ((double)v.z - dv2m) + fc * ((double)r.z - dc2));
-                    float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
-                    E = (float)(0.5 * (double)dd - ((double)p * inv_d) * opz_d);
+            S.s_imin = b.v < 1.0f ? b.i : 0;
+            if (!(a.v >= 0.0f) || A.nounbind || n == 0) {
+                S.s_go = 0;
+            } else {
+                int ib = a.i;
+                float4 r = qr[ib], v = qv[ib];
+                A.grp[qid[ib]] = 0;
+                ++nrem;
+                int nn = n - 1;
+                if (nn == 0) {
+                    S.d_mass = 0.0;
+                    for (int d = 3; d < 6; ++d) S.d_cm[d] = 0.0;
+                    S.s_go = 0;
                 } else {
-                    float dv0 = A.fShift * (v.x - vm0) + A.fCosmo * (r.x - cm0);
-                    float dv1 = A.fShift * (v.y - vm1) + A.fCosmo * (r.y - cm1);
-                    float dv2 = A.fShift * (v.z - vm2) + A.fCosmo * (r.z - cm2);
-                    float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
-                    E = 0.5f * dd - (__ll2float_rn(p) * A.inv_scale) * A.opz;
-                }
-                if (E > mx.v) { mx.v = E; mx.i = i; }
-                if (E < mn.v) { mn.v = E; mn.i = i; }
-            }
-            mx = warp_argmax(mx);
-            mn = warp_argmin(mn);
-            if (lane == 0) { smax[w] = mx; smin[w] = mn; }
-            __syncthreads();
-            if (tid == 0) {
-                ArgRed a = smax[0], b = smin[0];
-                for (int k = 1; k < RM_THREADS / 32; ++k) {
-                    ArgRed x = smax[k], y = smin[k];
-                    if (x.v > a.v || (x.v == a.v && x.i < a.i)) a = x;
-                    if (y.v < b.v || (y.v == b.v && y.i < b.i)) b = y;
-                }
-                // kd.c:1389-1409: fTotBig starts at -1, fTotMin at 1
-                s_imin = b.v < 1.0f ? b.i : 0;
-                if (!(a.v >= 0.0f) || A.nounbind || n == 0) {
-                    s_go = 0;
-                } else {
-                    int ib = a.i;
-                    float4 r = qr[ib], v = qv[ib];
-                    A.grp[qid[ib]] = 0;
-                    ++nrem;
-                    int nn = n - 1;
-                    if (nn == 0) {
-                        d_mass = 0.0;
-                        for (int d = 3; d < 6; ++d) d_cm[d] = 0.0;
-                        s_go = 0;
-                    } else {
-                        d_mass -= r.w;
-                        double f = (double)r.w / d_mass;
-                        d_cm[0] += f * (d_cm[0] - r.x);
-                        d_cm[1] += f * (d_cm[1] - r.y);
-                        d_cm[2] += f * (d_cm[2] - r.z);
-                        d_cm[3] += f * (d_cm[3] - v.x);
-                        d_cm[4] += f * (d_cm[4] - v.y);
-                        d_cm[5] += f * (d_cm[5] - v.z);
-                        for (int d = 0; d < 6; ++d) s_cm[d] = (float)d_cm[d];
-                        // swap with the last member (kd.c:1435-1440)
-                        float4 rl = qr[nn], vl = qv[nn];
-                        int il = qid[nn], ir = qid[ib];
-                        long long pl = pot[nn], pb = pot[ib];
-                        qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
-                        qr[nn] = r; qv[nn] = v; qid[nn] = ir; pot[nn] = pb;
-                        s_r = r;
-                        s_eps = v.w;
-                        s_have = 1;
+                    double mm = S.d_mass;
+                    for (int d = 0; d < 6; ++d) dcm[d] = S.d_cm[d];
+                    rcm_update(mm, dcm, r, v);
+                    S.d_mass = mm;
+                    for (int d = 0; d < 6; ++d) {
+                        S.d_cm[d] = dcm[d];
+                        S.s_cm[d] = (float)dcm[d];
                     }
-                    s_n = nn;
+                    float4 rl = qr[nn], vl = qv[nn];
+                    int il = qid[nn], ir = qid[ib];
+                    long long pl = pot[nn], pb = pot[ib];
+                    qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
+                    qr[nn] = r; qv[nn] = v; qid[nn] = ir; pot[nn] = pb;
+                    S.s_r = r;
+                    S.s_eps = v.w;
+                    S.s_have = 1;
                 }
+                S.s_n = nn;
             }
-            __syncthreads();
-            if (!s_go) break;
-        }
-        if (tid == 0) {
-            skid_group r = A.rec[g];
-            int n = s_n;
-            r.nMembers = n;
-            r.fMass = (float)d_mass;
-            r.vcm[0] = (float)d_cm[3];
-            r.vcm[1] = (float)d_cm[4];
-            r.vcm[2] = (float)d_cm[5];
-            float4 rb = qr[s_imin];
-            float hx = A.hP.x;   // kd.c:1452-1456 wraps every axis with hx
-            r.rBound[0] = wrap_h(fadd(rb.x, r.rel[0]), hx);
-            r.rBound[1] = wrap_h(fadd(rb.y, r.rel[1]), hx);
-            r.rBound[2] = wrap_h(fadd(rb.z, r.rel[2]), hx);
-            A.rec[g] = r;
-            if (nrem) atomicAdd(A.d_unbound, nrem);
         }
         __syncthreads();
+        if (!S.s_go) break;
+    }
+    if (tid == 0) {
+        double dcm[6];
+        for (int d = 0; d < 6; ++d) dcm[d] = S.d_cm[d];
+        write_record(A, g, S.s_n, S.d_mass, dcm, qr[S.s_imin], nrem);
+    }
+    __syncthreads();
+}
+
+// Persistent removal: queue items [0, nbig) are large groups (one block
+// each), then chunks of BS/32 small groups (one warp each), all largest
+// first.  With A.single > 0 one block processes just that group.
+template <int BS>
+__global__ void __launch_bounds__(BS) remove_kernel(RemoveArgs A)
+{
+    __shared__ BlockShared<BS> S;
+    __shared__ int s_item;
+    constexpr int W = BS / 32;
+    if (A.single > 0) {
+        block_group<BS>(A, A.single, S);
+        return;
+    }
+    const int nvalid = A.d_cnt[0], nbig = A.d_cnt[1];
+    const int nitems = nbig + (nvalid - nbig + W - 1) / W;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(A.d_queue, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= nitems) break;
+        if (item < nbig) {
+            block_group<BS>(A, (int)A.order[item], S);
+        } else {
+            int k = nbig + (item - nbig) * W + (threadIdx.x >> 5);
+            if (k < nvalid) warp_group(A, (int)A.order[k]);
+        }
     }
 }
 
+template <int BS>
+cudaError_t launch_remove(const RemoveArgs &A, int blocks, cudaStream_t st)
+{
+    remove_kernel<BS><<<blocks, BS, 0, st>>>(A); note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t remove_launch(const RemoveArgs &A, int bs, int blocks, cudaStream_t st)
+{
+    switch (bs) {
+    case 128: return launch_remove<128>(A, blocks, st);
+    case 512: return launch_remove<512>(A, blocks, st);
+    case 1024: return launch_remove<1024>(A, blocks, st);
+    default: return launch_remove<256>(A, blocks, st);
+    }
+}
+
+int remove_blocks(int bs)
+{
+    int perSM = 0;
+    switch (bs) {
+    case 128: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<128>, 128, 0); break;
+    case 512: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<512>, 512, 0); break;
+    case 1024: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<1024>, 1024, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<256>, 256, 0); break;
+    }
+    return num_sms() * (perSM > 0 ? perSM : 1);
+}
+
 }  // namespace
+
+// Candidate removal schedules (tw, BS) for the autotuner.
+static const int kTW[] = {0, 32, 64, 128};
+static const int kBS[] = {256, 512, 1024};
 
 cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *pos4,
                        const float4 *vel4, Tree &ut, const UnbindParams &P, int *grp,
@@ -425,21 +686,23 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     int ng = G.nGroup;
     if ((e = dalloc(U.qr, nslots)) || (e = dalloc(U.qv, nslots)) || (e = dalloc(U.qid, nslots)) ||
         (e = dalloc(U.pot, nslots)) || (e = dalloc(U.scnt, ng)) || (e = dalloc(U.soff, ng + 1)) ||
-        (e = dalloc(U.nt, ng)) || (e = dalloc(U.toff, ng + 1)) || (e = dalloc(U.cnt, 4)))
+        (e = dalloc(U.nt, ng)) || (e = dalloc(U.toff, ng + 1)) || (e = dalloc(U.cnt, 8)) ||
+        (e = dalloc(U.order, ng)))
         return e;
     float3 hP = make_float3((float)(0.5 * (double)P.period.x), (float)(0.5 * (double)P.period.y),
                             (float)(0.5 * (double)P.period.z));
-    prep_members<<<grid_for(nslots), 256, 0, st>>>(G.members.p, gof, nslots, pos4, vel4, G.rec.p,
-                                                   hP, U.qr.p, U.qv.p); skid::note_launch();
-    if ((e = cudaMemcpyAsync(U.qid.p, G.members.p, nslots * sizeof(int), cudaMemcpyDeviceToDevice,
-                             st)))
-        return e;
+    auto prep = [&]() -> cudaError_t {
+        prep_members<<<grid_for(nslots), 256, 0, st>>>(G.members.p, gof, nslots, pos4, vel4, G.rec.p,
+                                                       hP, U.qr.p, U.qv.p); note_launch();
+        return cudaMemcpyAsync(U.qid.p, G.members.p, nslots * sizeof(int), cudaMemcpyDeviceToDevice, st);
+    };
+    if ((e = prep())) return e;
     // scoop lists
     float fBall2 = P.fScoop * P.fScoop;
     float3 hL = make_float3(0.5f * P.period.x, 0.5f * P.period.y, 0.5f * P.period.z);
     scoop_kernel<<<grid_for(ng), 256, 0, st>>>(ut.view(), U.usoft.p, G.rec.p, G.count.p, ng, P.nmax,
                                               fBall2, P.period, hL, P.per, 0, U.scnt.p, nullptr,
-                                              nullptr, nullptr); skid::note_launch();
+                                              nullptr, nullptr); note_launch();
     if ((e = scan_exclusive(U.scnt.p, U.soff.p, ng, U.cnt.p, ss, st))) return e;
     int nscoop = 0;
     if ((e = cudaMemcpyAsync(&nscoop, U.cnt.p, sizeof(int), cudaMemcpyDeviceToHost, st))) return e;
@@ -449,23 +712,29 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     if (nscoop > 0)
         scoop_kernel<<<grid_for(ng), 256, 0, st>>>(ut.view(), U.usoft.p, G.rec.p, G.count.p, ng,
                                                   P.nmax, fBall2, P.period, hL, P.per, 1, U.scnt.p,
-                                                  U.soff.p, U.slist.p, U.ssoft.p); skid::note_launch();
-    // potential work items (group, tile)
-    pot_ntiles<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, U.nt.p); skid::note_launch();
-    if ((e = scan_exclusive(U.nt.p, U.toff.p, ng, U.cnt.p + 1, ss, st))) return e;
-    int nitems = 0;
-    if ((e = cudaMemcpyAsync(&nitems, U.cnt.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st)))
+                                                  U.soff.p, U.slist.p, U.ssoft.p); note_launch();
+    // groups by descending size
+    if ((e = dalloc(ss.k0, ng)) || (e = dalloc(ss.v0, ng)) || (e = dalloc(ss.k1, ng)) ||
+        (e = dalloc(ss.v1, ng)))
         return e;
+    sched_keys<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, ss.k0.p, ss.v0.p); note_launch();
+    if ((e = radix_sort(ss, ng, 32, st))) return e;
+    if ((e = cudaMemcpyAsync(U.order.p, ss.v0.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st)))
+        return e;
+    if ((e = cudaMemsetAsync(U.cnt.p + 2, 0, 2 * sizeof(int), st))) return e;
+    sched_counts<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, 1 << 30, U.cnt.p + 2); note_launch();
+    // potential items, largest groups first
+    pot_nitems<<<grid_for(ng), 256, 0, st>>>(U.order.p, U.cnt.p + 2, G.count.p, ng, U.nt.p); note_launch();
+    if ((e = scan_exclusive(U.nt.p, U.toff.p, ng, U.cnt.p + 1, ss, st))) return e;
+    int hc[3] = {0, 0, 0};
+    if ((e = cudaMemcpyAsync(hc, U.cnt.p + 1, 2 * sizeof(int), cudaMemcpyDeviceToHost, st))) return e;
     if ((e = cudaStreamSynchronize(st))) return e;
+    const int nitems = hc[0], nvalid = hc[1];
     if ((e = dalloc(U.items, nitems > 0 ? nitems : 1))) return e;
-    if (nitems > 0) {
-        pot_items<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, U.toff.p, U.items.p); skid::note_launch();
-        int blocks = nitems < num_sms() * 16 ? nitems : num_sms() * 16;
-        pot_kernel<<<blocks, POT_TILE, 0, st>>>(U.items.p, U.cnt.p + 1, G.start.p, G.count.p, U.qr.p,
-                                                U.qv.p, U.soff.p, U.scnt.p, U.slist.p, U.ssoft.p,
-                                                P.G, P.plummer, P.scale, U.pot.p); skid::note_launch();
-    }
-    // removal loop, one block per group
+    if (nitems > 0)
+        pot_fill<<<grid_for(nvalid), 256, 0, st>>>(U.order.p, U.cnt.p + 2, G.count.p, U.toff.p,
+                                                   U.items.p); note_launch();
+
     RemoveArgs A;
     A.gstart = G.start.p;
     A.gcount = G.count.p;
@@ -489,10 +758,110 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     A.plummer = P.plummer;
     A.subpot = P.subpot;
     A.nounbind = P.nounbind;
-    if ((e = cudaMemsetAsync(d_unbound, 0, sizeof(int), st))) return e;
-    int blocks = ng - 1 < num_sms() * 8 ? ng - 1 : num_sms() * 8;
-    if (blocks > 0) remove_kernel<<<blocks, RM_THREADS, 0, st>>>(A); skid::note_launch();
-    return cudaGetLastError();
+    A.order = U.order.p;
+    A.d_cnt = U.cnt.p + 4;
+    A.d_queue = U.cnt.p + 6;
+    A.single = 0;
+
+    const int potBlocks = nitems < num_sms() * 16 ? (nitems > 0 ? nitems : 1) : num_sms() * 16;
+    auto potentials = [&]() -> cudaError_t {
+        cudaError_t e2 = cudaMemsetAsync(U.pot.p, 0, nslots * sizeof(long long), st);
+        if (e2 || nitems <= 0) return e2;
+        pot_sym_kernel<<<potBlocks, POT_TILE, 0, st>>>(U.items.p, U.cnt.p + 1, -1, G.start.p, G.count.p,
+                                                       U.qr.p, U.qv.p, U.soff.p, U.scnt.p, U.slist.p,
+                                                       U.ssoft.p, P.G, P.plummer, P.scale, U.pot.p); note_launch();
+        return cudaGetLastError();
+    };
+    auto removal = [&](int tw, int bs) -> cudaError_t {
+        cudaError_t e2;
+        if ((e2 = cudaMemsetAsync(U.cnt.p + 4, 0, 3 * sizeof(int), st))) return e2;
+        sched_counts<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, tw, U.cnt.p + 4); note_launch();
+        if ((e2 = cudaMemsetAsync(d_unbound, 0, sizeof(int), st))) return e2;
+        if (nvalid <= 0) return cudaSuccess;
+        return remove_launch(A, bs, remove_blocks(bs), st);
+    };
+
+    if (P.per_group) {
+        // the reference's serial loop on the GPU: two launches per group
+        std::vector<uint32_t> order(ng);
+        std::vector<int> ioff(ng + 1);
+        if ((e = cudaMemcpyAsync(order.data(), U.order.p, ng * sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaMemcpyAsync(ioff.data(), U.toff.p, ng * sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaStreamSynchronize(st)))
+            return e;
+        ioff[nvalid] = nitems;
+        if ((e = cudaMemsetAsync(U.pot.p, 0, nslots * sizeof(long long), st))) return e;
+        if ((e = cudaMemsetAsync(d_unbound, 0, sizeof(int), st))) return e;
+        for (int k = 0; k < nvalid; ++k) {
+            int cnt = ioff[k + 1] - ioff[k];
+            pot_sym_kernel<<<cnt < num_sms() * 16 ? cnt : num_sms() * 16, POT_TILE, 0, st>>>(
+                U.items.p + ioff[k], nullptr, cnt, G.start.p, G.count.p, U.qr.p, U.qv.p, U.soff.p,
+                U.scnt.p, U.slist.p, U.ssoft.p, P.G, P.plummer, P.scale, U.pot.p); note_launch();
+            RemoveArgs A1 = A;
+            A1.single = (int)order[k];
+            if ((e = remove_launch(A1, 256, 1, st))) return e;
+        }
+        return cudaGetLastError();
+    }
+
+    if ((e = potentials())) return e;
+    int tw = P.tw, bs = P.bs;
+    if ((tw < 0 || bs < 0) && U.tuned_bs > 0) {
+        if (tw < 0) tw = U.tuned_tw;
+        if (bs < 0) bs = U.tuned_bs;
+    }
+    if (tw < 0 || bs < 0) {
+        // autotune: time every candidate removal schedule on these groups,
+        // restoring the inputs between runs, then keep the fastest
+        if ((e = dalloc(U.pot_save, nslots)) || (e = dalloc(U.rec_save, ng)) ||
+            (e = dalloc(U.grp_save, P.n > 0 ? P.n : 1)))
+            return e;
+        if ((e = cudaMemcpyAsync(U.pot_save.p, U.pot.p, nslots * sizeof(long long), cudaMemcpyDeviceToDevice, st)) ||
+            (e = cudaMemcpyAsync(U.rec_save.p, G.rec.p, ng * sizeof(skid_group), cudaMemcpyDeviceToDevice, st)) ||
+            (e = cudaMemcpyAsync(U.grp_save.p, grp, P.n * sizeof(int), cudaMemcpyDeviceToDevice, st)))
+            return e;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = FLT_MAX;
+        int btw = 32, bbs = 256;
+        for (int a : kTW) {
+            if (P.tw >= 0 && a != P.tw) continue;
+            for (int b : kBS) {
+                if (P.bs >= 0 && b != P.bs) continue;
+                if ((e = cudaMemcpyAsync(U.pot.p, U.pot_save.p, nslots * sizeof(long long), cudaMemcpyDeviceToDevice, st)) ||
+                    (e = cudaMemcpyAsync(G.rec.p, U.rec_save.p, ng * sizeof(skid_group), cudaMemcpyDeviceToDevice, st)) ||
+                    (e = cudaMemcpyAsync(grp, U.grp_save.p, P.n * sizeof(int), cudaMemcpyDeviceToDevice, st)) ||
+                    (e = prep()))
+                    break;
+                cudaEventRecord(e0, st);
+                if ((e = removal(a, b))) break;
+                cudaEventRecord(e1, st);
+                if ((e = cudaEventSynchronize(e1))) break;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                U.tune_ms[U.ntune < 16 ? U.ntune : 15] = ms;
+                ++U.ntune;
+                if (ms < best) { best = ms; btw = a; bbs = b; }
+            }
+            if (e) break;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (e) return e;
+        U.tuned_tw = btw;
+        U.tuned_bs = bbs;
+        tw = btw;
+        bs = bbs;
+        if ((e = cudaMemcpyAsync(U.pot.p, U.pot_save.p, nslots * sizeof(long long), cudaMemcpyDeviceToDevice, st)) ||
+            (e = cudaMemcpyAsync(G.rec.p, U.rec_save.p, ng * sizeof(skid_group), cudaMemcpyDeviceToDevice, st)) ||
+            (e = cudaMemcpyAsync(grp, U.grp_save.p, P.n * sizeof(int), cudaMemcpyDeviceToDevice, st)) ||
+            (e = prep()))
+            return e;
+    }
+    U.used_tw = tw;
+    U.used_bs = bs;
+    return removal(tw, bs);
 }
 
 }  // namespace skid

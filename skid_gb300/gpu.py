@@ -86,6 +86,7 @@ SIGNATURES = {
     "skid_restart": [_V],
     "skid_field_stats": [_V, C.c_int, C.POINTER(C.c_ulonglong)],
     "skid_set_option": [_V, C.c_char_p, C.c_double],
+    "skid_get_option": [_V, C.c_char_p, _D],
     "skid_knn_ball2": [_V, C.c_int, _F, C.c_int, _F],
     "skid_field": [_V, C.c_int, _F, _F],
     "skid_fof_points": [_V, C.c_int, _F, C.c_float, _I, _I],
@@ -206,6 +207,11 @@ class Context:
 
     def set_option(self, name: str, value: float):
         self._call("skid_set_option", self.h, name.encode(), float(value))
+
+    def get_option(self, name: str) -> float:
+        v = C.c_double()
+        self._call("skid_get_option", self.h, name.encode(), C.byref(v))
+        return v.value
 
     def field_stats(self, enable=True):
         """Counts so far (nodes, leaves, tests, hits); then restart counting."""

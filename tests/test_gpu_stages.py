@@ -83,3 +83,31 @@ def test_unbind_isolated(gpu_ready, name):
     np.testing.assert_allclose(rec["fMass"][1:][keep], og["fMass"][1:][keep], rtol=1e-6)
     np.testing.assert_allclose(rec["vcm"][1:][keep], og["vcm"][1:][keep], rtol=1e-4, atol=1e-6)
     assert np.abs(rec["rBound"][1:][keep] - og["rBound"][1:][keep]).max() < 1e-5
+
+
+@pytest.mark.parametrize("name", ["dark4k_periodic", "mixed6k"])
+def test_schedules_and_unfused_forms_agree(gpu_ready, name):
+    """Every removal schedule the autotuner can pick, the per-group launch
+    loop, and the unfused field-then-move form give the same catalogue."""
+    from skid_gb300 import pipeline
+    snap, opts, ref, counts, meta = gc.load(name)
+    settings = [{}, {"unbind_warp_max": 0, "unbind_block": 256},
+                {"unbind_warp_max": 128, "unbind_block": 1024},
+                {"unbind_warp_max": 32, "unbind_block": 512},
+                {"unbind_warp_max": 64, "unbind_block": 128},
+                {"unbind_per_group": 1}, {"field_unfused": 1}]
+    outs = []
+    for setting in settings:
+        with _ctx(opts) as ctx:
+            for k, v in setting.items():
+                ctx.set_option(k, v)
+            res = pipeline.run(snap, opts, ctx=ctx)
+            outs.append((res.grp.copy(), res.groups.copy(), ctx.get_option("unbind_warp_max"),
+                         ctx.get_option("unbind_block"), ctx.get_option("unbind_tune_candidates")))
+    base_grp, base_rec = outs[0][0], outs[0][1]
+    assert outs[0][2] in (0, 32, 64, 128) and outs[0][3] in (256, 512, 1024)
+    assert outs[0][4] == 12
+    for (grp, rec, *_), setting in zip(outs[1:], settings[1:]):
+        assert np.array_equal(grp, base_grp), setting
+        for f in ("nMembers", "fMass", "rCenter", "rBound", "vcm", "fRadius"):
+            assert np.array_equal(rec[f], base_rec[f]), (setting, f)
