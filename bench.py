@@ -18,9 +18,20 @@ ranks (torchrun), every rank runs an independent replica on its own GPU
 (the path does not shard within one snapshot): value = N x particles / max
 time over ranks.
 
+The metric compares two GPU forms at identical accuracy: the default form
+(moves driven by the fused density-field adjoint kernel, every unbinding
+group in one autotuned launch) is ``value``; the plain form (a separate
+gradient pass then a move kernel every step, and one potential and one
+removal launch per group, the reference's serial loop) is timed the same way
+and reported under ``config.plain`` with its per-particle catalogue agreement
+with the default form.  A run with ``-nsp`` (every scatterer kept) is
+reported under ``config.nsp``.
+
 ``--impl reference`` times the reference algorithm on the host cores: the
 reference's own binary cannot be built on this host (its sources are not
-here), so the oracle's C restatement of it runs, single-threaded like skid.
+here), so the oracle's C restatement of it runs: skid is single-threaded, so
+each host core runs one independent copy of the sample and the value is the
+aggregate particles/s.
 """
 from __future__ import annotations
 
@@ -58,6 +69,21 @@ def workload(n):
 def flags():
     from skid_gb300 import synth
     return list(synth.WORKLOAD_FLAGS[1])
+
+
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "field_kernel_skid_config1_2e21.md")
+
+
+def field_traffic():
+    """Mean DRAM bytes (read + write) per field_kernel launch over one full
+    run, from the committed ncu launch capture (or None)."""
+    import re
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            m = re.search(r"traffic_bytes_per_launch_mean:\s*([0-9.eE+]+)", f.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
 
 
 def measured_peak():
@@ -143,6 +169,22 @@ def cpu_baseline(n_sample=CPU_SAMPLE_N, repeats=1):
                       f"{best:.1f} s"}
 
 
+def reduce_max(x: float, world: int, device="cpu") -> float:
+    """Max of x over ranks (the slowest replica sets the job's time)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world: int, n: int, steps: int, total_ms: float) -> float:
+    """Whole-job particles/s: every rank processes its own n-particle replica per step."""
+    return world * n * steps / (total_ms / 1000.0)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -150,37 +192,62 @@ def dist_setup():
     return world, rank, local
 
 
+REF_SAMPLE_N = 1 << 15
+_ref_snap = None
+
+
+def _ref_init(n):
+    """Pool worker: build this core's copy of the sample once."""
+    global _ref_snap
+    from skid_gb300 import synth
+    _ref_snap = synth.make_snapshot(workload(n))
+
+
+def _ref_task(_):
+    from oracle import oracle
+    from skid_gb300.options import Options
+    t = time.perf_counter()
+    oracle.run(_ref_snap, Options.parse(flags()))
+    return time.perf_counter() - t
+
+
 def run_reference(args):
+    """The reference algorithm (oracle C restatement, single-threaded like
+    skid) on every host core: each core runs one copy of a bounded sample of
+    the workload per step; value = cores x particles / wall time."""
+    import multiprocessing as mp
     world, rank, local = dist_setup()
     if rank != 0:
         return 0
     from oracle import oracle
-    from skid_gb300 import synth
-    from skid_gb300.options import Options
     oracle.build()
-    n = CPU_SAMPLE_N
-    snap = synth.make_snapshot(workload(n))
-    opts = Options.parse(flags())
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        oracle.run(snap, opts)
-    times = []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        oracle.run(snap, opts)
-        times.append(time.perf_counter() - t)
-    tot = sum(times)
-    value = n * len(times) / tot
+    n = REF_SAMPLE_N
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(n,)) as pool:
+        for _ in range(min(args.warmup, 1)):
+            pool.map(_ref_task, range(cores), chunksize=1)
+        walls, per_core = [], []
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            ts = pool.map(_ref_task, range(cores), chunksize=1)
+            walls.append(time.perf_counter() - t)
+            per_core.extend(ts)
+    tot = sum(walls)
+    value = cores * n * len(walls) / tot
+    sample = (f"{cores} concurrent copies (one per host core) of a {n}-particle box generated "
+              f"like the 2^21 workload ({max(1, round(800 * n / N_DEFAULT))} halos), same flags, "
+              f"oracle C restatement of skid (the reference binary cannot be built on this "
+              f"host); {statistics.mean(per_core):.1f} s per copy")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / len(times),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / len(walls),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"skid on a {n}-particle sample of the 2^21 workload "
+            "config": {"workload": f"skid on {cores} x {n}-particle samples of the 2^21 workload "
                                    f"(NFW halos + background), periodic unit box",
-                       "flags": " ".join(flags()), "n_particles": n},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"{n} particles per step, oracle C restatement of "
-                                       f"skid (the reference binary is not buildable here), "
-                                       f"single-threaded like skid"},
+                       "flags": " ".join(flags()), "n_particles": n, "copies": cores},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -253,13 +320,8 @@ def run_gpu(args):
     barrier()
     t_after = ctx.timings()
     launches = t_after["kernel_launches"] - l0
-    tot_ms = sum(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([tot_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tot_ms = float(tt.item())
-    value = world * n * args.steps / (tot_ms / 1000.0)
+    tot_ms = reduce_max(sum(step_ms), world, "cuda")
+    value = job_value(world, n, args.steps, tot_ms)
 
     # roofline of the dominant kernel (move field): algorithmic bytes / event time
     f_ms = t_after["field_ms"] - t_before["field_ms"]
@@ -281,14 +343,52 @@ def run_gpu(args):
         e1.synchronize()
         e2e_ms.append(e0.elapsed_time(e1))
     barrier()
-    e2e_tot = sum(e2e_ms)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([e2e_tot], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_tot = float(tt.item())
+    e2e_tot = reduce_max(sum(e2e_ms), world, "cuda")
     h2d = n * (3 + 3 + 1 + 1 + 1) * 4
     d2h = n * 4 + (r.n_group + 1) * gpu.GROUP_DTYPE.itemsize
+
+    # ---- the plain GPU form, same workload, same timing ----
+    def timed_runs(c, o, k):
+        strm = torch.cuda.ExternalStream(c.stream_ptr(), device=torch.device("cuda", local))
+        ms, out = [], None
+        for _ in range(k):
+            flush_l2()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(strm)
+            out = pipeline.run(snap, o, ctx=c, upload=False)
+            e1.record(strm)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms, out
+
+    plain = nsp = None
+    if not args.no_compare:
+        from skid_gb300 import compare
+        pctx = gpu.Context(period=1.0, nSmooth=opts.nSmooth, device=local)
+        pctx.set_option("field_unfused", 1)
+        pctx.set_option("unbind_per_group", 1)
+        pipeline.run(snap, opts, ctx=pctx)            # warm-up, uploads the snapshot
+        p_ms, pres = timed_runs(pctx, opts, args.steps)
+        pl = pctx.timings()["kernel_launches"]
+        pctx.close()
+        m = compare.match_groups(res.grp, pres.grp)
+        plain = {"form": "separate gradient pass then move kernel every step; one potential "
+                         "and one removal launch per group",
+                 "value": world * n * len(p_ms) / (sum(p_ms) / 1000.0),
+                 "ms_per_step": sum(p_ms) / len(p_ms), "agreement": m.agreement,
+                 "same_groups": bool(m.same_groups()), "groups": pres.n_group,
+                 "unbind_ms": round(float(pres.timings["unbind_ms"]), 3),
+                 "moving_ms": round(float(pres.timings["moving_ms"]), 3)}
+        opts_nsp = Options.parse(flags() + ["-nsp"])
+        pipeline.run(snap, opts_nsp, ctx=ctx, upload=False)   # warm-up (graphs for -nsp)
+        n_ms, nres = timed_runs(ctx, opts_nsp, 1)
+        nsp = {"value": world * n / (n_ms[0] / 1000.0), "ms_per_step": n_ms[0],
+               "groups": nres.n_group, "iterations": nres.counts.get("nIter"),
+               "stage_ms": {k: round(float(nres.timings[k]), 3) for k in
+                            ("density_ms", "moving_ms", "unbind_ms")}}
+    sched = {"unbind_warp_max": ctx.get_option("unbind_warp_max"),
+             "unbind_block": ctx.get_option("unbind_block")}
 
     if rank != 0:
         ctx.close()
@@ -307,13 +407,16 @@ def run_gpu(args):
                    "unbound": res.counts.get("nUnbound"), "iterations": res.counts.get("nIter"),
                    "stage_ms": {k: round(float(tm[k]), 3) for k in
                                 ("density_ms", "moving_ms", "fof_ms", "micro_ms", "groups_ms",
-                                 "unbind_ms", "toosmall_ms")}},
-        "e2e": {"value": world * n * args.steps / (e2e_tot / 1000.0), "unit": UNIT,
+                                 "unbind_ms", "toosmall_ms")},
+                   "form": "fused density-field adjoint + move kernel; every unbinding group "
+                           "in one autotuned launch",
+                   "unbind_schedule": sched, "plain": plain, "nsp": nsp},
+        "e2e": {"value": job_value(world, n, args.steps, e2e_tot), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_tot / args.steps},
         "roofline": {"bound": "hbm", "kernel": "field_kernel (move-field gather + move)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": field_traffic(),
                      "launches": f_launch, "avg_launch_ms": f_ms / max(f_launch, 1),
                      "algorithmic_bytes_per_launch": f_bytes / max(f_launch, 1)},
         "gpu_launches": launches,
@@ -337,6 +440,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT, help="particles (default 2^21)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the plain-form and -nsp comparison runs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
