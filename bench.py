@@ -432,6 +432,50 @@ def run_gpu(args):
     return 0
 
 
+def run_batch(args):
+    """Config 2: independent periodic subvolumes of uneven sizes (N log-uniform
+    in [2^14, 2^20], halos proportional to N, nSmooth from {32, 64, 128},
+    tau = 0.5 N^(-1/3)) through skid_batch_run, host buffers in and out
+    (end to end).  Compares nWorkers concurrent pipelines with one."""
+    from skid_gb300 import build, gpu, synth
+    from skid_gb300.options import Options
+    build.build_lib()
+    specs = synth.subvolume_specs(args.n_vol)
+    t0 = time.perf_counter()
+    vols = [(synth.make_snapshot(spec), k, tau) for spec, k, tau in specs]
+    gen_s = time.perf_counter() - t0
+    ntot = sum(v[0].n for v in vols)
+    base = Options.parse(["-tau", "0.01", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
+                          "-H", f"{synth.hubble_for(0.3):.6g}"])
+    gpu.batch_run(vols[:4], base, n_workers=min(4, args.workers))     # warm-up
+    out = {}
+    for w in (args.workers, 1):
+        best = None
+        for _ in range(max(1, args.steps)):
+            t = time.perf_counter()
+            res = gpu.batch_run(vols, base, n_workers=w)
+            dt = time.perf_counter() - t
+            best = dt if best is None else min(best, dt)
+        out[w] = (best, res)
+    wbest, res = out[args.workers]
+    sbest, sres = out[1]
+    same = all(np.array_equal(a["grp"], b["grp"]) for a, b in zip(res, sres))
+    line = {"metric": "particles/s end-to-end SKID, batched subvolumes", "value": ntot / wbest,
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 1,
+            "ms_per_step": 1000 * wbest, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{len(vols)} periodic subvolumes, N log-uniform in [2^14, 2^20] "
+                                   f"({ntot} particles), halos proportional to N, nSmooth in "
+                                   f"{{32, 64, 128}}, tau = 0.5 N^(-1/3)",
+                       "workers": args.workers, "sequential_value": ntot / sbest,
+                       "sequential_ms": 1000 * sbest, "identical_to_sequential": bool(same),
+                       "groups": int(sum(r["nGroup"] for r in res)),
+                       "device_ms_sum": float(sum(r["device_ms"] for r in res)),
+                       "generation_s": gen_s}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -442,9 +486,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain-form and -nsp comparison runs")
+    ap.add_argument("--workload", default="single", choices=["single", "batch"],
+                    help="batch: the uneven-subvolume workload through skid_batch_run")
+    ap.add_argument("--n-vol", type=int, default=96)
+    ap.add_argument("--workers", type=int, default=12)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
     return run_gpu(args)
 
 

@@ -214,6 +214,49 @@ int skid_get_option(skid_ctx *ctx, const char *name, double *value);
  * order their own work against the library's (no reference counterpart). */
 int skid_stream(skid_ctx *ctx, void **stream);
 
+/* ---- Batched volumes (no reference counterpart: the reference runs one
+ * snapshot per process). ---- */
+
+/* One independent volume of a batch: inputs as for skid_set_particles and
+ * skid_params, per-volume nSmooth and link length; outputs filled in. */
+typedef struct skid_volume {
+    int nGas, nDark, nStar;
+    double time;
+    const float *pos, *vel, *mass, *soft, *temp;   /* host, by iOrder; temp may be NULL */
+    float period[3], center[3];
+    int periodic;
+    int nSmooth;
+    float fTau, fCvg, fScoop;    /* fCvg, fScoop <= 0: tau/2 and 2 tau (main.c:337-342) */
+    int *grp;                    /* out: n final group ids, or NULL */
+    skid_group *groups;          /* out: groups_cap records (index 0 = ungrouped), or NULL */
+    int groups_cap;
+    int nGroup, nGroupFoF, nUnbound, nIter;   /* out */
+    float device_ms;             /* out: summed stage time of this volume */
+    int status;                  /* out: 0, or the SKID_E* code that stopped it */
+    char message[96];            /* out: the CUDA error text behind a SKID_ECUDA */
+} skid_volume;
+
+/* Flags shared by every volume of a batch (main.c:82-345 meanings). */
+typedef struct skid_batch_flags {
+    float fDensMin, fTempMax, fMassMax;
+    int nMembers, nMaxMembers;
+    int bGasAndDark, bGasOnly, bForceInitialCut, bNoUnbind, bNoCut;
+    int iSoftType, bEps;
+    float fEps;
+    float G, z, a, aH;           /* a = 1/(1+z), aH = a*H(a) (kd.c:1317-1318) */
+    int maxIter;                 /* 0: until every mover has converged */
+} skid_batch_flags;
+
+/* Run the whole pipeline on nVol independent volumes of uneven sizes on one
+ * GPU.  nWorkers host workers (each with its own context and CUDA stream)
+ * take volumes largest first from a shared queue, so the pipelines of many
+ * volumes run on the GPU at once; each worker's contexts reuse their device
+ * memory, captured graphs and autotuned unbinding schedule across volumes.
+ * Results per volume are those of the single-volume sequence.  Returns 0 if
+ * every volume succeeded, else the first failing volume's status. */
+int skid_batch_run(skid_volume *vols, int nVol, const skid_batch_flags *flags, int nWorkers,
+                   int device);
+
 /* ---- Adjoints (no reference counterpart). ---- */
 
 #define SKID_ADJ_RECOMPUTE 0   /* find the neighbour pairs by walking the tree again */

@@ -220,7 +220,8 @@ int skid_ctx::sync_check()
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail_cuda(e);
     unsigned s = 0;
-    e = cudaMemcpy(&s, d_status, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    e = cudaMemcpyAsync(&s, d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail_cuda(e);
     if (s & ST_TIMEOUT) return fail(SKID_ETIMEOUT);
     if (s & ST_OVERFLOW) return fail(SKID_EOVERFLOW);
@@ -406,17 +407,22 @@ int skid_create(skid_ctx **pctx, const skid_params *par)
     ctx->L = make_float3(par->period[0], par->period[1], par->period[2]);
     ctx->hL = make_float3(0.5f * par->period[0], 0.5f * par->period[1], 0.5f * par->period[2]);
     ctx->per = par->period[0] < 0.25f * FLT_MAX;
-    bool ok = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaMalloc((void **)&ctx->d_scal, SC_COUNT * sizeof(int)) == cudaSuccess &&
-              cudaMalloc((void **)&ctx->d_fbytes, 2 * sizeof(double)) == cudaSuccess &&
-              cudaEventCreate(&ctx->ev0) == cudaSuccess && cudaEventCreate(&ctx->ev1) == cudaSuccess;
-    for (cudaEvent_t &e : ctx->fev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    bool ok;
+    {
+        std::lock_guard<std::recursive_mutex> lk(device_mutex());
+        ok = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaMalloc((void **)&ctx->d_scal, SC_COUNT * sizeof(int)) == cudaSuccess &&
+             cudaMalloc((void **)&ctx->d_fbytes, 2 * sizeof(double)) == cudaSuccess &&
+             cudaEventCreate(&ctx->ev0) == cudaSuccess && cudaEventCreate(&ctx->ev1) == cudaSuccess;
+        for (cudaEvent_t &e : ctx->fev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    }
     if (!ok) {
         delete ctx;
         return SKID_ENOMEM;
     }
-    cudaMemset(ctx->d_scal, 0, SC_COUNT * sizeof(int));
-    cudaMemset(ctx->d_fbytes, 0, 2 * sizeof(double));
+    cudaMemsetAsync(ctx->d_scal, 0, SC_COUNT * sizeof(int), ctx->st);
+    cudaMemsetAsync(ctx->d_fbytes, 0, 2 * sizeof(double), ctx->st);
+    cudaStreamSynchronize(ctx->st);
     ctx->d_status = (unsigned *)(ctx->d_scal + SC_STATUS);
     ctx->C.d_n = ctx->d_scal + SC_NC;
     ctx->C.d_n2 = ctx->d_scal + SC_NC2;
@@ -739,6 +745,9 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
             ran = true;
         } else {
             cudaGraph_t g;
+            // no other thread may allocate (and so synchronise the device)
+            // while this stream is being captured
+            std::lock_guard<std::recursive_mutex> lk(device_mutex());
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             set_capturing(true);
             int rc = 0;
@@ -814,7 +823,8 @@ int skid_get_timings(skid_ctx *ctx, skid_timings *t)
     if (!ctx || !t) return SKID_EINVAL;
     *t = ctx->tim;
     double fb[2] = {0.0, 0.0};
-    if (cudaMemcpy(fb, ctx->d_fbytes, sizeof(fb), cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (cudaMemcpyAsync(fb, ctx->d_fbytes, sizeof(fb), cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->st) != cudaSuccess)
         return ctx->fail(SKID_ECUDA);
     t->gather_launches = (long long)fb[1];
     t->kernel_launches = launches_total();
@@ -825,12 +835,18 @@ int skid_get_timings(skid_ctx *ctx, skid_timings *t)
 int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4)
 {
     if (!ctx) return SKID_EINVAL;
-    if (!ctx->d_fstats && cudaMalloc((void **)&ctx->d_fstats, 4 * sizeof(unsigned long long)))
+    if (!ctx->d_fstats) {
+        std::lock_guard<std::recursive_mutex> lk(device_mutex());
+        if (cudaMalloc((void **)&ctx->d_fstats, 4 * sizeof(unsigned long long))) ctx->d_fstats = nullptr;
+    }
+    if (!ctx->d_fstats)
         return ctx->fail(SKID_ENOMEM);
     if (out4) {
-        CK(cudaMemcpy(out4, ctx->d_fstats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(out4, ctx->d_fstats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
     }
-    CK(cudaMemset(ctx->d_fstats, 0, 4 * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(ctx->d_fstats, 0, 4 * sizeof(unsigned long long), ctx->st));
     ctx->field_stats_on = enable != 0;   // graphs are recaptured on the next iteration
     return 0;
 }

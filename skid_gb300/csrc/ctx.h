@@ -244,6 +244,7 @@ struct skid_ctx {
     }
     void drop_graphs()
     {
+        std::lock_guard<std::recursive_mutex> lk(skid::device_mutex());
         for (auto &g : iter_graph)
             if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     }
@@ -329,6 +330,7 @@ struct skid_ctx {
         dfree(probe_t); dfree(knn_heap);
         dfree(adj.win); dfree(adj.w); dfree(adj.g); dfree(adj.out); dfree(adj.nbr); dfree(adj.ncnt);
         dfree(adj.items); dfree(adj.gsel); dfree(adj.v); dfree(adj.E);
+        std::lock_guard<std::recursive_mutex> lk(skid::device_mutex());
         if (d_scal) cudaFree(d_scal);
         if (d_fbytes) cudaFree(d_fbytes);
         if (d_fstats) cudaFree(d_fstats);

@@ -6,11 +6,20 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace skid {
 
 // Device buffer that remembers its size.
+// Device allocation, freeing and graph capture take this process-wide lock:
+// cudaMalloc/cudaFree may synchronise the device, which must not happen while
+// another host thread's stream is being captured into a graph (batched runs
+// drive several contexts from several threads).  Recursive: a capture may
+// reach a dalloc that finds its buffer already large enough.
+std::recursive_mutex &device_mutex();
+
 template <typename T>
 struct DBuf {
     T *p = nullptr;
@@ -21,6 +30,7 @@ template <typename T>
 cudaError_t dalloc(DBuf<T> &b, size_t n)
 {
     if (b.n >= n && b.p) return cudaSuccess;
+    std::lock_guard<std::recursive_mutex> lk(device_mutex());
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.n = 0;
@@ -32,6 +42,8 @@ cudaError_t dalloc(DBuf<T> &b, size_t n)
 template <typename T>
 void dfree(DBuf<T> &b)
 {
+    if (!b.p) return;
+    std::lock_guard<std::recursive_mutex> lk(device_mutex());
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.n = 0;

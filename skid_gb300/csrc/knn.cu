@@ -12,6 +12,8 @@
 // entering a node when any lane's heap bound reaches its box.
 #include <cfloat>
 
+#include <mutex>
+
 #include "internal.h"
 
 namespace skid {
@@ -153,8 +155,18 @@ cudaError_t knn_ball2(const Tree &t, int k, float3 L, bool per, float *ball2_sor
     while (nw > 1 && (size_t)nw * (candBytes + heapBytes) > (size_t)optin) nw >>= 1;
     bool global = (size_t)nw * (candBytes + heapBytes) > (size_t)optin;
     size_t smem = (size_t)nw * candBytes + (global ? 0 : (size_t)nw * heapBytes);
-    cudaError_t e = cudaFuncSetAttribute(knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    // The attribute is process-wide and only an upper bound: raise it to the
+    // opt-in maximum once (contexts on other threads launch with other k).
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [&] {
+        cudaFuncAttributes fa;
+        attr_err = cudaFuncGetAttributes(&fa, knn_kernel);
+        if (!attr_err)
+            attr_err = cudaFuncSetAttribute(knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            optin - (int)fa.sharedSizeBytes);
+    });
+    cudaError_t e = attr_err;
     if (e) return e;
     int perSM = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, knn_kernel, nw * 32, smem);

@@ -24,6 +24,12 @@ long long launches_total() { return g_launches.load(); }
 
 void set_capturing(bool on) { g_capturing = on; }
 
+std::recursive_mutex &device_mutex()
+{
+    static std::recursive_mutex m;
+    return m;
+}
+
 namespace {
 
 constexpr int RS_THREADS = 256;

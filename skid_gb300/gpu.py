@@ -47,6 +47,27 @@ class Timings(C.Structure):
                 ("field_bytes", C.c_double)]
 
 
+class Volume(C.Structure):
+    _fields_ = [("nGas", C.c_int), ("nDark", C.c_int), ("nStar", C.c_int), ("time", C.c_double),
+                ("pos", C.c_void_p), ("vel", C.c_void_p), ("mass", C.c_void_p),
+                ("soft", C.c_void_p), ("temp", C.c_void_p), ("period", C.c_float * 3),
+                ("center", C.c_float * 3), ("periodic", C.c_int), ("nSmooth", C.c_int),
+                ("fTau", C.c_float), ("fCvg", C.c_float), ("fScoop", C.c_float),
+                ("grp", C.c_void_p), ("groups", C.c_void_p), ("groups_cap", C.c_int),
+                ("nGroup", C.c_int), ("nGroupFoF", C.c_int), ("nUnbound", C.c_int),
+                ("nIter", C.c_int), ("device_ms", C.c_float), ("status", C.c_int),
+                ("message", C.c_char * 96)]
+
+
+class BatchFlags(C.Structure):
+    _fields_ = [("fDensMin", C.c_float), ("fTempMax", C.c_float), ("fMassMax", C.c_float),
+                ("nMembers", C.c_int), ("nMaxMembers", C.c_int), ("bGasAndDark", C.c_int),
+                ("bGasOnly", C.c_int), ("bForceInitialCut", C.c_int), ("bNoUnbind", C.c_int),
+                ("bNoCut", C.c_int), ("iSoftType", C.c_int), ("bEps", C.c_int),
+                ("fEps", C.c_float), ("G", C.c_float), ("z", C.c_float), ("a", C.c_float),
+                ("aH", C.c_float), ("maxIter", C.c_int)]
+
+
 GROUP_DTYPE = np.dtype([("nMembers", "<i4"), ("fMass", "<f4"), ("rel", "<f4", 3),
                         ("rCenter", "<f4", 3), ("rBound", "<f4", 3), ("vcm", "<f4", 3),
                         ("fRadius", "<f4")])
@@ -93,6 +114,7 @@ SIGNATURES = {
     "skid_density_adjoint": [_V, _F, _F, C.c_int],
     "skid_field_adjoint": [_V, C.c_int, _F, _F, _F],
     "skid_potential_adjoint": [_V, C.c_int, C.c_float, C.c_int, _I, _F, _D, _F],
+    "skid_batch_run": [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int],
 }
 
 ADJ_RECOMPUTE = 0
@@ -366,3 +388,57 @@ class Context:
         ng = C.c_int()
         self._call("skid_fof_points", self.h, len(pos), _f(pos), tau, _i(grp), C.byref(ng))
         return grp, ng.value
+
+
+def batch_run(volumes, opts, n_workers=8, device=0, group_cap=None):
+    """Run many independent volumes in one skid_batch_run call.
+
+    volumes: list of (snapshot, nSmooth, tau); opts: an Options holding the
+    shared flags (its tau/nSmooth are ignored).  Returns one dict per volume
+    with grp, groups (GROUP_DTYPE, index 0 = ungrouped), counts and status."""
+    lib = load()
+    nv = len(volumes)
+    arr = (Volume * nv)()
+    keep = []
+    outs = []
+    for i, (snap, k, tau) in enumerate(volumes):
+        v = arr[i]
+        pos = _c32(snap.pos, (-1, 3)); vel = _c32(snap.vel, (-1, 3))
+        mass = _c32(snap.mass); soft = _c32(snap.soft); temp = _c32(snap.temp)
+        grp = np.empty(snap.n, np.int32)
+        cap = (snap.n + 1) if group_cap is None else group_cap
+        groups = np.zeros(cap, GROUP_DTYPE)
+        keep.extend([pos, vel, mass, soft, temp])
+        v.nGas, v.nDark, v.nStar, v.time = snap.n_gas, snap.n_dark, snap.n_star, float(snap.time)
+        v.pos, v.vel, v.mass = pos.ctypes.data, vel.ctypes.data, mass.ctypes.data
+        v.soft, v.temp = soft.ctypes.data, temp.ctypes.data
+        for d in range(3):
+            v.period[d] = opts.period[d]
+            v.center[d] = opts.center[d]
+        v.periodic = int(opts.periodic)
+        v.nSmooth = int(k)
+        v.fTau = float(tau)
+        v.fCvg = v.fScoop = 0.0
+        v.grp, v.groups, v.groups_cap = grp.ctypes.data, groups.ctypes.data, cap
+        outs.append((grp, groups))
+    f = BatchFlags()
+    f.fDensMin, f.fTempMax, f.fMassMax = opts.fDensMin, opts.fTempMax, opts.fMassMax
+    f.nMembers, f.nMaxMembers = opts.nMembers, min(opts.nMaxMembers, 2**31 - 1)
+    f.bGasAndDark, f.bGasOnly = int(opts.bGasAndDark), int(opts.bGasOnly)
+    f.bForceInitialCut, f.bNoUnbind, f.bNoCut = (int(opts.bForceInitialCut), int(opts.bNoUnbind),
+                                                 int(opts.bNoScatterCut))
+    f.iSoftType, f.bEps, f.fEps = opts.iSoftType, int(opts.bEps), opts.fEps
+    f.G, f.z, f.a, f.aH = opts.G, opts.z, opts.a_shift, opts.a_hubble
+    f.maxIter = opts.maxIter
+    rc = lib.skid_batch_run(C.addressof(arr), nv, C.addressof(f), int(n_workers), int(device))
+    res = []
+    for i, (grp, groups) in enumerate(outs):
+        v = arr[i]
+        res.append({"grp": grp, "groups": groups[:v.nGroup + 1], "nGroup": v.nGroup,
+                    "nGroupFoF": v.nGroupFoF, "nUnbound": v.nUnbound, "nIter": v.nIter,
+                    "device_ms": v.device_ms, "status": v.status,
+                    "message": v.message.decode(errors="replace")})
+    if rc:
+        msgs = sorted({r["message"] for r in res if r["message"]})
+        raise SkidError(rc, "skid_batch_run" + (f" [{'; '.join(msgs)}]" if msgs else ""))
+    return res
