@@ -194,7 +194,10 @@ field_kernel(FieldArgs a)
                 bool rel = false;
                 if (lane < cnt) {
                     float4 c = cpos_s[w][lane];
-                    float r = sqrtf(c.w) * (1.0f + 2e-6f) +
+                    // ball radius from the approximate reciprocal square root,
+                    // widened to cover its error (an empty ball, fBall2 = 0,
+                    // gives NaN and is rejected, as the exact test would)
+                    float r = c.w * rsqrtf(c.w) * (1.0f + 4e-6f) +
                               1e-6f * (fabsf(c.x) + fabsf(c.y) + fabsf(c.z)) + 1e-30f;
                     rel = c.x + r >= wlo.x && c.x - r <= whi.x && c.y + r >= wlo.y &&
                           c.y - r <= whi.y && c.z + r >= wlo.z && c.z - r <= whi.z;
@@ -216,16 +219,19 @@ field_kernel(FieldArgs a)
                     int j = __ffs(m) - 1;
                     float4 c = cpos_s[w][j];
                     float2 k = ccoef_s[w][j];
-                    float dx = fsub(c.x, y.x), dy = fsub(c.y, y.y), dz = fsub(c.z, y.z);
-                    // smooth1.c:450-458
-                    float r2 = fmul(d2of(dx, dy, dz), k.x);
-                    float rs = sqrtf(r2);
-                    float F = r2 < 1.0f ? __fmaf_rn(2.25f, rs, -3.0f)
-                                        : (-3.0f / rs + 3.0f - 0.75f * rs);
-                    F = fmul(F, k.y);
-                    ax = fadd(ax, fmul(dx, F));
-                    ay = fadd(ay, fmul(dy, F));
-                    az = fadd(az, fmul(dz, F));
+                    // the field value (smooth1.c:450-458) only has to be
+                    // accurate, not bit-exact: FMA and the approximate
+                    // reciprocal square root (q = r2 / sqrt(r2), 1/q)
+                    float dx = c.x - y.x, dy = c.y - y.y, dz = c.z - y.z;
+                    float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) * k.x;
+                    float iq = rsqrtf(r2);
+                    float q = r2 > 0.0f ? r2 * iq : 0.0f;
+                    float F = r2 < 1.0f ? __fmaf_rn(2.25f, q, -3.0f)
+                                        : __fmaf_rn(-0.75f, q, 3.0f) - 3.0f * iq;
+                    F *= k.y;
+                    ax = __fmaf_rn(dx, F, ax);
+                    ay = __fmaf_rn(dy, F, ay);
+                    az = __fmaf_rn(dz, F, az);
                 }
                 unsigned any = __reduce_or_sync(SKID_FULL, mask);
                 if ((any >> lane) & 1u) a.touched[cb + lane] = 1;
