@@ -85,7 +85,9 @@ void set_capturing(bool on);
 // ---- sort.cu ----
 // Stable LSD radix sort of (key, value) pairs on the low `bits` bits.
 // Result lands in (k0, v0) of the scratch.
-cudaError_t radix_sort(SortScratch &s, int n, int bits, cudaStream_t st);
+// With d_n, only the first min(n, *d_n) keys are sorted (the count is read
+// on the device, so a captured graph follows it); the rest are left as they are.
+cudaError_t radix_sort(SortScratch &s, int n, int bits, cudaStream_t st, const int *d_n = nullptr);
 // Exclusive scan of int flags/counts; out may alias in; total -> *d_total.
 cudaError_t scan_exclusive(const int *in, int *out, int n, int *d_total, SortScratch &s,
                            cudaStream_t st);

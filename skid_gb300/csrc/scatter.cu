@@ -217,17 +217,9 @@ __global__ void prune_flag_kernel(const float4 *__restrict__ mpos, const float4 
     }
 }
 
-__global__ void init_keys_kernel(int cap, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
-        keys[i] = ~0ull;
-        vals[i] = 0u;
-    }
-}
-
 // Survivors get rOld reset (kd.c:785-789) and the Morton key of their
-// current position at their compacted slot; empty slots keep keys that sort
-// last.
+// current position at their compacted slot (slots [0, survivors) are all
+// written; only those are sorted).
 __global__ void prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ pos,
                                      const int *d_nA, const int *__restrict__ act,
                                      const float4 *__restrict__ mpos, float4 *__restrict__ mold,
@@ -241,7 +233,9 @@ __global__ void prune_scatter_kernel(const int *__restrict__ keep, const int *__
         float4 p = mpos[m];
         mold[m] = p;
         int j = pos[i];
-        keys[j] = morton63(make_float3(p.x, p.y, p.z), lo, inv);
+        // the top 32 bits of the Morton key (10 to 11 bits per axis) are
+        // enough to give each warp a compact set of movers
+        keys[j] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
         vals[j] = (uint32_t)m;
     }
 }
@@ -334,11 +328,11 @@ cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyin
     int g = grid_for(cap);
     prune_flag_kernel<<<g, 256, 0, st>>>(m.mpos.p, m.mold.p, m.act.p, m.d_nA, cap, hP, fCvg2, m.keep.p); skid::note_launch();
     if ((e = scan_exclusive(m.keep.p, m.kpos.p, cap, m.d_nA2, ss, st))) return e;
-    init_keys_kernel<<<g, 256, 0, st>>>(cap, ss.k0.p, ss.v0.p); skid::note_launch();
     prune_scatter_kernel<<<g, 256, 0, st>>>(m.keep.p, m.kpos.p, m.d_nA, m.act.p, m.mpos.p, m.mold.p, keylo, keyinv, ss.k0.p, ss.v0.p); skid::note_launch();
     // an even number of digit passes leaves the result in (k0, v0), so a
-    // captured graph replays consistently
-    if ((e = radix_sort(ss, cap, 64, st))) return e;
+    // captured graph replays consistently; only the surviving movers' keys
+    // (the first *d_nA2 slots) are sorted
+    if ((e = radix_sort(ss, cap, 32, st, m.d_nA2))) return e;
     act_from_sorted<<<g, 256, 0, st>>>(ss.v0.p, m.d_nA2, m.act.p); skid::note_launch();
     set_count_kernel<<<1, 1, 0, st>>>(m.d_nA, m.d_nA2); skid::note_launch();
     return cudaGetLastError();

@@ -37,10 +37,11 @@ constexpr int RS_ROUNDS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 constexpr int RS_WARPS = RS_THREADS / 32;
 
-__global__ void rs_histogram(const uint64_t *__restrict__ keys, int n, int shift, int nTiles,
-                             uint32_t *__restrict__ hist)
+__global__ void rs_histogram(const uint64_t *__restrict__ keys, int n, const int *d_n, int shift,
+                             int nTiles, uint32_t *__restrict__ hist)
 {
     __shared__ uint32_t h[256];
+    if (d_n) n = min(n, *d_n);   // live count known only on the device
     h[threadIdx.x] = 0;
     __syncthreads();
     int base = blockIdx.x * RS_TILE;
@@ -54,10 +55,12 @@ __global__ void rs_histogram(const uint64_t *__restrict__ keys, int n, int shift
 
 __global__ void rs_scatter(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                            uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n,
-                           int shift, int nTiles, const uint32_t *__restrict__ offs)
+                           const int *d_n, int shift, int nTiles, const uint32_t *__restrict__ offs)
 {
     __shared__ uint32_t run[256];
     __shared__ uint32_t wcnt[RS_WARPS][256];
+    if (d_n) n = min(n, *d_n);
+    if ((int)blockIdx.x * RS_TILE >= n) return;   // tile beyond the live keys
     int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     run[tid] = offs[tid * nTiles + blockIdx.x];
     for (int j = 0; j < RS_WARPS; ++j) wcnt[j][tid] = 0;
@@ -194,17 +197,17 @@ int num_sms()
     return sms;
 }
 
-cudaError_t radix_sort(SortScratch &s, int n, int bits, cudaStream_t st)
+cudaError_t radix_sort(SortScratch &s, int n, int bits, cudaStream_t st, const int *d_n)
 {
     if (n <= 0) return cudaSuccess;
     int nTiles = (n + RS_TILE - 1) / RS_TILE;
     cudaError_t e = dalloc(s.hist, (size_t)256 * nTiles);
     if (e) return e;
     for (int shift = 0; shift < bits; shift += 8) {
-        rs_histogram<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, n, shift, nTiles, s.hist.p); skid::note_launch();
+        rs_histogram<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, n, d_n, shift, nTiles, s.hist.p); skid::note_launch();
         e = scan_exclusive((const int *)s.hist.p, (int *)s.hist.p, 256 * nTiles, nullptr, s, st);
         if (e) return e;
-        rs_scatter<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, s.v0.p, s.k1.p, s.v1.p, n, shift, nTiles,
+        rs_scatter<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, s.v0.p, s.k1.p, s.v1.p, n, d_n, shift, nTiles,
                                                   s.hist.p); skid::note_launch();
         std::swap(s.k0, s.k1);
         std::swap(s.v0, s.v1);
