@@ -131,7 +131,7 @@ density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL,
 // G candidates of a visited leaf (one cheap pass that sets a hit mask), then
 // runs the field terms for its hits only; a mover's lanes are combined with
 // a fixed xor-butterfly, so sums are deterministic for a given G.
-template <int G>
+template <int G, bool STATS>
 __global__ void __launch_bounds__(G_WARPS * 32)
 field_kernel(FieldArgs a)
 {
@@ -175,7 +175,7 @@ field_kernel(FieldArgs a)
             float4 blo = a.blo[cp], bhi = a.bhi[cp];
             bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y && y.y <= bhi.y &&
                         y.z >= blo.z && y.z <= bhi.z;
-            ++st_nodes;
+            if (STATS) ++st_nodes;
             if (__any_sync(SKID_FULL, want)) {
                 if (cp < a.leafBase) { cp <<= 1; continue; }
                 int cb = (cp - a.leafBase) * SKID_LEAF;
@@ -187,7 +187,7 @@ field_kernel(FieldArgs a)
                     ccoef_s[w][lane] = make_float2(cc.x, cc.y);
                 }
                 __syncwarp();
-                ++st_leaves;
+                if (STATS) ++st_leaves;
                 // prefilter: lane j keeps candidate j if its ball (radius
                 // rounded up) reaches the movers' box; the exact test below
                 // decides, so this only skips candidates that cannot hit
@@ -212,9 +212,9 @@ field_kernel(FieldArgs a)
                         float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
                         if (d2 < c.w) mask |= 1u << j;
                     }
-                    st_tests += __popc(R);
+                    if (STATS) st_tests += __popc(R);
                 }
-                st_hits += __popc(mask);
+                if (STATS) st_hits += __popc(mask);
                 for (unsigned m = mask; m; m &= m - 1) {
                     int j = __ffs(m) - 1;
                     float4 c = cpos_s[w][j];
@@ -268,7 +268,7 @@ field_kernel(FieldArgs a)
             a.mpos[mi] = make_float4(y.x, y.y, y.z, yp.w);
         }
     }
-    if (a.stats) {
+    if (STATS && a.stats) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             st_tests += __shfl_xor_sync(SKID_FULL, st_tests, o);
@@ -303,18 +303,25 @@ cudaError_t density_gather(const Tree &t, const float *ball2_sorted, float3 L, b
     return cudaGetLastError();
 }
 
-template <int G>
-static cudaError_t launch_field(const FieldArgs &a, int max_movers, cudaStream_t st)
+template <int G, bool STATS>
+static cudaError_t launch_field_t(const FieldArgs &a, int max_movers, cudaStream_t st)
 {
     int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, field_kernel<G>, G_WARPS * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, field_kernel<G, STATS>, G_WARPS * 32, 0);
     if (perSM < 1) perSM = 1;
     int blocks = num_sms() * perSM;
     int need = ((max_movers + G - 1) / G + G_WARPS - 1) / G_WARPS;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
-    field_kernel<G><<<blocks, G_WARPS * 32, 0, st>>>(a); skid::note_launch();
+    field_kernel<G, STATS><<<blocks, G_WARPS * 32, 0, st>>>(a); skid::note_launch();
     return cudaGetLastError();
+}
+
+// Work counters compiled in only when asked for (they cost registers).
+template <int G>
+static cudaError_t launch_field(const FieldArgs &a, int max_movers, cudaStream_t st)
+{
+    return a.stats ? launch_field_t<G, true>(a, max_movers, st) : launch_field_t<G, false>(a, max_movers, st);
 }
 
 // The move alone (kdMoveParticles, kd.c:702-732) from a field written by
