@@ -388,7 +388,11 @@ def run_gpu(args):
                "stage_ms": {k: round(float(nres.timings[k]), 3) for k in
                             ("density_ms", "moving_ms", "unbind_ms")}}
     sched = {"unbind_warp_max": ctx.get_option("unbind_warp_max"),
-             "unbind_block": ctx.get_option("unbind_block")}
+             "unbind_block": ctx.get_option("unbind_block"),
+             "pot_ms": round(ctx.get_option("unbind_pot_ms"), 3),
+             "remove_ms": round(ctx.get_option("unbind_remove_ms"), 3),
+             "candidates_ms": [round(ctx.get_option(f"unbind_tune_ms{k}"), 3)
+                               for k in range(int(ctx.get_option("unbind_tune_candidates")))]}
 
     if rank != 0:
         ctx.close()

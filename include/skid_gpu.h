@@ -189,7 +189,8 @@ int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
  *   "field_g32_min"          active movers at or above which 32 per warp
  *   "field_g8_min"           active movers at or above which 8 per warp
  *   "unbind_warp_max"        groups up to this size get one warp each in the
- *                            removal loop: 0, 32, 64, 128, or -1 = autotuned
+ *                            removal loop: 0, 32, 64, 128, 256, 512, 1024,
+ *                            or -1 = autotuned
  *                            (default: every candidate is timed on the first
  *                            skid_unbind of the context, the fastest is kept)
  *   "unbind_block"           threads per block for larger groups: 128, 256,
@@ -206,8 +207,11 @@ int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
 int skid_set_option(skid_ctx *ctx, const char *name, double value);
 
 /* Current value of a knob; for "unbind_warp_max" and "unbind_block" the
- * schedule the last skid_unbind used, and "unbind_tune_candidates" the
- * number of schedules the autotuner timed. */
+ * schedule the last skid_unbind used, "unbind_tune_candidates" the number of
+ * schedules the autotuner timed, "unbind_tune_ms<k>" the removal time of
+ * candidate k (warp sizes outer, block sizes inner), "unbind_pot_ms" and
+ * "unbind_remove_ms" the potential and removal times of the last
+ * skid_unbind (CUDA events). */
 int skid_get_option(skid_ctx *ctx, const char *name, double *value);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that time or

@@ -865,7 +865,8 @@ int skid_set_option(skid_ctx *ctx, const char *name, double value)
         if (v < 0) return SKID_EINVAL;
         ctx->opt_g8_min = v;
     } else if (!strcmp(name, "unbind_warp_max")) {
-        if (v != -1 && v != 0 && v != 32 && v != 64 && v != 128) return SKID_EINVAL;
+        if (v != -1 && v != 0 && v != 32 && v != 64 && v != 128 && v != 256 && v != 512 && v != 1024)
+            return SKID_EINVAL;
         ctx->opt_unbind_tw = v;
     } else if (!strcmp(name, "unbind_block")) {
         if (v != -1 && v != 128 && v != 256 && v != 512 && v != 1024) return SKID_EINVAL;
@@ -894,6 +895,13 @@ int skid_get_option(skid_ctx *ctx, const char *name, double *value)
     else if (!strcmp(name, "unbind_block")) *value = ctx->U.used_bs;
     else if (!strcmp(name, "unbind_per_group")) *value = ctx->opt_unbind_per_group;
     else if (!strcmp(name, "unbind_tune_candidates")) *value = ctx->U.ntune;
+    else if (!strcmp(name, "unbind_pot_ms")) *value = ctx->U.pot_ms;
+    else if (!strcmp(name, "unbind_remove_ms")) *value = ctx->U.remove_ms;
+    else if (!strncmp(name, "unbind_tune_ms", 14)) {
+        int k = atoi(name + 14);
+        if (k < 0 || k >= 32 || k >= ctx->U.ntune) return SKID_EINVAL;
+        *value = ctx->U.tune_ms[k];
+    }
     else if (!strcmp(name, "field_unfused")) *value = ctx->opt_field_unfused;
     else return SKID_EINVAL;
     return 0;

@@ -89,8 +89,9 @@ struct UnbindScratch {
     DBuf<skid_group> rec_save;
     int tuned_tw = -1, tuned_bs = -1;   // autotuned removal schedule (kept per context)
     int used_tw = -1, used_bs = -1;     // schedule of the last run
-    float tune_ms[16] = {};
-    int ntune = 0;
+    float tune_ms[32] = {};
+    int ntune = 0, ntune_now = 0;
+    float pot_ms = 0.0f, remove_ms = 0.0f;   // last run (CUDA events)
 };
 
 // fof.cu

@@ -74,8 +74,63 @@ __device__ __forceinline__ float wrap_h(float d, float h)
     return d;
 }
 
-// Fixed-point quantum of a float term (scale = 2^S, exact multiply).
-__device__ __forceinline__ long long fx(float t, float scale) { return __float2ll_rn(t * scale); }
+// float -> int64 with round-half-to-even, bit-identical to __float2ll_rn for
+// finite |f| < 2^63, on the integer units: the mantissa shifted by the
+// exponent.  (GB300 runs the 64-bit conversion instructions on its FP64
+// path, which made them the bottleneck of the potential sums.)
+__device__ __forceinline__ long long f2ll_rn(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const int e = (int)((b >> 23) & 0xffu);
+    if (e == 0) return 0;                              // zero or denormal (< 0.5)
+    const unsigned long long m = (b & 0x7fffffu) | 0x800000u;
+    const int sh = e - 150;                            // |f| = m * 2^sh
+    unsigned long long q;
+    if (sh > 39) {
+        q = 0x7fffffffffffffffull;                     // |f| >= 2^63: saturate
+    } else if (sh >= 0) {
+        q = m << sh;
+    } else if (sh > -25) {
+        const int r = -sh;                             // 1..24
+        const unsigned long long rem = m & ((1ull << r) - 1ull);
+        const unsigned long long half = 1ull << (r - 1);
+        q = m >> r;
+        q += (rem > half) || (rem == half && (q & 1ull));
+    } else {
+        q = 0;                                         // |f| < 0.5
+    }
+    return (b >> 31) ? -(long long)q : (long long)q;
+}
+
+// int64 -> float within two roundings (relative error <= 2^-23), on the
+// FP32 and integer units: |p| in three 22-bit chunks, each exact as a float
+// (2^23 + x - 2^23), recombined by two fused multiply-adds.
+__device__ __forceinline__ float ll2f_approx(long long p)
+{
+    const unsigned long long a = p < 0 ? (unsigned long long)(-p) : (unsigned long long)p;
+    const float c0 = __uint_as_float(0x4B000000u | (unsigned)(a & 0x3fffffull)) - 8388608.0f;
+    const float c1 = __uint_as_float(0x4B000000u | (unsigned)((a >> 22) & 0x3fffffull)) - 8388608.0f;
+    const float c2 = __uint_as_float(0x4B000000u | (unsigned)((a >> 44) & 0x3fffffull)) - 8388608.0f;
+    const float f = __fmaf_rn(c2, 17592186044416.0f, __fmaf_rn(c1, 4194304.0f, c0));   // 2^44, 2^22
+    return p < 0 ? -f : f;
+}
+
+// Fixed-point quantum of a float term (scale = 2^S, exact multiply), equal to
+// __float2ll_rn(t * scale).  Terms are non-negative: below 2^23 adding 2^23
+// rounds to the nearest integer (ties to even) in the float adder, at or above
+// it the float is already an integer, its mantissa shifted by the exponent.
+__device__ __forceinline__ long long fx(float t, float scale)
+{
+    const float f = t * scale;
+    if (f < 8388608.0f) {
+        if (!(f >= 0.0f)) return f2ll_rn(f);          // negative or NaN: general form
+        return (long long)(__float_as_uint(f + 8388608.0f) - 0x4B000000u);
+    }
+    const unsigned b = __float_as_uint(f);
+    const int sh = (int)(b >> 23) - 150;              // 0 .. for f >= 2^23
+    if (sh > 39) return f2ll_rn(f);                   // beyond 2^63: saturates
+    return (long long)(((unsigned long long)((b & 0x7fffffu) | 0x800000u)) << sh);
+}
 
 __global__ void prep_members(const int *__restrict__ members, const int *__restrict__ gof, int n,
                              const float4 *__restrict__ pos4, const float4 *__restrict__ vel4,
@@ -257,8 +312,11 @@ pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_h
                 float4 rj = sr[jl];
                 float d2 = d2of(fsub(ri.x, rj.x), fsub(ri.y, rj.y), fsub(ri.z, rj.z));
                 float dir = spline_pot(d2, fadd(ei, ss[jl]), plummer);
-                acc += fx(fmul(fmul(G, rj.w), dir), scale);
-                atomicAdd(&acc_j[jl], (unsigned long long)fx(fmul(fmul(G, ri.w), dir), scale));
+                const long long tij = fx(fmul(fmul(G, rj.w), dir), scale);
+                // equal masses (all-dark runs): both ends get the same term
+                const long long tji = rj.w == ri.w ? tij : fx(fmul(fmul(G, ri.w), dir), scale);
+                acc += tij;
+                atomicAdd(&acc_j[jl], (unsigned long long)tji);
             }
         }
         if (I == J) {
@@ -353,7 +411,28 @@ __device__ __forceinline__ float member_energy(bool exact, const RemoveArgs &A, 
     float dv1 = A.fShift * (v.y - scm[4]) + A.fCosmo * (r.y - scm[1]);
     float dv2 = A.fShift * (v.z - scm[5]) + A.fCosmo * (r.z - scm[2]);
     float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
-    return 0.5f * dd - (__ll2float_rn(p) * A.inv_scale) * A.opz;
+    return 0.5f * dd - (ll2f_approx(p) * A.inv_scale) * A.opz;
+}
+
+// Bound on |FP32 energy - exact energy|: each of them is within a few
+// roundings of the real value of the same expression, so 2^-19 of the sum of
+// the magnitudes that enter it (velocity and position terms before their
+// cancellation, the kinetic term, the potential term) bounds the difference.
+__device__ __forceinline__ float energy_err(const RemoveArgs &A, float4 r, float4 v, long long p,
+                                            const float *scm, float e32)
+{
+    const float a = fabsf(A.fShift), c = fabsf(A.fCosmo);
+    float s = 0.0f, k = 0.0f;
+    const float vv[3] = {v.x, v.y, v.z}, rr[3] = {r.x, r.y, r.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float mag = a * (fabsf(vv[d]) + fabsf(scm[3 + d])) + c * (fabsf(rr[d]) + fabsf(scm[d]));
+        float dv = A.fShift * (vv[d] - scm[3 + d]) + A.fCosmo * (rr[d] - scm[d]);
+        s += mag * (2.0f * fabsf(dv) + mag);
+        k += dv * dv;
+    }
+    float pe = fabsf(ll2f_approx(p) * A.inv_scale * A.opz);
+    return 1.9073486e-06f * (s + k + pe + fabsf(e32)) + 1e-30f;   // 2^-19
 }
 
 // kdSubPot (grav.c:44-59) of the removed particle rs on member (r, v).
@@ -430,6 +509,8 @@ __device__ void warp_group(const RemoveArgs &A, int g)
     float es = 0.0f;
     for (;;) {
         ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
+        // FP32 energies (with error bounds for the exact form)
+        float emax = -FLT_MAX, emin = FLT_MAX, dmax = 0.0f;
         for (int i = lane; i < n; i += 32) {
             float4 r = qr[i], v = qv[i];
             long long p = pot[i];
@@ -437,9 +518,37 @@ __device__ void warp_group(const RemoveArgs &A, int g)
                 p = sub_pot(A, rs, es, r, v, p);
                 pot[i] = p;
             }
-            float E = member_energy(exact, A, r, v, p, dcm, scm, inv_d, opz_d);
-            if (E > mx.v) { mx.v = E; mx.i = i; }
-            if (E < mn.v) { mn.v = E; mn.i = i; }
+            float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
+            if (exact) {
+                emax = fmaxf(emax, E);
+                emin = fminf(emin, E);
+                dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
+            } else {
+                if (E > mx.v) { mx.v = E; mx.i = i; }
+                if (E < mn.v) { mn.v = E; mn.i = i; }
+            }
+        }
+        if (exact) {
+            // only members whose FP32 energy is within twice the error bound
+            // of the extremes can be the exact arg-max / arg-min: evaluate
+            // those exactly (FP64, as the reference does)
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                emax = fmaxf(emax, __shfl_xor_sync(SKID_FULL, emax, o));
+                emin = fminf(emin, __shfl_xor_sync(SKID_FULL, emin, o));
+                dmax = fmaxf(dmax, __shfl_xor_sync(SKID_FULL, dmax, o));
+            }
+            const float hi = emax - 2.0f * dmax, lo = emin + 2.0f * dmax;
+            for (int i = lane; i < n; i += 32) {
+                float4 r = qr[i], v = qv[i];
+                long long p = pot[i];
+                float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
+                if (E >= hi || E <= lo) {
+                    float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
+                    if (E >= hi && X > mx.v) { mx.v = X; mx.i = i; }
+                    if (E <= lo && X < mn.v) { mn.v = X; mn.i = i; }
+                }
+            }
         }
         mx = warp_argmax(mx);
         mn = warp_argmin(mn);
@@ -489,6 +598,7 @@ struct BlockShared {
     int s_n, s_go, s_have, s_imin;
     double d_cm[6], d_mass;
     double part[BS / 32][7];
+    float ext[BS / 32][3];      // per-warp FP32 energy max, min, error bound
 };
 
 // A large group, the whole block.
@@ -546,6 +656,7 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         float scm[6];
         for (int d = 0; d < 6; ++d) { dcm[d] = S.d_cm[d]; scm[d] = S.s_cm[d]; }
         ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
+        float emax = -FLT_MAX, emin = FLT_MAX, dmax = 0.0f;
         for (int i = tid; i < n; i += BS) {
             float4 r = qr[i], v = qv[i];
             long long p = pot[i];
@@ -553,9 +664,47 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 p = sub_pot(A, rs, es, r, v, p);
                 pot[i] = p;
             }
-            float E = member_energy(exact, A, r, v, p, dcm, scm, inv_d, opz_d);
-            if (E > mx.v) { mx.v = E; mx.i = i; }
-            if (E < mn.v) { mn.v = E; mn.i = i; }
+            float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
+            if (exact) {
+                emax = fmaxf(emax, E);
+                emin = fminf(emin, E);
+                dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
+            } else {
+                if (E > mx.v) { mx.v = E; mx.i = i; }
+                if (E < mn.v) { mn.v = E; mn.i = i; }
+            }
+        }
+        if (exact) {
+            // filtered exact evaluation, as in warp_group
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                emax = fmaxf(emax, __shfl_xor_sync(SKID_FULL, emax, o));
+                emin = fminf(emin, __shfl_xor_sync(SKID_FULL, emin, o));
+                dmax = fmaxf(dmax, __shfl_xor_sync(SKID_FULL, dmax, o));
+            }
+            if (lane == 0) {
+                S.ext[w][0] = emax;
+                S.ext[w][1] = emin;
+                S.ext[w][2] = dmax;
+            }
+            __syncthreads();
+            emax = -FLT_MAX; emin = FLT_MAX; dmax = 0.0f;
+            for (int k = 0; k < BS / 32; ++k) {
+                emax = fmaxf(emax, S.ext[k][0]);
+                emin = fminf(emin, S.ext[k][1]);
+                dmax = fmaxf(dmax, S.ext[k][2]);
+            }
+            const float hi = emax - 2.0f * dmax, lo = emin + 2.0f * dmax;
+            for (int i = tid; i < n; i += BS) {
+                float4 r = qr[i], v = qv[i];
+                long long p = pot[i];
+                float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
+                if (E >= hi || E <= lo) {
+                    float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
+                    if (E >= hi && X > mx.v) { mx.v = X; mx.i = i; }
+                    if (E <= lo && X < mn.v) { mn.v = X; mn.i = i; }
+                }
+            }
         }
         mx = warp_argmax(mx);
         mn = warp_argmin(mn);
@@ -675,7 +824,7 @@ int remove_blocks(int bs)
 }  // namespace
 
 // Candidate removal schedules (tw, BS) for the autotuner.
-static const int kTW[] = {0, 32, 64, 128};
+static const int kTW[] = {0, 32, 128, 256, 512, 1024};
 static const int kBS[] = {256, 512, 1024};
 
 cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *pos4,
@@ -804,7 +953,13 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
         return cudaGetLastError();
     }
 
+    cudaEvent_t t0 = nullptr, t1 = nullptr, t2 = nullptr;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    cudaEventCreate(&t2);
+    cudaEventRecord(t0, st);
     if ((e = potentials())) return e;
+    cudaEventRecord(t1, st);
     int tw = P.tw, bs = P.bs;
     if ((tw < 0 || bs < 0) && U.tuned_bs > 0) {
         if (tw < 0) tw = U.tuned_tw;
@@ -840,8 +995,9 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
                 if ((e = cudaEventSynchronize(e1))) break;
                 float ms = 0.0f;
                 cudaEventElapsedTime(&ms, e0, e1);
-                U.tune_ms[U.ntune < 16 ? U.ntune : 15] = ms;
+                U.tune_ms[U.ntune < 32 ? U.ntune : 31] = ms;
                 ++U.ntune;
+                U.ntune_now = 1;
                 if (ms < best) { best = ms; btw = a; bbs = b; }
             }
             if (e) break;
@@ -861,7 +1017,20 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     }
     U.used_tw = tw;
     U.used_bs = bs;
-    return removal(tw, bs);
+    if (U.ntune) cudaEventRecord(t1, st);   // tuning ran in between: time the final removal only
+    e = removal(tw, bs);
+    cudaEventRecord(t2, st);
+    if (!e) e = cudaEventSynchronize(t2);
+    float a = 0.0f, b = 0.0f;
+    if (!e && !U.ntune_now) cudaEventElapsedTime(&a, t0, t1);
+    if (!e) cudaEventElapsedTime(&b, t1, t2);
+    if (!U.ntune_now) U.pot_ms = a;
+    U.remove_ms = b;
+    U.ntune_now = 0;
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaEventDestroy(t2);
+    return e;
 }
 
 }  // namespace skid

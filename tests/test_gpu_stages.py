@@ -95,6 +95,7 @@ def test_schedules_and_unfused_forms_agree(gpu_ready, name):
                 {"unbind_warp_max": 128, "unbind_block": 1024},
                 {"unbind_warp_max": 32, "unbind_block": 512},
                 {"unbind_warp_max": 64, "unbind_block": 128},
+                {"unbind_warp_max": 1024, "unbind_block": 256},
                 {"unbind_per_group": 1}, {"field_unfused": 1}]
     outs = []
     for setting in settings:
@@ -105,8 +106,8 @@ def test_schedules_and_unfused_forms_agree(gpu_ready, name):
             outs.append((res.grp.copy(), res.groups.copy(), ctx.get_option("unbind_warp_max"),
                          ctx.get_option("unbind_block"), ctx.get_option("unbind_tune_candidates")))
     base_grp, base_rec = outs[0][0], outs[0][1]
-    assert outs[0][2] in (0, 32, 64, 128) and outs[0][3] in (256, 512, 1024)
-    assert outs[0][4] == 12
+    assert outs[0][2] in (0, 32, 128, 256, 512, 1024) and outs[0][3] in (256, 512, 1024)
+    assert outs[0][4] == 18
     for (grp, rec, *_), setting in zip(outs[1:], settings[1:]):
         assert np.array_equal(grp, base_grp), setting
         for f in ("nMembers", "fMass", "rCenter", "rBound", "vcm", "fRadius"):
