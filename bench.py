@@ -56,8 +56,13 @@ CPU_SAMPLE_N = 1 << 16
 FALLBACK_HBM = 6800.0
 
 
+CONFIG = 1   # 1: the 2^21 dark-matter workload; 4: the 2^24 mixed-species one
+
+
 def workload(n):
     from skid_gb300 import synth
+    if CONFIG == 4:
+        return synth.CONFIGS[4]
     if n == N_DEFAULT:
         spec = synth.CONFIGS[1]
     else:
@@ -68,7 +73,7 @@ def workload(n):
 
 def flags():
     from skid_gb300 import synth
-    return list(synth.WORKLOAD_FLAGS[1])
+    return list(synth.WORKLOAD_FLAGS[CONFIG])
 
 
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "field_kernel_skid_config1_2e21.md")
@@ -403,8 +408,12 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"skid config 1: N={n} periodic unit box, 800 NFW halos "
-                               f"(3 dex, c 4-20, r200max 0.02, 55%) + uniform background",
+        "config": {"workload": (f"skid config 1: N={n} periodic unit box, 800 NFW halos "
+                                f"(3 dex, c 4-20, r200max 0.02, 55%) + uniform background"
+                                if CONFIG == 1 else
+                                f"skid config 4: N={n} (50% gas of mass 0.2, 50% dark), 6000 NFW "
+                                f"halos (3.5 dex, c 4-20, 50%) + Zel'dovich-displaced k^-2 "
+                                f"Gaussian random field background, z = 0.5, -gd"),
                    "flags": " ".join(flags()), "n_particles": n, "l2": "flushed before each step",
                    "parallelism": f"replicas x{world}", "groups": res.n_group,
                    "groups_before_unbind": res.counts.get("nGroupFoF"),
@@ -433,6 +442,81 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+    return 0
+
+
+def synth_n(config):
+    from skid_gb300 import synth
+    return synth.CONFIGS[config].n
+
+
+def run_adjoint(args):
+    """Config 3: N = 2^20.  Times the density adjoint (dL/dx of sum w_i rho_i,
+    both neighbour modes) and the potential-energy adjoint of the 200 largest
+    groups, after the ordinary pipeline up to the group centres; with --check,
+    compares 1024 random particles with FP64 central differences (h = 1e-6)."""
+    import torch
+    from skid_gb300 import build, gpu, synth
+    from skid_gb300.options import Options
+    build.build_lib()
+    snap = synth.make_snapshot(synth.CONFIGS[3])
+    opts = Options.parse(synth.WORKLOAD_FLAGS[3])
+    rng = np.random.default_rng(synth.SEED_BASE + 30)
+    w = rng.standard_normal(snap.n).astype(np.float32)
+    ctx = gpu.Context(period=1.0, nSmooth=opts.nSmooth)
+    strm = torch.cuda.ExternalStream(ctx.stream_ptr())
+
+    def timed(fn, k):
+        ms = []
+        out = None
+        for _ in range(k):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(strm)
+            out = fn()
+            e1.record(strm)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return min(ms), out
+
+    ctx.set_particles(snap)
+    ctx.scatter_active(False, False)
+    ctx.density()
+    dens_ms, _ = timed(lambda: (ctx.restart(), ctx.scatter_active(False, False), ctx.density()), 3)
+    walk_ms, g_walk = timed(lambda: ctx.density_adjoint(w, gpu.ADJ_RECOMPUTE), max(2, args.steps))
+    list_ms, g_list = timed(lambda: ctx.density_adjoint(w, gpu.ADJ_STORED), max(2, args.steps))
+    ctx.init_move(opts.fDensMin, opts.fTempMax, opts.fMassMax, False, False)
+    ctx.move_step(opts.fStep, True, False)
+    na = 1
+    while na:
+        na, _ = ctx.move_iterate(opts.fStep, opts.fCvg, False)
+    ng = ctx.fof(opts.fTau)
+    ctx.group_centers()
+    grp, _ = ctx.get_groups(ng)
+    sizes = np.bincount(grp, minlength=ng + 1)[1:]
+    sel = (np.argsort(-sizes, kind="stable")[:200] + 1).astype(np.int32)
+    v = rng.standard_normal(len(sel)).astype(np.float32)
+    pot_ms, (E, gpot) = timed(lambda: ctx.potential_adjoint(sel, v, G=opts.G), max(2, args.steps))
+    ctx.close()
+    check = None
+    if args.check:
+        from oracle import oracle
+        pick = rng.choice(snap.n, 1024, replace=False)
+        an, fd, ab = oracle.density_adjoint_check(snap.pos, snap.mass, w, opts.nSmooth, 1.0, pick)
+        def rel(a, ref):
+            return float(np.max(np.linalg.norm(np.asarray(a, np.float64) - ref, axis=1) / ab))
+        check = {"particles": len(pick), "fd_step": 1e-6,
+                 "density_vs_fp64": rel(g_walk[pick], an), "density_vs_fd": rel(g_walk[pick], fd),
+                 "stored_vs_fp64": rel(g_list[pick], an), "fp64_analytic_vs_fd": rel(an, fd)}
+    pairs = float(np.sum(np.minimum(sizes[sel - 1], 10 ** 9).astype(np.float64) ** 2))
+    line = {"metric": "adjoint throughput, N=2^20", "unit": "particles/s",
+            "value": snap.n / (walk_ms / 1000.0), "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "config 3: N=2^20 periodic unit box, 400 NFW halos + background",
+                       "density_ms": dens_ms, "density_adjoint_recompute_ms": walk_ms,
+                       "density_adjoint_stored_ms": list_ms,
+                       "potential_adjoint_ms": pot_ms, "potential_groups": len(sel),
+                       "potential_pairs": pairs, "check": check}}
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -490,15 +574,26 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain-form and -nsp comparison runs")
-    ap.add_argument("--workload", default="single", choices=["single", "batch"],
-                    help="batch: the uneven-subvolume workload through skid_batch_run")
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "mixed", "adjoint"],
+                    help="batch: the uneven-subvolume workload through skid_batch_run; mixed: "
+                         "2^24 gas + dark with a Zel'dovich background (-gd, z = 0.5); adjoint: "
+                         "density and potential adjoints at 2^20")
     ap.add_argument("--n-vol", type=int, default=96)
+    ap.add_argument("--check", action="store_true", help="adjoint: FP64 finite-difference check")
     ap.add_argument("--workers", type=int, default=12)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
+    if args.workload == "mixed":
+        global CONFIG
+        CONFIG = 4
+        args.n = synth_n(4)
+        args.no_compare = True          # per-group unbinding of ~10^5 groups: minutes
+        args.no_cpu_baseline = True     # the CPU port would take hours at 2^24
     return run_gpu(args)
 
 

@@ -37,6 +37,7 @@ class HaloSpec:
     gas_frac: float = 0.0    # fraction of particles that are gas (mixed runs)
     gas_mass_ratio: float = 0.2
     gas_temp: float = 1.0e4
+    background: str = "uniform"   # or "grf": Zel'dovich-displaced Gaussian random field
 
 
 # The workloads.  Skid flags that go with each are in WORKLOAD_FLAGS.
@@ -44,7 +45,8 @@ CONFIGS = {
     0: HaloSpec(32768, 20, 1.5, (5.0, 15.0), 0.05, 0.60, SEED_BASE + 0),
     1: HaloSpec(1 << 21, 800, 3.0, (4.0, 20.0), 0.02, 0.55, SEED_BASE + 1),
     3: HaloSpec(1 << 20, 400, 3.0, (4.0, 20.0), 0.02, 0.55, SEED_BASE + 3),
-    4: HaloSpec(1 << 24, 6000, 3.5, (4.0, 20.0), 0.02, 0.50, SEED_BASE + 4, gas_frac=0.5),
+    4: HaloSpec(1 << 24, 6000, 3.5, (4.0, 20.0), 0.02, 0.50, SEED_BASE + 4, gas_frac=0.5,
+                background="grf"),
 }
 
 
@@ -65,6 +67,29 @@ def _nfw_x(u: np.ndarray, c: np.ndarray) -> np.ndarray:
         lo = np.where(below, mid, lo)
         hi = np.where(below, hi, mid)
     return 0.5 * (lo + hi)
+
+
+def grf_displacement(rng, ngrid: int, slope: float = -2.0, rms_cells: float = 0.5):
+    """Zel'dovich displacement field of a Gaussian random field with power
+    spectrum P(k) ~ k^slope on an ngrid^3 periodic grid: psi(k) = i k / k^2
+    delta(k), scaled so the rms displacement is rms_cells grid cells.
+    Returns an (ngrid, ngrid, ngrid, 3) float32 array in box units."""
+    k1 = np.fft.fftfreq(ngrid) * ngrid
+    kr = np.fft.rfftfreq(ngrid) * ngrid
+    kx, ky, kz = np.meshgrid(k1, k1, kr, indexing="ij")
+    k2 = kx * kx + ky * ky + kz * kz
+    k2[0, 0, 0] = 1.0
+    amp = np.sqrt(k2 ** (0.5 * slope))
+    amp[0, 0, 0] = 0.0
+    noise = rng.normal(size=(ngrid, ngrid, ngrid))
+    delta = np.fft.rfftn(noise) * amp
+    psi = np.empty((ngrid, ngrid, ngrid, 3), np.float32)
+    for d, kd in enumerate((kx, ky, kz)):
+        psi[..., d] = np.fft.irfftn(1j * kd / k2 * delta, s=(ngrid, ngrid, ngrid)).astype(np.float32)
+    rms = float(np.sqrt(np.mean(np.sum(psi.astype(np.float64) ** 2, axis=-1))))
+    if rms > 0:
+        psi *= np.float32(rms_cells / ngrid / rms)
+    return psi
 
 
 def _wrap32(x: np.ndarray) -> np.ndarray:
@@ -107,6 +132,15 @@ def make_halos(spec: HaloSpec):
     nb = n - n_halo_p
     bpos = rng.uniform(-0.5, 0.5, (nb, 3))
     bvel = rng.normal(0.0, 0.05, (nb, 3))
+    if spec.background == "grf" and nb > 0:
+        # uniform points displaced by the field at their nearest grid cell;
+        # velocities follow the displacement (linear growth, unit factor)
+        ngrid = int(min(256, max(16, 2 ** round(math.log2(nb ** (1.0 / 3.0))))))
+        psi = grf_displacement(rng, ngrid)
+        cell = np.floor((bpos + 0.5) * ngrid).astype(np.int64) % ngrid
+        disp = psi[cell[:, 0], cell[:, 1], cell[:, 2]].astype(np.float64)
+        bpos = bpos + disp
+        bvel = bvel + disp
     pos = np.concatenate([hpos, bpos])
     vel = np.concatenate([hvel, bvel])
     perm = rng.permutation(n)
@@ -155,4 +189,6 @@ WORKLOAD_FLAGS = {
         "-H", f"{hubble_for(0.3):.6g}"],
     3: ["-tau", "0.005", "-s", "64", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
         "-H", f"{hubble_for(0.3):.6g}"],
+    4: ["-tau", "0.002", "-s", "64", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
+        "-z", "0.5", "-gd", "-H", f"{hubble_for(0.3):.6g}"],
 }
