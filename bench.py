@@ -503,11 +503,15 @@ def run_adjoint(args):
         from oracle import oracle
         pick = rng.choice(snap.n, 1024, replace=False)
         an, fd, ab = oracle.density_adjoint_check(snap.pos, snap.mass, w, opts.nSmooth, 1.0, pick)
+        _, fdr, _ = oracle.density_adjoint_check(snap.pos, snap.mass, w, opts.nSmooth, 1.0, pick,
+                                                 richardson=True)
         def rel(a, ref):
             return float(np.max(np.linalg.norm(np.asarray(a, np.float64) - ref, axis=1) / ab))
         check = {"particles": len(pick), "fd_step": 1e-6,
                  "density_vs_fp64": rel(g_walk[pick], an), "density_vs_fd": rel(g_walk[pick], fd),
-                 "stored_vs_fp64": rel(g_list[pick], an), "fp64_analytic_vs_fd": rel(an, fd)}
+                 "density_vs_fd_richardson": rel(g_walk[pick], fdr),
+                 "stored_vs_fp64": rel(g_list[pick], an), "fp64_analytic_vs_fd": rel(an, fd),
+                 "fp64_analytic_vs_fd_richardson": rel(an, fdr)}
     pairs = float(np.sum(np.minimum(sizes[sel - 1], 10 ** 9).astype(np.float64) ** 2))
     line = {"metric": "adjoint throughput, N=2^20", "unit": "particles/s",
             "value": snap.n / (walk_ms / 1000.0), "n_gpus": 1, "data": "synthetic",

@@ -132,6 +132,14 @@ int or_density_adjoint_check(int n, const float *pos, const float *mass,
                              int nsel, const int *sel, double hfd,
                              double *grad_an, double *grad_fd, double *absterm,
                              int *lists_ok);
+/* The same, also with central differences of step hfd/2 (grad_fd_half,
+ * may be NULL) for Richardson extrapolation. */
+int or_density_adjoint_check2(int n, const float *pos, const float *mass,
+                              const float *w, int k, const float period[3],
+                              int nsel, const int *sel, double hfd,
+                              double *grad_an, double *grad_fd,
+                              double *grad_fd_half, double *absterm,
+                              int *lists_ok);
 /* Density field of ns scatterers at nq points: gradient, central
  * differences, sum of |term|. */
 int or_field_grad_check(int ns, const float *spos, const float *smass,
