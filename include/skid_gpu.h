@@ -185,9 +185,11 @@ int skid_get_timings(skid_ctx *ctx, skid_timings *t);
 int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
 
 /* Tuning knobs (no reference counterpart).  Names:
- *   "field_movers_per_warp"  0 = by active count (default), or 32, 8, 1
+ *   "field_movers_per_warp"  0 = by active count (default), or 32, 16, 8, 4, 1
  *   "field_g32_min"          active movers at or above which 32 per warp
- *   "field_g8_min"           active movers at or above which 8 per warp
+ *   "field_g16_min"          ... 16 per warp
+ *   "field_g8_min"           ... 8 per warp
+ *   "field_g4_min"           ... 4 per warp (one per warp below)
  *   "unbind_warp_max"        groups up to this size get one warp each in the
  *                            removal loop: 0, 32, 64, 128, 256, 512, 1024,
  *                            or -1 = autotuned

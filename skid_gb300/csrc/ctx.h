@@ -184,11 +184,12 @@ struct skid_ctx {
     skid::AdjointState adj;         // density / potential adjoints
 
     // outer-iteration CUDA graphs, one per movers-per-warp setting
-    cudaGraphExec_t iter_graph[3] = {nullptr, nullptr, nullptr};
-    long long iter_graph_kernels[3] = {0, 0, 0};
-    float g_fStep[3] = {0, 0, 0}, g_fCvg[3] = {0, 0, 0};
-    bool g_nocut[3] = {false, false, false};
-    bool g_stats[3] = {false, false, false};
+    static constexpr int NSLOT = 5;          // movers per warp 32, 16, 8, 4, 1
+    cudaGraphExec_t iter_graph[NSLOT] = {};
+    long long iter_graph_kernels[NSLOT] = {};
+    float g_fStep[NSLOT] = {}, g_fCvg[NSLOT] = {};
+    bool g_nocut[NSLOT] = {};
+    bool g_stats[NSLOT] = {};
     float3 mkey_lo{}, mkey_inv{};   // Morton frame of mover positions
     // move-field kernel timing: an event pair per step slot of an iteration
     cudaEvent_t fev[2 * skid::PRUNE_STEPS] = {};
@@ -231,9 +232,9 @@ struct skid_ctx {
     }
     int enqueue_step(float fStep, bool initial, bool nocut, int slot, int G);
     // Crossovers measured on GB300 with the 2^21-particle workload: per-step
-    // move-field time is lowest with 32 movers per warp above ~450k active
-    // movers, 8 per warp down to ~24k, and one per warp below.
-    int opt_G = 0, opt_g32_min = 450000, opt_g8_min = 24000;
+    // move-field time is lowest with 32 movers per warp above ~600k active
+    // movers, 16 down to ~400k, 8 down to ~50k, 4 down to ~25k, one below.
+    int opt_G = 0, opt_g32_min = 600000, opt_g16_min = 400000, opt_g8_min = 50000, opt_g4_min = 25000;
     int opt_unbind_tw = -1, opt_unbind_bs = -1;   // -1: autotuned on the first skid_unbind
     bool opt_unbind_per_group = false;
     bool opt_field_unfused = false;                // field pass and move pass as separate kernels
@@ -241,7 +242,11 @@ struct skid_ctx {
     int movers_per_warp() const
     {
         if (opt_G) return opt_G;
-        return nActive >= opt_g32_min ? 32 : (nActive >= opt_g8_min ? 8 : 1);
+        return nActive >= opt_g32_min   ? 32
+               : nActive >= opt_g16_min ? 16
+               : nActive >= opt_g8_min  ? 8
+               : nActive >= opt_g4_min  ? 4
+                                        : 1;
     }
     void drop_graphs()
     {

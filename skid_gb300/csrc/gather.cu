@@ -168,7 +168,10 @@ field_kernel(FieldArgs a)
         }
         // candidates a lane may test: every L-th one starting at its sub-index
         const unsigned mine = G == 32 ? SKID_FULL
-                              : (G == 8 ? (0x11111111u << sub) : (1u << sub));
+                              : G == 16 ? (0x55555555u << sub)
+                              : G == 8  ? (0x11111111u << sub)
+                              : G == 4  ? (0x01010101u << sub)
+                                        : (1u << sub);
         float ax = 0.0f, ay = 0.0f, az = 0.0f;
         int cp = 1;
         for (;;) {
@@ -370,7 +373,9 @@ cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st)
     if (e) return e;
     switch (a.G) {
     case 1: return launch_field<1>(a, max_movers, st);
+    case 4: return launch_field<4>(a, max_movers, st);
     case 8: return launch_field<8>(a, max_movers, st);
+    case 16: return launch_field<16>(a, max_movers, st);
     default: return launch_field<32>(a, max_movers, st);
     }
 }
