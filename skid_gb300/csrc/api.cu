@@ -259,6 +259,8 @@ FieldArgs skid_ctx::field_args(float fStep, bool initial, float *acc_out)
     a.blo = ctree.blo.p;
     a.bhi = ctree.bhi.p;
     a.leafBase = ctree.leafBase;
+    a.subShift = 0;
+    while (a.subShift < 5 && (2 << a.subShift) <= a.leafBase) ++a.subShift;
     a.d_nC = C.d_n;
     a.mpos = M.mpos.p;
     a.act = M.act.p;
@@ -342,7 +344,7 @@ static int field_probe(skid_ctx *ctx, int nm, const float *mpos)
     a.mpos = p4.p;
     a.act = act.p;
     a.d_nA = act.p + nm;
-    a.G = 32;
+    a.G = ctx->opt_G ? ctx->opt_G : 32;   // a forced movers-per-warp applies here too
     a.stats = nullptr;
     a.touched = ctx->probe_touched();
     if (!a.touched) return ctx->fail(SKID_ENOMEM);

@@ -27,6 +27,16 @@ namespace {
 
 constexpr int G_WARPS = 4;
 
+// Field kernel build tunables: unroll of the candidate test loop, and the
+// minimum resident blocks per SM passed to __launch_bounds__ (caps registers).
+#ifndef SKID_FIELD_UNROLL
+#define SKID_FIELD_UNROLL 4
+#endif
+#ifndef SKID_FIELD_MINB
+#define SKID_FIELD_MINB 12
+#endif
+constexpr int FIELD_UNROLL = SKID_FIELD_UNROLL;
+
 __device__ __forceinline__ float w_m4(float r2)
 {
     float q = sqrtf(r2);
@@ -132,7 +142,7 @@ density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL,
 // runs the field terms for its hits only; a mover's lanes are combined with
 // a fixed xor-butterfly, so sums are deterministic for a given G.
 template <int G, bool STATS>
-__global__ void __launch_bounds__(G_WARPS * 32)
+__global__ void __launch_bounds__(G_WARPS * 32, SKID_FIELD_MINB)
 field_kernel(FieldArgs a)
 {
     constexpr int L = 32 / G;   // lanes per mover
@@ -166,78 +176,98 @@ field_kernel(FieldArgs a)
             whi.y = fmaxf(whi.y, __shfl_xor_sync(SKID_FULL, whi.y, o));
             whi.z = fmaxf(whi.z, __shfl_xor_sync(SKID_FULL, whi.z, o));
         }
-        // candidates a lane may test: every L-th one starting at its sub-index
-        const unsigned mine = G == 32 ? SKID_FULL
-                              : G == 16 ? (0x55555555u << sub)
-                              : G == 8  ? (0x11111111u << sub)
-                              : G == 4  ? (0x01010101u << sub)
-                                        : (1u << sub);
         float ax = 0.0f, ay = 0.0f, az = 0.0f;
+        // Depth-first walk by ball boxes.  Nodes whose subtree holds the last
+        // 2^subShift leaves (5 levels) are not descended one by one: each lane
+        // tests one of their leaves against the movers' box, and the leaves
+        // that pass are visited in order (the depth-first leaf order).
+        const int rootLo = a.leafBase >> a.subShift;
         int cp = 1;
         for (;;) {
-            float4 blo = a.blo[cp], bhi = a.bhi[cp];
-            bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y && y.y <= bhi.y &&
-                        y.z >= blo.z && y.z <= bhi.z;
-            if (STATS) ++st_nodes;
-            if (__any_sync(SKID_FULL, want)) {
-                if (cp < a.leafBase) { cp <<= 1; continue; }
-                int cb = (cp - a.leafBase) * SKID_LEAF;
-                int cnt = min(SKID_LEAF, nC - cb);
-                __syncwarp();
-                if (lane < cnt) {
-                    cpos_s[w][lane] = a.cpos[cb + lane];
-                    float4 cc = a.ccoef[cb + lane];
-                    ccoef_s[w][lane] = make_float2(cc.x, cc.y);
+            if (cp >= rootLo) {
+                const int first = cp << a.subShift;
+                bool pass = false;
+                if (lane < (1 << a.subShift)) {
+                    float4 bl = a.blo[first + lane], bh = a.bhi[first + lane];
+                    pass = bl.x <= whi.x && bh.x >= wlo.x && bl.y <= whi.y && bh.y >= wlo.y &&
+                           bl.z <= whi.z && bh.z >= wlo.z;
                 }
-                __syncwarp();
-                if (STATS) ++st_leaves;
-                // prefilter: lane j keeps candidate j if its ball (radius
-                // rounded up) reaches the movers' box; the exact test below
-                // decides, so this only skips candidates that cannot hit
-                bool rel = false;
-                if (lane < cnt) {
-                    float4 c = cpos_s[w][lane];
-                    // ball radius from the approximate reciprocal square root,
-                    // widened to cover its error (an empty ball, fBall2 = 0,
-                    // gives NaN and is rejected, as the exact test would)
-                    float r = c.w * rsqrtf(c.w) * (1.0f + 4e-6f) +
-                              1e-6f * (fabsf(c.x) + fabsf(c.y) + fabsf(c.z)) + 1e-30f;
-                    rel = c.x + r >= wlo.x && c.x - r <= whi.x && c.y + r >= wlo.y &&
-                          c.y - r <= whi.y && c.z + r >= wlo.z && c.z - r <= whi.z;
-                }
-                const unsigned R = __ballot_sync(SKID_FULL, rel) & mine;
-                unsigned mask = 0;
-                if (want) {
-                    for (unsigned m = R; m; m &= m - 1) {
+                if (STATS) ++st_nodes;
+                for (unsigned lm = __ballot_sync(SKID_FULL, pass); lm; lm &= lm - 1) {
+                    const int node = first + __ffs(lm) - 1;
+                    float4 blo = a.blo[node], bhi = a.bhi[node];
+                    bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y &&
+                                y.y <= bhi.y && y.z >= blo.z && y.z <= bhi.z;
+                    if (!__any_sync(SKID_FULL, want)) continue;
+                    int cb = (node - a.leafBase) * SKID_LEAF;
+                    int cnt = min(SKID_LEAF, nC - cb);
+                    if (STATS) ++st_leaves;
+                    // prefilter: lane j keeps candidate j if its ball (radius
+                    // rounded up) reaches the movers' box; the exact test below
+                    // decides, so this only skips candidates that cannot hit
+                    bool rel = false;
+                    float4 c4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (lane < cnt) {
+                        c4 = a.cpos[cb + lane];
+                        // ball radius from the approximate reciprocal square root,
+                        // widened to cover its error (an empty ball, fBall2 = 0,
+                        // gives NaN and is rejected, as the exact test would)
+                        float r = c4.w * rsqrtf(c4.w) * (1.0f + 4e-6f) +
+                                  1e-6f * (fabsf(c4.x) + fabsf(c4.y) + fabsf(c4.z)) + 1e-30f;
+                        rel = c4.x + r >= wlo.x && c4.x - r <= whi.x && c4.y + r >= wlo.y &&
+                              c4.y - r <= whi.y && c4.z + r >= wlo.z && c4.z - r <= whi.z;
+                    }
+                    // the survivors, compacted in candidate order
+                    const unsigned R = __ballot_sync(SKID_FULL, rel);
+                    const int nR = __popc(R);
+                    const int slotR = __popc(R & ((1u << lane) - 1u));
+                    __syncwarp();
+                    if (rel) {
+                        cpos_s[w][slotR] = c4;
+                        float4 cc = a.ccoef[cb + lane];
+                        ccoef_s[w][slotR] = make_float2(cc.x, cc.y);
+                    }
+                    __syncwarp();
+                    // a mover's L lanes take every L-th survivor
+                    unsigned mask = 0;
+                    if (want) {
+#pragma unroll FIELD_UNROLL
+                        for (int t = sub; t < nR; t += L) {
+                            float4 c = cpos_s[w][t];
+                            // smBallGather's test (smooth1.c:365-369), from the copy
+                            float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
+                            mask |= (unsigned)(d2 < c.w) << t;
+                        }
+                        if (STATS) st_tests += (nR - sub + L - 1) / L;
+                    }
+                    if (STATS) st_hits += __popc(mask);
+                    for (unsigned m = mask; m; m &= m - 1) {
                         int j = __ffs(m) - 1;
                         float4 c = cpos_s[w][j];
-                        // smBallGather's test (smooth1.c:365-369), from the copy
-                        float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
-                        if (d2 < c.w) mask |= 1u << j;
+                        float2 k = ccoef_s[w][j];
+                        // the field value (smooth1.c:450-458) only has to be
+                        // accurate, not bit-exact: FMA and the approximate
+                        // reciprocal square root (q = r2 / sqrt(r2), 1/q)
+                        float dx = c.x - y.x, dy = c.y - y.y, dz = c.z - y.z;
+                        float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) * k.x;
+                        float iq = rsqrtf(r2);
+                        float q = r2 > 0.0f ? r2 * iq : 0.0f;
+                        float F = r2 < 1.0f ? __fmaf_rn(2.25f, q, -3.0f)
+                                            : __fmaf_rn(-0.75f, q, 3.0f) - 3.0f * iq;
+                        F *= k.y;
+                        ax = __fmaf_rn(dx, F, ax);
+                        ay = __fmaf_rn(dy, F, ay);
+                        az = __fmaf_rn(dz, F, az);
                     }
-                    if (STATS) st_tests += __popc(R);
+                    unsigned any = __reduce_or_sync(SKID_FULL, mask);
+                    if (rel && ((any >> slotR) & 1u)) a.touched[cb + lane] = 1;
                 }
-                if (STATS) st_hits += __popc(mask);
-                for (unsigned m = mask; m; m &= m - 1) {
-                    int j = __ffs(m) - 1;
-                    float4 c = cpos_s[w][j];
-                    float2 k = ccoef_s[w][j];
-                    // the field value (smooth1.c:450-458) only has to be
-                    // accurate, not bit-exact: FMA and the approximate
-                    // reciprocal square root (q = r2 / sqrt(r2), 1/q)
-                    float dx = c.x - y.x, dy = c.y - y.y, dz = c.z - y.z;
-                    float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) * k.x;
-                    float iq = rsqrtf(r2);
-                    float q = r2 > 0.0f ? r2 * iq : 0.0f;
-                    float F = r2 < 1.0f ? __fmaf_rn(2.25f, q, -3.0f)
-                                        : __fmaf_rn(-0.75f, q, 3.0f) - 3.0f * iq;
-                    F *= k.y;
-                    ax = __fmaf_rn(dx, F, ax);
-                    ay = __fmaf_rn(dy, F, ay);
-                    az = __fmaf_rn(dz, F, az);
-                }
-                unsigned any = __reduce_or_sync(SKID_FULL, mask);
-                if ((any >> lane) & 1u) a.touched[cb + lane] = 1;
+            } else {
+                float4 blo = a.blo[cp], bhi = a.bhi[cp];
+                bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y && y.y <= bhi.y &&
+                            y.z >= blo.z && y.z <= bhi.z;
+                if (STATS) ++st_nodes;
+                if (__any_sync(SKID_FULL, want)) { cp <<= 1; continue; }
             }
             cp = next_node(cp);
             if (cp == 1) break;

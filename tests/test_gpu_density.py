@@ -52,12 +52,15 @@ def test_knn_probe_brute(gpu_ready):
             assert np.array_equal(b, oracle.knn_ball2(pos, k, 1.0, brute=True))
 
 
-@pytest.mark.parametrize("period", [1.0, None])
-def test_move_field(gpu_ready, period):
-    """The move field (minus grad rho, smooth1.c:447-459) at every particle."""
+@pytest.mark.parametrize("period,G", [(1.0, 32), (None, 32), (1.0, 16), (1.0, 8), (None, 4),
+                                      (1.0, 1)])
+def test_move_field(gpu_ready, period, G):
+    """The move field (minus grad rho, smooth1.c:447-459) at every particle,
+    for each number of movers per warp the move step uses."""
     from skid_gb300 import gpu
     snap = small_snapshot(n=8192, seed=21)
     with gpu.Context(period=period, nSmooth=64) as ctx:
+        ctx.set_option("field_movers_per_warp", G)
         ctx.set_particles(snap)
         ctx.scatter_active()
         ctx.density()
