@@ -57,13 +57,46 @@ __device__ __forceinline__ float shifted(float x, int s, float L)
     return s == 0 ? x : (s < 0 ? fsub(x, L) : fadd(x, L));
 }
 
+// Lower bound of the float squared distance between any point of box a
+// (any periodic image) and any point of box b: the box_lb bound taken over
+// every point of a, with the slack of a's largest coordinate.
+__device__ __forceinline__ float boxbox_lb1(float alo, float ahi, float blo, float bhi, float L,
+                                            bool per)
+{
+    float d = fmaxf(fmaxf(blo - ahi, alo - bhi), 0.0f);
+    if (per) {
+        d = fminf(d, fmaxf(fmaxf(blo - (ahi + L), (alo + L) - bhi), 0.0f));
+        d = fminf(d, fmaxf(fmaxf(blo - (ahi - L), (alo - L) - bhi), 0.0f));
+    }
+    float slack = 4.8e-7f * (fmaxf(fabsf(alo), fabsf(ahi)) + (per ? L : 0.0f) +
+                             fmaxf(fabsf(blo), fabsf(bhi)));
+    return fmaxf(d - slack, 0.0f);
+}
+
+__device__ __forceinline__ float boxbox_lb(float4 alo, float4 ahi, float4 blo, float4 bhi, float3 L,
+                                           bool per)
+{
+    float dx = boxbox_lb1(alo.x, ahi.x, blo.x, bhi.x, L.x, per);
+    float dy = boxbox_lb1(alo.y, ahi.y, blo.y, bhi.y, L.y, per);
+    float dz = boxbox_lb1(alo.z, ahi.z, blo.z, bhi.z, L.z, per);
+    return (dx * dx + dy * dy + dz * dz) * (1.0f - 4e-6f);
+}
+
+// One warp per leaf of queries.  The walk descends a node while some lane's
+// ball reaches its box or some ball below may hold the lane (box distance
+// below max(b_i, max ball2 below)); the last 2^subShift leaves of a subtree
+// are tested one per lane against the query leaf's box.  At a visited leaf,
+// lane j keeps candidate j if its distance to the query box is below
+// max(its ball, the largest query ball) -- the only candidates that can
+// enter either half -- and the survivors, compacted in order, are summed.
 __global__ void __launch_bounds__(G_WARPS * 32)
 density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL, bool per,
-               float *__restrict__ rho, int *work)
+               int subShift, float *__restrict__ rho, int *work)
 {
     __shared__ float4 cpos[G_WARPS][SKID_LEAF];
     __shared__ float4 caux[G_WARPS][SKID_LEAF];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int rootLo = t.leafBase >> subShift;
     for (;;) {
         int leaf = 0;
         if (lane == 0) leaf = atomicAdd(work, 1);
@@ -77,38 +110,58 @@ density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL,
         float bi = ball2[valid ? qi : base];
         float ih2i = 4.0f / bi;
         float fni = 0.5f * (float)M_1_PI * sqrtf(ih2i) * ih2i;
+        // the query leaf's box (its points) and largest ball
+        const float4 qlo = t.lo[t.leafBase + leaf], qhi = t.hi[t.leafBase + leaf];
         float s = 0.0f, c = 0.0f;
         int cp = 1;
         for (;;) {
-            float4 blo = t.lo[cp], bhi = t.hi[cp];
-            float bd = box_lb(q, blo, bhi, L, per);
-            bool want = bd < fmaxf(bi, blo.w);
-            if (__any_sync(SKID_FULL, want)) {
-                if (cp < t.leafBase) { cp <<= 1; continue; }
-                int lf = cp - t.leafBase;
-                if (lf < t.nLeaf) {
+            if (cp >= rootLo) {
+                const int first = cp << subShift;
+                bool pass = false;
+                if (lane < (1 << subShift)) {
+                    float4 bl = t.lo[first + lane], bh = t.hi[first + lane];
+                    pass = boxbox_lb(qlo, qhi, bl, bh, L, per) < fmaxf(qlo.w, bl.w);
+                }
+                for (unsigned lm = __ballot_sync(SKID_FULL, pass); lm; lm &= lm - 1) {
+                    const int node = first + __ffs(lm) - 1;
+                    const int lf = node - t.leafBase;
+                    if (lf >= t.nLeaf) break;
+                    float4 blo = t.lo[node], bhi = t.hi[node];
+                    bool want = box_lb(q, blo, bhi, L, per) < fmaxf(bi, blo.w);
+                    if (!__any_sync(SKID_FULL, want)) continue;
                     int cb = lf * SKID_LEAF;
                     int cnt = min(SKID_LEAF, t.n - cb);
-                    __syncwarp();
+                    bool rel = false;
+                    float4 cj4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    float bj = 0.0f;
                     if (lane < cnt) {
-                        float b = ball2[cb + lane];
-                        float ih2 = 4.0f / b;
-                        cpos[w][lane] = t.pos[cb + lane];
-                        caux[w][lane] = make_float4(b, ih2, 0.5f * (float)M_1_PI * sqrtf(ih2) * ih2, 0.0f);
+                        cj4 = t.pos[cb + lane];
+                        bj = ball2[cb + lane];
+                        rel = box_lb(make_float3(cj4.x, cj4.y, cj4.z), qlo, qhi, L, per) <
+                              fmaxf(bj, qlo.w);
+                    }
+                    const unsigned R = __ballot_sync(SKID_FULL, rel);
+                    const int nR = __popc(R);
+                    __syncwarp();
+                    if (rel) {
+                        const int k = __popc(R & ((1u << lane) - 1u));
+                        float ih2 = 4.0f / bj;
+                        cpos[w][k] = cj4;
+                        caux[w][k] = make_float4(bj, ih2, 0.5f * (float)M_1_PI * sqrtf(ih2) * ih2, 0.0f);
                     }
                     __syncwarp();
+                    if (!want) continue;
                     int cx = img_class(q.x, blo.x, bhi.x, hL.x);
                     int cy = img_class(q.y, blo.y, bhi.y, hL.y);
                     int cz = img_class(q.z, blo.z, bhi.z, hL.z);
                     bool mixed = (cx == 2) | (cy == 2) | (cz == 2);
-                    bool slow = __any_sync(SKID_FULL, mixed);
                     bool noshift = (cx == 0) & (cy == 0) & (cz == 0);
                     float sx = shifted(q.x, cx, L.x), sy = shifted(q.y, cy, L.y), sz = shifted(q.z, cz, L.z);
-                    for (int j = 0; j < cnt; ++j) {
+                    for (int j = 0; j < nR; ++j) {
                         float4 cj = cpos[w][j];
                         float4 aj = caux[w][j];
                         float dik, dki;
-                        if (slow) {
+                        if (mixed) {
                             dik = d2of(img_dx(q.x, cj.x, L.x, hL.x), img_dx(q.y, cj.y, L.y, hL.y),
                                        img_dx(q.z, cj.z, L.z, hL.z));
                             dki = d2of(img_dx(cj.x, q.x, L.x, hL.x), img_dx(cj.y, q.y, L.y, hL.y),
@@ -127,6 +180,10 @@ density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL,
                         if (dki < aj.x) kahan_add(s, c, cj.w * aj.z * w_m4(dki * aj.y));
                     }
                 }
+            } else {
+                float4 blo = t.lo[cp], bhi = t.hi[cp];
+                bool want = box_lb(q, blo, bhi, L, per) < fmaxf(bi, blo.w);
+                if (__any_sync(SKID_FULL, want)) { cp <<= 1; continue; }
             }
             cp = next_node(cp);
             if (cp == 1) break;
@@ -331,8 +388,10 @@ cudaError_t density_gather(const Tree &t, const float *ball2_sorted, float3 L, b
     int need = (t.nLeaf + G_WARPS - 1) / G_WARPS;
     if (blocks > need) blocks = need;
     float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
-    density_kernel<<<blocks, G_WARPS * 32, 0, st>>>(t.view(), ball2_sorted, L, hL, per, rho_sorted,
-                                                    d_work); skid::note_launch();
+    int subShift = 0;
+    while (subShift < 5 && (2 << subShift) <= t.leafBase) ++subShift;
+    density_kernel<<<blocks, G_WARPS * 32, 0, st>>>(t.view(), ball2_sorted, L, hL, per, subShift,
+                                                    rho_sorted, d_work); skid::note_launch();
     return cudaGetLastError();
 }
 

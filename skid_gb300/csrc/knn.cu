@@ -46,17 +46,54 @@ __device__ __forceinline__ void heap_replace_top(float *heap, int k, float d)
     heap[i * 32] = d;
 }
 
-// Process one leaf: candidates staged in shared memory, every lane tests all.
+// Lower bound of the float squared distance between any point of box a and
+// any point of box b (periodic images included); box_lb over every point of
+// a, with the slack of a's largest coordinate.
+__device__ __forceinline__ float boxbox_lb1(float alo, float ahi, float blo, float bhi, float L,
+                                            bool per)
+{
+    float d = fmaxf(fmaxf(blo - ahi, alo - bhi), 0.0f);
+    if (per) {
+        d = fminf(d, fmaxf(fmaxf(blo - (ahi + L), (alo + L) - bhi), 0.0f));
+        d = fminf(d, fmaxf(fmaxf(blo - (ahi - L), (alo - L) - bhi), 0.0f));
+    }
+    float slack = 4.8e-7f * (fmaxf(fabsf(alo), fabsf(ahi)) + (per ? L : 0.0f) +
+                             fmaxf(fabsf(blo), fabsf(bhi)));
+    return fmaxf(d - slack, 0.0f);
+}
+
+__device__ __forceinline__ float boxbox_lb(float4 alo, float4 ahi, float4 blo, float4 bhi, float3 L,
+                                           bool per)
+{
+    float dx = boxbox_lb1(alo.x, ahi.x, blo.x, bhi.x, L.x, per);
+    float dy = boxbox_lb1(alo.y, ahi.y, blo.y, bhi.y, L.y, per);
+    float dz = boxbox_lb1(alo.z, ahi.z, blo.z, bhi.z, L.z, per);
+    return (dx * dx + dy * dy + dz * dz) * (1.0f - 4e-6f);
+}
+
+// Process one leaf: candidates staged in shared memory, every lane tests all
+// of them.  With a query box (filter), lane j first drops candidate j when
+// its distance to the box is at least the warp's largest heap bound tmax:
+// no lane can take it; the survivors are compacted in order.
 __device__ __forceinline__ void knn_leaf(const TreeView &t, int node, float4 blo, float4 bhi,
-                                         KnnLane &ln, int k, float3 L, float3 hL, float4 *cand,
-                                         int lane)
+                                         KnnLane &ln, int k, float3 L, float3 hL, bool per,
+                                         float4 *cand, int lane, bool filter, float4 qlo,
+                                         float4 qhi, float tmax)
 {
     int leaf = node - t.leafBase;
     if (leaf >= t.nLeaf) return;
     int base = leaf * SKID_LEAF;
     int cnt = min(SKID_LEAF, t.n - base);
+    float4 c4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    bool rel = lane < cnt;
+    if (rel) {
+        c4 = t.pos[base + lane];
+        if (filter) rel = box_lb(make_float3(c4.x, c4.y, c4.z), qlo, qhi, L, per) < tmax;
+    }
+    const unsigned R = __ballot_sync(SKID_FULL, rel);
+    cnt = __popc(R);
     __syncwarp();
-    if (lane < cnt) cand[lane] = t.pos[base + lane];
+    if (rel) cand[__popc(R & ((1u << lane) - 1u))] = c4;
     __syncwarp();
     int cx = img_class(ln.q.x, blo.x, bhi.x, hL.x);
     int cy = img_class(ln.q.y, blo.y, bhi.y, hL.y);
@@ -90,12 +127,19 @@ __device__ __forceinline__ void knn_leaf(const TreeView &t, int node, float4 blo
     }
 }
 
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(SKID_FULL, v, o));
+    return v;
+}
+
 // Heaps live in shared memory after the candidate buffers, or -- for k too
 // large for one warp's heaps to fit -- in global scratch (gheap, one slab per
 // resident warp).
-__global__ void __launch_bounds__(KNN_WARPS * 32)
-knn_kernel(TreeView t, int k, float3 L, float3 hL, bool per, float *__restrict__ ball2,
-           int *work, float *gheap)
+__global__ void __launch_bounds__(KNN_WARPS * 32, 6)
+knn_kernel(TreeView t, int k, float3 L, float3 hL, bool per, int logLeafBase, int subShift,
+           float *__restrict__ ball2, int *work, float *gheap)
 {
     extern __shared__ float4 smem4[];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -103,6 +147,7 @@ knn_kernel(TreeView t, int k, float3 L, float3 hL, bool per, float *__restrict__
     float4 *cand = smem4 + w * SKID_LEAF;
     float *heaps = gheap ? gheap + (size_t)blockIdx.x * nw * k * 32
                          : reinterpret_cast<float *>(smem4 + nw * SKID_LEAF);
+    const int rootLo = t.leafBase >> subShift;
     KnnLane ln;
     ln.heap = heaps + (size_t)w * k * 32 + lane;
     for (;;) {
@@ -118,18 +163,35 @@ knn_kernel(TreeView t, int k, float3 L, float3 hL, bool per, float *__restrict__
         for (int i = 0; i < k; ++i) ln.heap[i * 32] = FLT_MAX;
         ln.thr = FLT_MAX;
         int own = t.leafBase + leaf;
-        knn_leaf(t, own, t.lo[own], t.hi[own], ln, k, L, hL, cand, lane);
+        const float4 qlo = t.lo[own], qhi = t.hi[own];   // the queries' box
+        knn_leaf(t, own, qlo, qhi, ln, k, L, hL, per, cand, lane, false, qlo, qhi, FLT_MAX);
         int cell = own;
         while (cell > 1) {
             int cp = cell ^ 1;
             int end = next_node(cp);
             for (;;) {
-                float4 blo = t.lo[cp], bhi = t.hi[cp];
-                float bd = box_lb(ln.q, blo, bhi, L, per);
-                bool want = bd < ln.thr;
-                if (__any_sync(SKID_FULL, want)) {
-                    if (cp < t.leafBase) { cp <<= 1; continue; }
-                    knn_leaf(t, cp, blo, bhi, ln, k, L, hL, cand, lane);
+                if (cp >= rootLo) {
+                    // a subtree of at most 2^subShift leaves: one lane per
+                    // leaf against the queries' box and the largest bound,
+                    // then each passing leaf in order with the exact bounds
+                    const int sh = logLeafBase - (31 - __clz(cp));
+                    const int first = cp << sh;
+                    float tmax = warp_max(ln.thr);
+                    bool pass = false;
+                    if (lane < (1 << sh) && first + lane - t.leafBase < t.nLeaf)
+                        pass = boxbox_lb(qlo, qhi, t.lo[first + lane], t.hi[first + lane], L, per) < tmax;
+                    for (unsigned lm = __ballot_sync(SKID_FULL, pass); lm; lm &= lm - 1) {
+                        const int node = first + __ffs(lm) - 1;
+                        float4 blo = t.lo[node], bhi = t.hi[node];
+                        bool want = box_lb(ln.q, blo, bhi, L, per) < ln.thr;
+                        if (!__any_sync(SKID_FULL, want)) continue;
+                        knn_leaf(t, node, blo, bhi, ln, k, L, hL, per, cand, lane, true, qlo, qhi,
+                                 warp_max(ln.thr));
+                    }
+                } else {
+                    float4 blo = t.lo[cp], bhi = t.hi[cp];
+                    bool want = box_lb(ln.q, blo, bhi, L, per) < ln.thr;
+                    if (__any_sync(SKID_FULL, want)) { cp <<= 1; continue; }
                 }
                 cp = next_node(cp);
                 if (cp == end) break;
@@ -182,7 +244,11 @@ cudaError_t knn_ball2(const Tree &t, int k, float3 L, bool per, float *ball2_sor
     }
     float3 hL = make_float3(0.5f * L.x, 0.5f * L.y, 0.5f * L.z);
     if ((e = cudaMemsetAsync(d_work, 0, sizeof(int), st))) return e;
-    knn_kernel<<<blocks, nw * 32, smem, st>>>(t.view(), k, L, hL, per, ball2_sorted, d_work, gh); skid::note_launch();
+    int logLeafBase = 0;
+    while ((2 << logLeafBase) <= t.leafBase) ++logLeafBase;
+    int subShift = logLeafBase < 5 ? logLeafBase : 5;
+    knn_kernel<<<blocks, nw * 32, smem, st>>>(t.view(), k, L, hL, per, logLeafBase, subShift,
+                                              ball2_sorted, d_work, gh); skid::note_launch();
     return cudaGetLastError();
 }
 
