@@ -259,8 +259,8 @@ FieldArgs skid_ctx::field_args(float fStep, bool initial, float *acc_out)
     a.blo = ctree.blo.p;
     a.bhi = ctree.bhi.p;
     a.leafBase = ctree.leafBase;
-    a.subShift = 0;
-    while (a.subShift < 5 && (2 << a.subShift) <= a.leafBase) ++a.subShift;
+    a.logLeafBase = 0;
+    while ((2 << a.logLeafBase) <= a.leafBase) ++a.logLeafBase;
     a.d_nC = C.d_n;
     a.mpos = M.mpos.p;
     a.act = M.act.p;

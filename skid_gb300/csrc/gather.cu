@@ -192,12 +192,13 @@ density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL,
     }
 }
 
-// Movers per warp G: 32 (one per lane), 8 (4 lanes each) or 1 (the warp
-// shares one mover).  Fewer movers per warp keep the union of their
-// neighbourhoods small when the active movers are sparse.  Each lane tests
-// G candidates of a visited leaf (one cheap pass that sets a hit mask), then
-// runs the field terms for its hits only; a mover's lanes are combined with
-// a fixed xor-butterfly, so sums are deterministic for a given G.
+// Movers per warp G: 32, 16, 8, 4 or 1, with 32/G lanes per mover.  Fewer
+// movers per warp keep the union of their neighbourhoods small when the
+// active movers are sparse.  At a visited leaf the candidates whose ball
+// reaches the movers' box are compacted in order; a mover's lanes test every
+// (32/G)-th of them (one cheap pass that sets a hit mask), then run the field
+// terms for their hits only, and are combined with a fixed xor-butterfly, so
+// sums are deterministic for a given G.
 template <int G, bool STATS>
 __global__ void __launch_bounds__(G_WARPS * 32, SKID_FIELD_MINB)
 field_kernel(FieldArgs a)
@@ -234,100 +235,109 @@ field_kernel(FieldArgs a)
             whi.z = fmaxf(whi.z, __shfl_xor_sync(SKID_FULL, whi.z, o));
         }
         float ax = 0.0f, ay = 0.0f, az = 0.0f;
-        // Depth-first walk by ball boxes.  Nodes whose subtree holds the last
-        // 2^subShift leaves (5 levels) are not descended one by one: each lane
-        // tests one of their leaves against the movers' box, and the leaves
-        // that pass are visited in order (the depth-first leaf order).
-        const int rootLo = a.leafBase >> a.subShift;
-        int cp = 1;
-        for (;;) {
-            if (cp >= rootLo) {
-                const int first = cp << a.subShift;
-                bool pass = false;
-                if (lane < (1 << a.subShift)) {
-                    float4 bl = a.blo[first + lane], bh = a.bhi[first + lane];
-                    pass = bl.x <= whi.x && bh.x >= wlo.x && bl.y <= whi.y && bh.y >= wlo.y &&
-                           bl.z <= whi.z && bh.z >= wlo.z;
+        // Depth-first walk by ball boxes in strides of five levels, aligned
+        // so the last stride ends at the leaves: a visited node has each lane
+        // test one of its 32 descendants five levels down against the movers'
+        // box, and those that pass are visited in order (so leaves come in
+        // depth-first order).  A visited node is entered only if some mover
+        // lies in its ball box.  Stack level l (its first node and the
+        // descendants still to visit) is held by lane l.
+        auto reach = [&](int node) {
+            float4 bl = a.blo[node], bh = a.bhi[node];
+            return bl.x <= whi.x && bh.x >= wlo.x && bl.y <= whi.y && bh.y >= wlo.y &&
+                   bl.z <= whi.z && bh.z >= wlo.z;
+        };
+        unsigned smask;
+        int sfirst;
+        {
+            const int d0 = a.logLeafBase % 5;
+            sfirst = 1 << d0;
+            smask = __ballot_sync(SKID_FULL, lane < (1 << d0) && reach(sfirst + lane));
+        }
+        int sp = 0;
+        while (sp >= 0) {
+            const unsigned m = __shfl_sync(SKID_FULL, smask, sp);
+            if (!m) { --sp; continue; }
+            const int node = __shfl_sync(SKID_FULL, sfirst, sp) + __ffs(m) - 1;
+            if (lane == sp) smask = m & (m - 1);
+            if (STATS) ++st_nodes;
+            {
+                float4 blo = a.blo[node], bhi = a.bhi[node];
+                bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y &&
+                            y.y <= bhi.y && y.z >= blo.z && y.z <= bhi.z;
+                if (!__any_sync(SKID_FULL, want)) continue;
+                if (node < a.leafBase) {
+                    const int cf = node << 5;
+                    const unsigned cm = __ballot_sync(SKID_FULL, reach(cf + lane));
+                    if (cm) {
+                        ++sp;
+                        if (lane == sp) { smask = cm; sfirst = cf; }
+                    }
+                    continue;
                 }
-                if (STATS) ++st_nodes;
-                for (unsigned lm = __ballot_sync(SKID_FULL, pass); lm; lm &= lm - 1) {
-                    const int node = first + __ffs(lm) - 1;
-                    float4 blo = a.blo[node], bhi = a.bhi[node];
-                    bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y &&
-                                y.y <= bhi.y && y.z >= blo.z && y.z <= bhi.z;
-                    if (!__any_sync(SKID_FULL, want)) continue;
-                    int cb = (node - a.leafBase) * SKID_LEAF;
-                    int cnt = min(SKID_LEAF, nC - cb);
-                    if (STATS) ++st_leaves;
-                    // prefilter: lane j keeps candidate j if its ball (radius
-                    // rounded up) reaches the movers' box; the exact test below
-                    // decides, so this only skips candidates that cannot hit
-                    bool rel = false;
-                    float4 c4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (lane < cnt) {
-                        c4 = a.cpos[cb + lane];
-                        // ball radius from the approximate reciprocal square root,
-                        // widened to cover its error (an empty ball, fBall2 = 0,
-                        // gives NaN and is rejected, as the exact test would)
-                        float r = c4.w * rsqrtf(c4.w) * (1.0f + 4e-6f) +
-                                  1e-6f * (fabsf(c4.x) + fabsf(c4.y) + fabsf(c4.z)) + 1e-30f;
-                        rel = c4.x + r >= wlo.x && c4.x - r <= whi.x && c4.y + r >= wlo.y &&
-                              c4.y - r <= whi.y && c4.z + r >= wlo.z && c4.z - r <= whi.z;
-                    }
-                    // the survivors, compacted in candidate order
-                    const unsigned R = __ballot_sync(SKID_FULL, rel);
-                    const int nR = __popc(R);
-                    const int slotR = __popc(R & ((1u << lane) - 1u));
-                    __syncwarp();
-                    if (rel) {
-                        cpos_s[w][slotR] = c4;
-                        float4 cc = a.ccoef[cb + lane];
-                        ccoef_s[w][slotR] = make_float2(cc.x, cc.y);
-                    }
-                    __syncwarp();
-                    // a mover's L lanes take every L-th survivor
-                    unsigned mask = 0;
-                    if (want) {
+                int cb = (node - a.leafBase) * SKID_LEAF;
+                int cnt = min(SKID_LEAF, nC - cb);
+                if (STATS) ++st_leaves;
+                // prefilter: lane j keeps candidate j if its ball (radius
+                // rounded up) reaches the movers' box; the exact test below
+                // decides, so this only skips candidates that cannot hit
+                bool rel = false;
+                float4 c4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (lane < cnt) {
+                    c4 = a.cpos[cb + lane];
+                    // ball radius from the approximate reciprocal square root,
+                    // widened to cover its error (an empty ball, fBall2 = 0,
+                    // gives NaN and is rejected, as the exact test would)
+                    float r = c4.w * rsqrtf(c4.w) * (1.0f + 4e-6f) +
+                              1e-6f * (fabsf(c4.x) + fabsf(c4.y) + fabsf(c4.z)) + 1e-30f;
+                    rel = c4.x + r >= wlo.x && c4.x - r <= whi.x && c4.y + r >= wlo.y &&
+                          c4.y - r <= whi.y && c4.z + r >= wlo.z && c4.z - r <= whi.z;
+                }
+                // the survivors, compacted in candidate order
+                const unsigned R = __ballot_sync(SKID_FULL, rel);
+                const int nR = __popc(R);
+                const int slotR = __popc(R & ((1u << lane) - 1u));
+                __syncwarp();
+                if (rel) {
+                    cpos_s[w][slotR] = c4;
+                    float4 cc = a.ccoef[cb + lane];
+                    ccoef_s[w][slotR] = make_float2(cc.x, cc.y);
+                }
+                __syncwarp();
+                // a mover's L lanes take every L-th survivor
+                unsigned mask = 0;
+                if (want) {
 #pragma unroll FIELD_UNROLL
-                        for (int t = sub; t < nR; t += L) {
-                            float4 c = cpos_s[w][t];
-                            // smBallGather's test (smooth1.c:365-369), from the copy
-                            float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
-                            mask |= (unsigned)(d2 < c.w) << t;
-                        }
-                        if (STATS) st_tests += (nR - sub + L - 1) / L;
+                    for (int t = sub; t < nR; t += L) {
+                        float4 c = cpos_s[w][t];
+                        // smBallGather's test (smooth1.c:365-369), from the copy
+                        float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
+                        mask |= (unsigned)(d2 < c.w) << t;
                     }
-                    if (STATS) st_hits += __popc(mask);
-                    for (unsigned m = mask; m; m &= m - 1) {
-                        int j = __ffs(m) - 1;
-                        float4 c = cpos_s[w][j];
-                        float2 k = ccoef_s[w][j];
-                        // the field value (smooth1.c:450-458) only has to be
-                        // accurate, not bit-exact: FMA and the approximate
-                        // reciprocal square root (q = r2 / sqrt(r2), 1/q)
-                        float dx = c.x - y.x, dy = c.y - y.y, dz = c.z - y.z;
-                        float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) * k.x;
-                        float iq = rsqrtf(r2);
-                        float q = r2 > 0.0f ? r2 * iq : 0.0f;
-                        float F = r2 < 1.0f ? __fmaf_rn(2.25f, q, -3.0f)
-                                            : __fmaf_rn(-0.75f, q, 3.0f) - 3.0f * iq;
-                        F *= k.y;
-                        ax = __fmaf_rn(dx, F, ax);
-                        ay = __fmaf_rn(dy, F, ay);
-                        az = __fmaf_rn(dz, F, az);
-                    }
-                    unsigned any = __reduce_or_sync(SKID_FULL, mask);
-                    if (rel && ((any >> slotR) & 1u)) a.touched[cb + lane] = 1;
+                    if (STATS) st_tests += (nR - sub + L - 1) / L;
                 }
-            } else {
-                float4 blo = a.blo[cp], bhi = a.bhi[cp];
-                bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y && y.y <= bhi.y &&
-                            y.z >= blo.z && y.z <= bhi.z;
-                if (STATS) ++st_nodes;
-                if (__any_sync(SKID_FULL, want)) { cp <<= 1; continue; }
+                if (STATS) st_hits += __popc(mask);
+                for (unsigned m = mask; m; m &= m - 1) {
+                    int j = __ffs(m) - 1;
+                    float4 c = cpos_s[w][j];
+                    float2 k = ccoef_s[w][j];
+                    // the field value (smooth1.c:450-458) only has to be
+                    // accurate, not bit-exact: FMA and the approximate
+                    // reciprocal square root (q = r2 / sqrt(r2), 1/q)
+                    float dx = c.x - y.x, dy = c.y - y.y, dz = c.z - y.z;
+                    float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) * k.x;
+                    float iq = rsqrtf(r2);
+                    float q = r2 > 0.0f ? r2 * iq : 0.0f;
+                    float F = r2 < 1.0f ? __fmaf_rn(2.25f, q, -3.0f)
+                                        : __fmaf_rn(-0.75f, q, 3.0f) - 3.0f * iq;
+                    F *= k.y;
+                    ax = __fmaf_rn(dx, F, ax);
+                    ay = __fmaf_rn(dy, F, ay);
+                    az = __fmaf_rn(dz, F, az);
+                }
+                unsigned any = __reduce_or_sync(SKID_FULL, mask);
+                if (rel && ((any >> slotR) & 1u)) a.touched[cb + lane] = 1;
             }
-            cp = next_node(cp);
-            if (cp == 1) break;
         }
 #pragma unroll
         for (int o = L / 2; o > 0; o >>= 1) {

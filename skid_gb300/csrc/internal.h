@@ -165,7 +165,7 @@ struct FieldArgs {
     const float4 *cpos, *ccoef;      // copies
     const float4 *blo, *bhi;         // ball boxes of the copy tree
     int leafBase;
-    int subShift;                    // log2 of the leaves a node tests in parallel (<= 5)
+    int logLeafBase;                 // depth of the leaves (leafBase = 2^logLeafBase)
     const int *d_nC;                 // live copies
     float4 *mpos;                    // mover positions (w unused)
     const int *act;                  // active mover indices
