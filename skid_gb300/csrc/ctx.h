@@ -234,7 +234,7 @@ struct skid_ctx {
     // Crossovers measured on GB300 with the 2^21-particle workload: per-step
     // move-field time is lowest with 32 movers per warp above ~600k active
     // movers, 16 down to ~400k, 8 down to ~50k, 4 down to ~25k, one below.
-    int opt_G = 0, opt_g32_min = 600000, opt_g16_min = 400000, opt_g8_min = 50000, opt_g4_min = 25000;
+    int opt_G = 0, opt_g32_min = 600000, opt_g16_min = 400000, opt_g8_min = 100000, opt_g4_min = 30000;
     int opt_unbind_tw = -1, opt_unbind_bs = -1;   // -1: autotuned on the first skid_unbind
     bool opt_unbind_per_group = false;
     bool opt_field_unfused = false;                // field pass and move pass as separate kernels

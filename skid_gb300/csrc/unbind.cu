@@ -66,6 +66,18 @@ __device__ __forceinline__ float spline_pot(float d2, float twoh, int plummer)
     return 1.0f / r;
 }
 
+// The pair factor used for every potential term, added (potentials) and
+// subtracted (removal) alike.  Beyond the softening (r >= 2h, certain once
+// d2 clears (2h)^2 by the margin below) it is 1/r, taken as the correctly
+// rounded reciprocal square root of d2 -- one rounding, as the FP64 1/sqrt
+// of grav.h:11-31 rounded to float; inside, the spline above.
+__device__ __forceinline__ float pair_dir(float d2, float twoh, int plummer)
+{
+    if (plummer) return rsqrtf(d2 + 0.25f * twoh * twoh);
+    if (d2 >= twoh * twoh * 1.000001f) return rsqrtf(d2);
+    return spline_pot(d2, twoh, 0);
+}
+
 __device__ __forceinline__ float wrap_h(float d, float h)
 {
     // kd.c:1345-1350: if (dx > hx) dx -= 2*hx; if (dx <= -hx) dx += 2*hx
@@ -266,12 +278,34 @@ __global__ void pot_fill(const uint32_t *__restrict__ order, const int *d_nvalid
     }
 }
 
-// One tile pair (I, J) of one group per block iteration.  Off-diagonal
-// items take every (i in I, j in J); diagonal items every i < j in the tile,
-// plus the scoop terms of the tile's rows (kdAddScoopPot, grav.c:112-127).
-// At rotation step k thread t pairs its row with column (t + k) mod T, so a
-// column's shared accumulator is touched by one thread per step.
-__global__ void __launch_bounds__(POT_TILE)
+// One tile pair (I, J) of one group per block iteration, POT_TILE / 2
+// threads with two rows each (t and t + POT_TILE / 2).  Off-diagonal items
+// take every (i in I, j in J); diagonal items every i < j in the tile, plus
+// the scoop terms of the tile's rows (kdAddScoopPot, grav.c:112-127).  At
+// rotation step k thread t pairs its rows with column (t + k) mod T: the
+// lanes of a warp touch distinct columns, so each warp keeps its own column
+// accumulators (plain adds, a warp barrier per step), summed at the end.
+// Columns carry G m 2^S, so a term is one multiply from its quantum.
+constexpr int POT_THREADS = POT_TILE / 2;
+
+struct PotRow {
+    float4 r;     // position, G m 2^S
+    float e;      // softening
+    bool v;       // a member of the tile
+};
+
+// The terms of row a and column j (tr: on a, tc: on j).
+__device__ __forceinline__ void pot_pair(const PotRow &a, float4 rj, float ej, int plummer,
+                                         long long &tr, long long &tc)
+{
+    float d2 = d2of(fsub(a.r.x, rj.x), fsub(a.r.y, rj.y), fsub(a.r.z, rj.z));
+    float dir = pair_dir(d2, fadd(a.e, ej), plummer);
+    tr = fx(fmul(rj.w, dir), 1.0f);
+    // equal masses (all-dark runs): both ends get the same term
+    tc = rj.w == a.r.w ? tr : fx(fmul(a.r.w, dir), 1.0f);
+}
+
+__global__ void __launch_bounds__(POT_THREADS)
 pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_host,
                const int *__restrict__ gstart, const int *__restrict__ gcount,
                const float4 *__restrict__ qr, const float4 *__restrict__ qv,
@@ -279,68 +313,100 @@ pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_h
                const float4 *__restrict__ slist, const float *__restrict__ ssoft, float G,
                int plummer, float scale, long long *__restrict__ pot)
 {
-    constexpr int T = POT_TILE;
+    constexpr int T = POT_TILE, H = POT_TILE / 2, NW = POT_THREADS / 32;
     __shared__ float4 sr[T];
     __shared__ float ss[T];
-    __shared__ unsigned long long acc_j[T];
-    const int t = threadIdx.x;
+    __shared__ long long acc_w[NW][T];
+    const int t = threadIdx.x, wid = t >> 5;
     const int nitems = nitems_host >= 0 ? nitems_host : *d_nitems;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         int2 w = items[it];
         int g = w.x, I = w.y >> 16, J = w.y & 0xffff;
         int s = gstart[g], n = gcount[g];
-        int i = I * T + t;
-        bool vi = i < n;
-        float4 ri = vi ? qr[s + i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        float ei = vi ? qv[s + i].w : 0.0f;
+        PotRow ra, rb;
+        {
+            const int ia = I * T + t, ib = ia + H;
+            ra.v = ia < n;
+            rb.v = ib < n;
+            float4 q = ra.v ? qr[s + ia] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            ra.r = make_float4(q.x, q.y, q.z, fmul(G, q.w) * scale);
+            ra.e = ra.v ? qv[s + ia].w : 0.0f;
+            q = rb.v ? qr[s + ib] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            rb.r = make_float4(q.x, q.y, q.z, fmul(G, q.w) * scale);
+            rb.e = rb.v ? qv[s + ib].w : 0.0f;
+        }
         int j0 = J * T;
         int nj = min(T, n - j0);
         __syncthreads();
-        if (t < nj) {
-            sr[t] = qr[s + j0 + t];
-            ss[t] = qv[s + j0 + t].w;
-        }
-        acc_j[t] = 0ull;
-        __syncthreads();
-        long long acc = 0;
-        if (vi) {
-            int kmax = I != J ? T : T / 2 + 1;
-            for (int k = I != J ? 0 : 1; k < kmax; ++k) {
-                int jl = (t + k) & (T - 1);
-                if (jl >= nj) continue;
-                if (I == J && k == T / 2 && t >= T / 2) continue;   // each pair once
-                float4 rj = sr[jl];
-                float d2 = d2of(fsub(ri.x, rj.x), fsub(ri.y, rj.y), fsub(ri.z, rj.z));
-                float dir = spline_pot(d2, fadd(ei, ss[jl]), plummer);
-                const long long tij = fx(fmul(fmul(G, rj.w), dir), scale);
-                // equal masses (all-dark runs): both ends get the same term
-                const long long tji = rj.w == ri.w ? tij : fx(fmul(fmul(G, ri.w), dir), scale);
-                acc += tij;
-                atomicAdd(&acc_j[jl], (unsigned long long)tji);
+        for (int c = t; c < T; c += POT_THREADS) {
+            if (c < nj) {
+                float4 q = qr[s + j0 + c];
+                sr[c] = make_float4(q.x, q.y, q.z, fmul(G, q.w) * scale);
+                ss[c] = qv[s + j0 + c].w;
             }
+#pragma unroll
+            for (int k = 0; k < NW; ++k) acc_w[k][c] = 0;
         }
-        if (I == J) {
+        __syncthreads();
+        long long acca = 0, accb = 0;
+        if (I != J) {
+            for (int k = 0; k < T; ++k) {
+                const int jl = (t + k) & (T - 1);
+                if (jl < nj) {
+                    const float4 rj = sr[jl];
+                    const float ej = ss[jl];
+                    long long tr, tc, col = 0;
+                    if (ra.v) { pot_pair(ra, rj, ej, plummer, tr, tc); acca += tr; col += tc; }
+                    if (rb.v) { pot_pair(rb, rj, ej, plummer, tr, tc); accb += tr; col += tc; }
+                    acc_w[wid][jl] += col;
+                }
+                __syncwarp();
+            }
+        } else {
+            // offset (column - row) mod T in 1..T/2 for row t (k = 1..H),
+            // 1..T/2-1 for row t + H (k = H+1..T-1): each pair once
+            for (int k = 1; k < T; ++k) {
+                const int jl = (t + k) & (T - 1);
+                const PotRow &a = k <= H ? ra : rb;
+                if (jl < nj && a.v) {
+                    long long tr, tc;
+                    pot_pair(a, sr[jl], ss[jl], plummer, tr, tc);
+                    if (k <= H) acca += tr; else accb += tr;
+                    acc_w[wid][jl] += tc;
+                }
+                __syncwarp();
+            }
             int so = soff[g], sc = scnt[g];
             for (int jb = 0; jb < sc; jb += T) {
                 __syncthreads();
-                if (jb + t < sc) {
-                    sr[t] = slist[so + jb + t];
-                    ss[t] = ssoft[so + jb + t];
-                }
+                for (int c = t; c < T; c += POT_THREADS)
+                    if (jb + c < sc) {
+                        float4 q = slist[so + jb + c];
+                        sr[c] = make_float4(q.x, q.y, q.z, fmul(G, q.w) * scale);
+                        ss[c] = ssoft[so + jb + c];
+                    }
                 __syncthreads();
                 int cnt = min(T, sc - jb);
-                if (vi)
-                    for (int k = 0; k < cnt; ++k) {
-                        float4 rj = sr[k];
-                        float d2 = d2of(fsub(rj.x, ri.x), fsub(rj.y, ri.y), fsub(rj.z, ri.z));
-                        float dir = spline_pot(d2, fadd(ss[k], ei), plummer);
-                        acc += fx(fmul(fmul(G, rj.w), dir), scale);
-                    }
+                for (int k = 0; k < cnt; ++k) {
+                    const float4 rj = sr[k];
+                    const float ej = ss[k];
+                    // kdAddScoopPot's pair: d2 from the scoop particle
+                    float d2a = d2of(fsub(rj.x, ra.r.x), fsub(rj.y, ra.r.y), fsub(rj.z, ra.r.z));
+                    float d2b = d2of(fsub(rj.x, rb.r.x), fsub(rj.y, rb.r.y), fsub(rj.z, rb.r.z));
+                    if (ra.v) acca += fx(fmul(rj.w, pair_dir(d2a, fadd(ej, ra.e), plummer)), 1.0f);
+                    if (rb.v) accb += fx(fmul(rj.w, pair_dir(d2b, fadd(ej, rb.e), plummer)), 1.0f);
+                }
             }
         }
         __syncthreads();
-        if (vi) atomicAdd((unsigned long long *)&pot[s + i], (unsigned long long)acc);
-        if (t < nj && acc_j[t]) atomicAdd((unsigned long long *)&pot[s + j0 + t], acc_j[t]);
+        if (ra.v) atomicAdd((unsigned long long *)&pot[s + I * T + t], (unsigned long long)acca);
+        if (rb.v) atomicAdd((unsigned long long *)&pot[s + I * T + t + H], (unsigned long long)accb);
+        for (int c = t; c < nj; c += POT_THREADS) {
+            long long cs = 0;
+#pragma unroll
+            for (int k = 0; k < NW; ++k) cs += acc_w[k][c];
+            if (cs) atomicAdd((unsigned long long *)&pot[s + j0 + c], (unsigned long long)cs);
+        }
     }
 }
 
@@ -440,8 +506,8 @@ __device__ __forceinline__ long long sub_pot(const RemoveArgs &A, float4 rs, flo
                                              float4 v, long long p)
 {
     float d2 = d2of(fsub(rs.x, r.x), fsub(rs.y, r.y), fsub(rs.z, r.z));
-    float dir = spline_pot(d2, fadd(es, v.w), A.plummer);
-    return p - fx(fmul(fmul(A.G, rs.w), dir), A.scale);
+    float dir = pair_dir(d2, fadd(es, v.w), A.plummer);
+    return p - fx(fmul(fmul(A.G, rs.w) * A.scale, dir), 1.0f);
 }
 
 // centre of mass: kd.c:1360-1375 (FP64 sums of float products)
@@ -912,11 +978,11 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     A.d_queue = U.cnt.p + 6;
     A.single = 0;
 
-    const int potBlocks = nitems < num_sms() * 16 ? (nitems > 0 ? nitems : 1) : num_sms() * 16;
+    const int potBlocks = nitems < num_sms() * 32 ? (nitems > 0 ? nitems : 1) : num_sms() * 32;
     auto potentials = [&]() -> cudaError_t {
         cudaError_t e2 = cudaMemsetAsync(U.pot.p, 0, nslots * sizeof(long long), st);
         if (e2 || nitems <= 0) return e2;
-        pot_sym_kernel<<<potBlocks, POT_TILE, 0, st>>>(U.items.p, U.cnt.p + 1, -1, G.start.p, G.count.p,
+        pot_sym_kernel<<<potBlocks, POT_THREADS, 0, st>>>(U.items.p, U.cnt.p + 1, -1, G.start.p, G.count.p,
                                                        U.qr.p, U.qv.p, U.soff.p, U.scnt.p, U.slist.p,
                                                        U.ssoft.p, P.G, P.plummer, P.scale, U.pot.p); note_launch();
         return cudaGetLastError();
@@ -943,7 +1009,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
         if ((e = cudaMemsetAsync(d_unbound, 0, sizeof(int), st))) return e;
         for (int k = 0; k < nvalid; ++k) {
             int cnt = ioff[k + 1] - ioff[k];
-            pot_sym_kernel<<<cnt < num_sms() * 16 ? cnt : num_sms() * 16, POT_TILE, 0, st>>>(
+            pot_sym_kernel<<<cnt < num_sms() * 32 ? cnt : num_sms() * 32, POT_THREADS, 0, st>>>(
                 U.items.p + ioff[k], nullptr, cnt, G.start.p, G.count.p, U.qr.p, U.qv.p, U.soff.p,
                 U.scnt.p, U.slist.p, U.ssoft.p, P.G, P.plummer, P.scale, U.pot.p); note_launch();
             RemoveArgs A1 = A;
