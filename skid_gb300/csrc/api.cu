@@ -278,12 +278,6 @@ FieldArgs skid_ctx::field_args(float fStep, bool initial, float *acc_out)
     return a;
 }
 
-__global__ void field_bytes_kernel(const int *d_nA, const int *d_nS, double *acc)
-{
-    acc[0] += 24.0 * (double)*d_nA + 20.0 * (double)*d_nS;
-    acc[1] += 1.0;
-}
-
 // One move pass: field + move, cut, refit.  Stream-ordered, no host sync.
 // `slot` picks the event pair that times this step's field kernel.
 int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int G)
@@ -291,7 +285,6 @@ int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int 
     skid_ctx *ctx = this;
     FieldArgs a = field_args(fStep, initial, nullptr);
     a.G = G;
-    field_bytes_kernel<<<1, 1, 0, st>>>(M.d_nA, C.d_n, d_fbytes); skid::note_launch();
     // while capturing, external records make the events real timing nodes of
     // the outer-iteration graph (a plain record would only order the capture)
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -308,7 +301,7 @@ int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int 
         CK(field_move(a, nMove, st));
     }
     CK(cudaEventRecordWithFlags(fev[2 * slot + 1], st, evflags));
-    CK(scatter_cut(C, initial, nocut, rho_final.p, ss, st));
+    CK(scatter_cut(C, initial, nocut, rho_final.p, M.d_nA, d_fbytes, st));
     CK(tree_refit(ctree, C.cpos.p, nullptr, C.d_n, st, true, C.d_dirty));
     return 0;
 }
@@ -430,6 +423,7 @@ int skid_create(skid_ctx **pctx, const skid_params *par)
     ctx->C.d_n2 = ctx->d_scal + SC_NC2;
     ctx->C.d_floor = (unsigned *)(ctx->d_scal + SC_FLOOR);
     ctx->C.d_dirty = ctx->d_scal + SC_DIRTY;
+    ctx->C.d_done = ctx->d_scal + SC_DONE;
     ctx->M.d_nA = ctx->d_scal + SC_NA;
     ctx->M.d_nA2 = ctx->d_scal + SC_NA2;
     *pctx = ctx;
@@ -731,7 +725,8 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
     int G = ctx->movers_per_warp();
     int gs = graph_slot(G);
     bool same = ctx->iter_graph[gs] && ctx->g_fStep[gs] == fStep && ctx->g_fCvg[gs] == fCvg &&
-                ctx->g_nocut[gs] == (bNoCut != 0) && ctx->g_stats[gs] == ctx->field_stats_on;
+                ctx->g_nocut[gs] == (bNoCut != 0) && ctx->g_stats[gs] == ctx->field_stats_on &&
+                ctx->g_bound[gs] >= ctx->nActive;
     bool ran = false;
     if (!same) {
         if (ctx->iter_graph[gs]) {
@@ -755,7 +750,8 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
             int rc = 0;
             for (int i = 0; i < PRUNE_STEPS && !rc; ++i)
                 rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G);
-            if (!rc && mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st))
+            const int bound = ctx->slot_bound(G);
+            if (!rc && mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st, bound))
                 rc = SKID_ECUDA;
             set_capturing(false);
             cudaError_t ce = cudaStreamEndCapture(st, &g);
@@ -778,6 +774,7 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
             ctx->g_fCvg[gs] = fCvg;
             ctx->g_nocut[gs] = bNoCut != 0;
             ctx->g_stats[gs] = ctx->field_stats_on;
+            ctx->g_bound[gs] = bound;
         }
     }
     if (!ran) {

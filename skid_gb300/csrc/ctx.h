@@ -25,6 +25,7 @@ enum {
     SC_NG2 = 10,
     SC_NUNB = 11,    // particles unbound
     SC_WORK2 = 12,
+    SC_DONE = 13,    // finished blocks of the copy write-back (last one publishes)
     SC_COUNT = 32
 };
 
@@ -190,6 +191,7 @@ struct skid_ctx {
     float g_fStep[NSLOT] = {}, g_fCvg[NSLOT] = {};
     bool g_nocut[NSLOT] = {};
     bool g_stats[NSLOT] = {};
+    int g_bound[NSLOT] = {};                 // active movers the graph's prune is sized for
     float3 mkey_lo{}, mkey_inv{};   // Morton frame of mover positions
     // move-field kernel timing: an event pair per step slot of an iteration
     cudaEvent_t fev[2 * skid::PRUNE_STEPS] = {};
@@ -239,6 +241,18 @@ struct skid_ctx {
     bool opt_unbind_per_group = false;
     bool opt_field_unfused = false;                // field pass and move pass as separate kernels
     skid::DBuf<float> unfused_acc;
+    // Largest active count that selects G (the prune of an iteration graph
+    // for G is sized for it; the count only falls within a run).
+    int slot_bound(int G) const
+    {
+        int b = opt_G || G == 32 ? M.cap
+                : G == 16        ? opt_g32_min
+                : G == 8         ? opt_g16_min
+                : G == 4         ? opt_g8_min
+                                 : opt_g4_min;
+        if (b < nActive) b = nActive;
+        return b < M.cap ? b : M.cap;
+    }
     int movers_per_warp() const
     {
         if (opt_G) return opt_G;

@@ -335,6 +335,8 @@ field_kernel(FieldArgs a)
                     ay = __fmaf_rn(dy, F, ay);
                     az = __fmaf_rn(dz, F, az);
                 }
+                // copies that reached a mover: touched, and their density
+                // enters the floor of the cut (smooth1.c:460-461)
                 unsigned any = __reduce_or_sync(SKID_FULL, mask);
                 if (rel && ((any >> slotR) & 1u)) a.touched[cb + lane] = 1;
             }

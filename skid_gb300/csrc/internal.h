@@ -66,6 +66,7 @@ struct Tree {
     DBuf<float4> lo, hi;   // point boxes per node
     DBuf<float4> blo, bhi; // ball boxes per node (scatterer trees)
     DBuf<int> flag;        // up-pass arrival counters
+    bool flag_clear = false;   // flag holds zeros (each refit leaves it so)
     TreeView view() const
     {
         TreeView v;
@@ -131,19 +132,21 @@ struct CopyState {
     DBuf<float4> cpos, ccoef, cpos2, ccoef2;
     DBuf<unsigned char> touched;    // reached an active mover this step
     DBuf<int> keep, kpos;
+    DBuf<int> blk;                  // kept copies per cut tile
     DBuf<unsigned> mask;            // build-time image masks
     DBuf<int> cnt, off;             // build-time copy counts / offsets
     int *d_n = nullptr;             // live copies (device)
     int *d_n2 = nullptr;
     unsigned *d_floor = nullptr;    // ordered-uint min density (fScatDens)
     int *d_dirty = nullptr;         // copies changed since the last refit
+    int *d_done = nullptr;          // finished write-back blocks (zero between steps)
     cudaError_t alloc(int n)
     {
         cudaError_t e;
         size_t m = n > 0 ? n : 1;
         if ((e = dalloc(cpos, m)) || (e = dalloc(ccoef, m)) || (e = dalloc(cpos2, m)) ||
             (e = dalloc(ccoef2, m)) || (e = dalloc(touched, m)) || (e = dalloc(keep, m)) ||
-            (e = dalloc(kpos, m)))
+            (e = dalloc(kpos, m)) || (e = dalloc(blk, (m + 4095) / 4096)))
             return e;
         cap = (int)m;
         return cudaSuccess;
@@ -157,6 +160,7 @@ struct MoverState {
     DBuf<float4> mpos, mold;
     DBuf<int> mio;                  // iOrder of each mover
     DBuf<int> act, act2, keep, kpos;
+    DBuf<int> blk;                  // surviving movers per prune tile
     int *d_nA = nullptr;
     int *d_nA2 = nullptr;
 };
@@ -192,11 +196,12 @@ cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rh
                          int ns, float3 L, float3 boxlo, float3 boxhi, bool periodic,
                          CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st);
 // After a move pass: density floor, cut, stable compaction, counts.
-cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, SortScratch &ss,
-                        cudaStream_t st);
+cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, const int *d_nA,
+                        double *d_fbytes, cudaStream_t st);
 // Prune converged movers, then re-sort the active ones by Morton key.
+// bound: active movers at most (the sort and tiles are sized for it).
 cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,
-                        SortScratch &ss, cudaStream_t st);
+                        SortScratch &ss, cudaStream_t st, int bound = -1);
 
 inline int grid_for(int n, int threads = 256)
 {

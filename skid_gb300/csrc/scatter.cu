@@ -120,7 +120,46 @@ __global__ void copy_permute_kernel(const uint32_t *__restrict__ perm, int n,
     }
 }
 
-// Pass 1 of the cut: density floor over touched copies.
+// ---- the cut, in tiles of CT_TILE slots: keep flags and per-tile counts,
+// then each tile compacts itself from the counts before it ----
+constexpr int CT_THREADS = 256;
+constexpr int CT_ITEMS = 16;
+constexpr int CT_TILE = CT_THREADS * CT_ITEMS;   // matches the blk sizing (4096)
+
+// Sum over the block (every thread gets it).
+__device__ __forceinline__ int block_sum(int v, int *sh)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(SKID_FULL, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    int t = 0;
+    for (int k = 0; k < nw; ++k) t += sh[k];
+    return t;
+}
+
+// Exclusive prefix over the block's threads in thread order.
+__device__ __forceinline__ int block_excl(int v, int *sh)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(SKID_FULL, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    int before = 0;
+    for (int k = 0; k < w; ++k) before += sh[k];
+    (void)nw;
+    return before + x - v;
+}
+
+// The density floor over touched copies (smooth1.c:460-461).
 __global__ void floor_kernel(const float4 *__restrict__ ccoef,
                              const unsigned char *__restrict__ touched, const int *d_n,
                              unsigned *d_floor)
@@ -129,24 +168,30 @@ __global__ void floor_kernel(const float4 *__restrict__ ccoef,
     unsigned best = 0xffffffffu;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         if (touched[i]) best = min(best, f2ord(ccoef[i].z));
-#pragma unroll
-    for (int o = 16; o; o >>= 1) best = min(best, __shfl_xor_sync(SKID_FULL, best, o));
+    best = __reduce_min_sync(SKID_FULL, best);
     if ((threadIdx.x & 31) == 0 && best != 0xffffffffu) atomicMin(d_floor, best);
 }
 
-// Pass 2: keep flags, zeroed first-step densities, touched reset.
-__global__ void cut_kernel(const float4 *__restrict__ ccoef, unsigned char *__restrict__ touched,
-                           const int *d_n, int cap, const unsigned *d_floor, int initial,
-                           int nocut, int *__restrict__ keep, float *__restrict__ final_rho)
+// Keep flags (smooth1.c:460-470 with the floor over the touched copies), first-step zeroed densities, touched reset; per-tile kept
+// counts.  Block 0 also accumulates the step's algorithmic field bytes.
+__global__ void __launch_bounds__(CT_THREADS)
+cut_tiles_kernel(const float4 *__restrict__ ccoef, unsigned char *__restrict__ touched,
+                 const int *d_n, const unsigned *d_floor, int initial, int nocut,
+                 int *__restrict__ keep, float *__restrict__ final_rho, int *__restrict__ blk,
+                 const int *d_nA, double *fbytes)
 {
-    int n = *d_n;
-    unsigned fl = *d_floor;
-    float fScatDens = fl == 0xffffffffu ? 0.0f : ord2f(fl);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
-        if (i >= n) { keep[i] = 0; continue; }
+    __shared__ int sh[32];
+    const int n = *d_n;
+    const unsigned fl = *d_floor;
+    const float fScatDens = fl == 0xffffffffu ? 0.0f : ord2f(fl);
+    const int base = blockIdx.x * CT_TILE + threadIdx.x * CT_ITEMS;
+    int kept = 0;
+    for (int j = 0; j < CT_ITEMS; ++j) {
+        const int i = base + j;
+        if (i >= n) break;
         float4 c = ccoef[i];
         bool t = touched[i] != 0;
-        touched[i] = 0;
+        if (t) touched[i] = 0;
         int k = 1;
         if (!nocut) {
             if (initial) {
@@ -160,52 +205,98 @@ __global__ void cut_kernel(const float4 *__restrict__ ccoef, unsigned char *__re
             }
         }
         keep[i] = k;
+        kept += k;
+    }
+    kept = block_sum(kept, sh);
+    if (threadIdx.x == 0) {
+        blk[blockIdx.x] = kept;
+        if (blockIdx.x == 0 && fbytes) {
+            fbytes[0] += 24.0 * (double)*d_nA + 20.0 * (double)n;
+            fbytes[1] += 1.0;
+        }
     }
 }
 
-// Stable compaction into the spare arrays, skipped when nothing was cut.
-__global__ void compact_copies_kernel(const int *__restrict__ keep, const int *__restrict__ pos,
-                                      const int *d_n, const int *d_n2,
-                                      const float4 *__restrict__ cpos,
-                                      const float4 *__restrict__ ccoef, float4 *__restrict__ cpos2,
-                                      float4 *__restrict__ ccoef2)
+// Stable compaction into the spare arrays: tile b starts at the sum of the
+// counts of tiles before it.  Block 0 publishes the new count in *d_n2 and
+// resets the density floor for the next step.  Nothing is written when
+// nothing was cut.
+__global__ void __launch_bounds__(CT_THREADS)
+compact_tiles_kernel(const int *__restrict__ keep, const int *__restrict__ blk, int nb,
+                     const int *d_n, int *d_n2, unsigned *d_floor,
+                     const float4 *__restrict__ cpos, const float4 *__restrict__ ccoef,
+                     float4 *__restrict__ cpos2, float4 *__restrict__ ccoef2)
 {
-    int n = *d_n;
-    if (*d_n2 == n) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    __shared__ int sh[32];
+    const int n = *d_n;
+    const int b = blockIdx.x;
+    int pre = 0, all = 0;
+    for (int k = threadIdx.x; k < nb; k += CT_THREADS) {
+        int v = blk[k];
+        all += v;
+        if (k < b) pre += v;
+    }
+    pre = block_sum(pre, sh);
+    all = block_sum(all, sh);
+    if (b == 0 && threadIdx.x == 0) {
+        *d_n2 = all;
+        *d_floor = 0xffffffffu;
+    }
+    if (all == n) return;
+    const int base = b * CT_TILE + threadIdx.x * CT_ITEMS;
+    int cnt = 0;
+    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) cnt += keep[base + j];
+    int o = pre + block_excl(cnt, sh);
+    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) {
+        const int i = base + j;
         if (!keep[i]) continue;
-        int j = pos[i];
-        cpos2[j] = cpos[i];
-        ccoef2[j] = ccoef[i];
+        cpos2[o] = cpos[i];
+        ccoef2[o] = ccoef[i];
+        ++o;
     }
 }
 
-// Copy the compacted arrays back and mark the tree dirty.  A captured graph
-// therefore always reads the primary arrays.
-__global__ void copyback_copies_kernel(const int *d_n, const int *d_n2, float4 *__restrict__ cpos,
-                                       float4 *__restrict__ ccoef,
-                                       const float4 *__restrict__ cpos2,
-                                       const float4 *__restrict__ ccoef2, int *d_dirty)
+// Copy the compacted arrays back (a captured graph always reads the primary
+// arrays); the last block to finish publishes the count and marks the tree
+// dirty, after every block has read the old count.
+__global__ void copyback_tiles_kernel(int *d_n, const int *d_n2, float4 *__restrict__ cpos,
+                                      float4 *__restrict__ ccoef,
+                                      const float4 *__restrict__ cpos2,
+                                      const float4 *__restrict__ ccoef2, int *d_dirty, int *d_done)
 {
-    int n2 = *d_n2;
-    if (n2 == *d_n) return;
+    const int n = *d_n, n2 = *d_n2;
+    if (n2 == n) return;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += gridDim.x * blockDim.x) {
         cpos[j] = cpos2[j];
         ccoef[j] = ccoef2[j];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *d_dirty = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(d_done, 1) == (int)gridDim.x - 1) {
+            *d_n = n2;
+            *d_dirty = 1;
+            *d_done = 0;
+        }
+    }
 }
 
-__global__ void prune_flag_kernel(const float4 *__restrict__ mpos, const float4 *__restrict__ mold,
-                                  const int *__restrict__ act, const int *d_nA, int cap, float3 hP,
-                                  float fCvg2, int *__restrict__ keep)
+// kdPruneInactive's test (kd.c:752-762) per active slot, in cut tiles, with
+// per-tile survivor counts.
+__global__ void __launch_bounds__(CT_THREADS)
+prune_flag_kernel(const float4 *__restrict__ mpos, const float4 *__restrict__ mold,
+                  const int *__restrict__ act, const int *d_nA, float3 hP, float fCvg2,
+                  int *__restrict__ keep, int *__restrict__ blk)
 {
-    int n = *d_nA;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
-        if (i >= n) { keep[i] = 0; continue; }
+    __shared__ int sh[32];
+    const int n = *d_nA;
+    const int base = blockIdx.x * CT_TILE + threadIdx.x * CT_ITEMS;
+    int kept = 0;
+    for (int j = 0; j < CT_ITEMS; ++j) {
+        const int i = base + j;
+        if (i >= n) break;
         int m = act[i];
         float4 r = mpos[m], o = mold[m];
-        // kd.c:752-762
         float dx = fsub(r.x, o.x), dy = fsub(r.y, o.y), dz = fsub(r.z, o.z);
         if (dx > hP.x) dx = fsub(dx, fmul(2.0f, hP.x));
         if (dx <= -hP.x) dx = fadd(dx, fmul(2.0f, hP.x));
@@ -213,42 +304,64 @@ __global__ void prune_flag_kernel(const float4 *__restrict__ mpos, const float4 
         if (dy <= -hP.y) dy = fadd(dy, fmul(2.0f, hP.y));
         if (dz > hP.z) dz = fsub(dz, fmul(2.0f, hP.z));
         if (dz <= -hP.z) dz = fadd(dz, fmul(2.0f, hP.z));
-        keep[i] = d2of(dx, dy, dz) >= fCvg2;
+        int k = d2of(dx, dy, dz) >= fCvg2;
+        keep[i] = k;
+        kept += k;
     }
+    kept = block_sum(kept, sh);
+    if (threadIdx.x == 0) blk[blockIdx.x] = kept;
 }
 
 // Survivors get rOld reset (kd.c:785-789) and the Morton key of their
-// current position at their compacted slot (slots [0, survivors) are all
-// written; only those are sorted).
-__global__ void prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ pos,
-                                     const int *d_nA, const int *__restrict__ act,
-                                     const float4 *__restrict__ mpos, float4 *__restrict__ mold,
-                                     float3 lo, float3 inv, uint64_t *__restrict__ keys,
-                                     uint32_t *__restrict__ vals)
+// current position at their compacted slot (tile b starts after the
+// survivors of the tiles before it; slots [0, survivors) are all written and
+// only those are sorted).  Block 0 publishes the survivor count in *d_nA2.
+__global__ void __launch_bounds__(CT_THREADS)
+prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ blk, int nb,
+                     const int *d_nA, int *d_nA2, const int *__restrict__ act,
+                     const float4 *__restrict__ mpos, float4 *__restrict__ mold, float3 lo,
+                     float3 inv, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
 {
-    int n = *d_nA;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    __shared__ int sh[32];
+    const int n = *d_nA;
+    const int b = blockIdx.x;
+    int pre = 0, all = 0;
+    for (int k = threadIdx.x; k < nb; k += CT_THREADS) {
+        int v = blk[k];
+        all += v;
+        if (k < b) pre += v;
+    }
+    pre = block_sum(pre, sh);
+    all = block_sum(all, sh);
+    if (b == 0 && threadIdx.x == 0) *d_nA2 = all;
+    const int base = b * CT_TILE + threadIdx.x * CT_ITEMS;
+    int cnt = 0;
+    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) cnt += keep[base + j];
+    int o = pre + block_excl(cnt, sh);
+    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) {
+        const int i = base + j;
         if (!keep[i]) continue;
         int m = act[i];
         float4 p = mpos[m];
         mold[m] = p;
-        int j = pos[i];
         // the top 32 bits of the Morton key (10 to 11 bits per axis) are
         // enough to give each warp a compact set of movers
-        keys[j] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
-        vals[j] = (uint32_t)m;
+        keys[o] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
+        vals[o] = (uint32_t)m;
+        ++o;
     }
 }
 
+// The sorted movers become the active list; block 0 publishes the count
+// (the other blocks read only *d_n2).
 __global__ void act_from_sorted(const uint32_t *__restrict__ vals, const int *d_n2,
-                                int *__restrict__ act)
+                                int *__restrict__ act, int *d_n)
 {
     int n2 = *d_n2;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += gridDim.x * blockDim.x)
         act[j] = (int)vals[j];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_n = n2;
 }
-
-__global__ void set_count_kernel(int *dst, const int *src) { *dst = *src; }
 
 float ord_to_float(unsigned u)
 {
@@ -291,33 +404,35 @@ cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rh
     copy_permute_kernel<<<grid_for(nc), 256, 0, st>>>(ss.v0.p, nc, C.cpos2.p, C.ccoef2.p, C.cpos.p, C.ccoef.p); skid::note_launch();
     if ((e = cudaMemsetAsync(C.touched.p, 0, C.cap, st))) return e;
     if ((e = cudaMemsetAsync(C.d_dirty, 0, sizeof(int), st))) return e;
+    if ((e = cudaMemsetAsync(C.d_floor, 0xff, sizeof(unsigned), st))) return e;
     *nCopies = nc;
     return cudaGetLastError();
 }
 
-cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, SortScratch &ss,
-                        cudaStream_t st)
+cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, const int *d_nA,
+                        double *d_fbytes, cudaStream_t st)
 {
-    cudaError_t e;
-    int cap = C.cap;
-    if ((e = cudaMemsetAsync(C.d_floor, 0xff, sizeof(unsigned), st))) return e;
-    int g = grid_for(cap);
-    floor_kernel<<<g, 256, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, C.d_floor); skid::note_launch();
-    cut_kernel<<<g, 256, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, cap, C.d_floor, initial ? 1 : 0, nocut ? 1 : 0, C.keep.p, final_rho); skid::note_launch();
-    if ((e = cudaGetLastError())) return e;
-    if (nocut) return cudaSuccess;
-    if ((e = scan_exclusive(C.keep.p, C.kpos.p, cap, C.d_n2, ss, st))) return e;
-    compact_copies_kernel<<<g, 256, 0, st>>>(C.keep.p, C.kpos.p, C.d_n, C.d_n2, C.cpos.p, C.ccoef.p, C.cpos2.p, C.ccoef2.p); skid::note_launch();
-    copyback_copies_kernel<<<g, 256, 0, st>>>(C.d_n, C.d_n2, C.cpos.p, C.ccoef.p, C.cpos2.p, C.ccoef2.p, C.d_dirty); skid::note_launch();
-    set_count_kernel<<<1, 1, 0, st>>>(C.d_n, C.d_n2); skid::note_launch();
+    const int nb = (C.cap + CT_TILE - 1) / CT_TILE;
+    if (C.blk.n < (size_t)nb) return cudaErrorInvalidValue;
+    floor_kernel<<<grid_for(C.cap), 256, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, C.d_floor); skid::note_launch();
+    cut_tiles_kernel<<<nb, CT_THREADS, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, C.d_floor,
+                                                initial ? 1 : 0, nocut ? 1 : 0, C.keep.p, final_rho,
+                                                C.blk.p, d_nA, d_fbytes); skid::note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e) return e;
+    if (nocut) return cudaMemsetAsync(C.d_floor, 0xff, sizeof(unsigned), st);
+    compact_tiles_kernel<<<nb, CT_THREADS, 0, st>>>(C.keep.p, C.blk.p, nb, C.d_n, C.d_n2, C.d_floor,
+                                                    C.cpos.p, C.ccoef.p, C.cpos2.p, C.ccoef2.p); skid::note_launch();
+    copyback_tiles_kernel<<<grid_for(C.cap), 256, 0, st>>>(C.d_n, C.d_n2, C.cpos.p, C.ccoef.p, C.cpos2.p,
+                                                           C.ccoef2.p, C.d_dirty, C.d_done); skid::note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,
-                        SortScratch &ss, cudaStream_t st)
+                        SortScratch &ss, cudaStream_t st, int bound)
 {
     cudaError_t e;
-    int cap = m.cap;
+    int cap = bound > 0 && bound < m.cap ? bound : m.cap;
     // sort scratch for cap keys (allocated on the first, uncaptured call)
     if ((e = dalloc(ss.k0, cap)) || (e = dalloc(ss.k1, cap)) || (e = dalloc(ss.v0, cap)) ||
         (e = dalloc(ss.v1, cap)))
@@ -326,15 +441,18 @@ cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyin
                             (float)(0.5 * (double)period.z));
     float fCvg2 = fCvg * fCvg;
     int g = grid_for(cap);
-    prune_flag_kernel<<<g, 256, 0, st>>>(m.mpos.p, m.mold.p, m.act.p, m.d_nA, cap, hP, fCvg2, m.keep.p); skid::note_launch();
-    if ((e = scan_exclusive(m.keep.p, m.kpos.p, cap, m.d_nA2, ss, st))) return e;
-    prune_scatter_kernel<<<g, 256, 0, st>>>(m.keep.p, m.kpos.p, m.d_nA, m.act.p, m.mpos.p, m.mold.p, keylo, keyinv, ss.k0.p, ss.v0.p); skid::note_launch();
+    const int nb = (cap + CT_TILE - 1) / CT_TILE;
+    if ((e = dalloc(m.blk, (size_t)nb))) return e;
+    prune_flag_kernel<<<nb, CT_THREADS, 0, st>>>(m.mpos.p, m.mold.p, m.act.p, m.d_nA, hP, fCvg2,
+                                                 m.keep.p, m.blk.p); skid::note_launch();
+    prune_scatter_kernel<<<nb, CT_THREADS, 0, st>>>(m.keep.p, m.blk.p, nb, m.d_nA, m.d_nA2, m.act.p,
+                                                    m.mpos.p, m.mold.p, keylo, keyinv, ss.k0.p,
+                                                    ss.v0.p); skid::note_launch();
     // an even number of digit passes leaves the result in (k0, v0), so a
     // captured graph replays consistently; only the surviving movers' keys
     // (the first *d_nA2 slots) are sorted
     if ((e = radix_sort(ss, cap, 32, st, m.d_nA2))) return e;
-    act_from_sorted<<<g, 256, 0, st>>>(ss.v0.p, m.d_nA2, m.act.p); skid::note_launch();
-    set_count_kernel<<<1, 1, 0, st>>>(m.d_nA, m.d_nA2); skid::note_launch();
+    act_from_sorted<<<g, 256, 0, st>>>(ss.v0.p, m.d_nA2, m.act.p, m.d_nA); skid::note_launch();
     return cudaGetLastError();
 }
 

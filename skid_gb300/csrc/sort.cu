@@ -94,7 +94,7 @@ __global__ void rs_scatter(const uint64_t *__restrict__ kin, const uint32_t *__r
     }
 }
 
-// ---- int scan (3 phase) ----
+// ---- int scan: tile sums, then each tile from the sums before it ----
 constexpr int SC_THREADS = 512;
 constexpr int SC_ITEMS = 8;
 constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
@@ -139,34 +139,24 @@ __global__ void scan_tile_sums(const int *in, int n, int *blk)
     if (threadIdx.x == 0) blk[blockIdx.x] = tot;
 }
 
-__global__ void scan_blocks(int *blk, int m, int *d_total)
+// Each block scans its tile from the sum of the tile sums before it (read
+// here, so the scan takes two launches); block 0 also writes the total.
+__global__ void scan_apply(const int *in, int *out, int n, const int *blk, int nb, int *d_total)
 {
     __shared__ int sh[32];
-    // m <= blockDim.x * 16
-    int t = threadIdx.x;
-    int vals[16];
-    int s = 0;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        int i = t * 16 + j;
-        vals[j] = i < m ? blk[i] : 0;
-        s += vals[j];
+    const int b = blockIdx.x;
+    int pre = 0, all = 0;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+        int v = blk[k];
+        all += v;
+        if (k < b) pre += v;
     }
     int tot;
-    int run = block_excl_scan(s, sh, &tot);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        int i = t * 16 + j;
-        if (i < m) blk[i] = run;
-        run += vals[j];
-    }
-    if (t == 0 && d_total) *d_total = tot;
-}
-
-__global__ void scan_apply(const int *in, int *out, int n, const int *blk)
-{
-    __shared__ int sh[32];
-    int base = blockIdx.x * SC_TILE + threadIdx.x * SC_ITEMS;
+    block_excl_scan(pre, sh, &tot);
+    pre = tot;
+    block_excl_scan(all, sh, &tot);
+    all = tot;
+    int base = b * SC_TILE + threadIdx.x * SC_ITEMS;
     int v[SC_ITEMS];
     int s = 0;
 #pragma unroll
@@ -174,13 +164,13 @@ __global__ void scan_apply(const int *in, int *out, int n, const int *blk)
         v[j] = (base + j < n) ? in[base + j] : 0;
         s += v[j];
     }
-    int tot;
-    int run = block_excl_scan(s, sh, &tot) + blk[blockIdx.x];
+    int run = block_excl_scan(s, sh, &tot) + pre;
 #pragma unroll
     for (int j = 0; j < SC_ITEMS; ++j) {
         if (base + j < n) out[base + j] = run;
         run += v[j];
     }
+    if (b == 0 && threadIdx.x == 0 && d_total) *d_total = all;
 }
 
 }  // namespace
@@ -227,8 +217,7 @@ cudaError_t scan_exclusive(const int *in, int *out, int n, int *d_total, SortScr
     cudaError_t e = dalloc(s.blk, (size_t)nb);
     if (e) return e;
     scan_tile_sums<<<nb, SC_THREADS, 0, st>>>(in, n, s.blk.p); skid::note_launch();
-    scan_blocks<<<1, 512, 0, st>>>(s.blk.p, nb, d_total); skid::note_launch();
-    scan_apply<<<nb, SC_THREADS, 0, st>>>(in, out, n, s.blk.p); skid::note_launch();
+    scan_apply<<<nb, SC_THREADS, 0, st>>>(in, out, n, s.blk.p, nb, d_total); skid::note_launch();
     return cudaGetLastError();
 }
 

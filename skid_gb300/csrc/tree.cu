@@ -71,7 +71,7 @@ __global__ void gather_sorted(const float4 *__restrict__ p, const uint32_t *__re
 __global__ void upward_kernel(const float4 *__restrict__ pos, const float *__restrict__ ball2,
                               const float4 *__restrict__ aux, int ballw, int n_host, const int *d_n,
                               int leafBase, float4 *lo, float4 *hi, float4 *blo, float4 *bhi,
-                              int *flag, const int *d_dirty)
+                              int *flag, int *d_dirty)
 {
     int leaf = blockIdx.x * blockDim.x + threadIdx.x;
     if (leaf >= leafBase) return;
@@ -115,10 +115,14 @@ __global__ void upward_kernel(const float4 *__restrict__ pos, const float *__res
     hi[node] = h;
     if (balls) { blo[node] = bl; bhi[node] = bh; }
     __threadfence();
+    if (leafBase == 1 && d_dirty) *d_dirty = 0;   // the only leaf is the root
     node >>= 1;
     while (node >= 1) {
         int old = atomicAdd(&flag[node], 1);
         if (old == 0) return;
+        // the second arrival finishes the node and clears its flag for the
+        // next refit (each node has exactly two arrivals per launch)
+        flag[node] = 0;
         __threadfence();
         float4 l0 = __ldcg(&lo[2 * node]), l1 = __ldcg(&lo[2 * node + 1]);
         float4 h0 = __ldcg(&hi[2 * node]), h1 = __ldcg(&hi[2 * node + 1]);
@@ -132,6 +136,8 @@ __global__ void upward_kernel(const float4 *__restrict__ pos, const float *__res
             bhi[node] = make_float4(fmaxf(c0.x, c1.x), fmaxf(c0.y, c1.y), fmaxf(c0.z, c1.z), 0.0f);
         }
         __threadfence();
+        // the root is finished after every leaf thread has read d_dirty
+        if (node == 1 && d_dirty) *d_dirty = 0;
         node >>= 1;
     }
 }
@@ -168,6 +174,7 @@ cudaError_t tree_build(Tree &t, const float4 *pts, int n, bool balls, SortScratc
     if ((e = dalloc(t.pos, n)) || (e = dalloc(t.perm, n)) || (e = dalloc(t.lo, nodes)) ||
         (e = dalloc(t.hi, nodes)) || (e = dalloc(t.flag, nodes)))
         return e;
+    t.flag_clear = false;
     if (balls) {
         if ((e = dalloc(t.blo, nodes)) || (e = dalloc(t.bhi, nodes))) return e;
     }
@@ -196,8 +203,12 @@ cudaError_t morton_order(const float4 *pts, int n, SortScratch &s, cudaStream_t 
 cudaError_t tree_refit(Tree &t, const float4 *pos, const float4 *aux, const int *d_n,
                        cudaStream_t st, bool ballw, int *d_dirty)
 {
-    cudaError_t e = cudaMemsetAsync(t.flag.p, 0, 2 * (size_t)t.leafBase * sizeof(int), st);
-    if (e) return e;
+    cudaError_t e = cudaSuccess;
+    // arrival flags start zero (allocation) and every launch leaves them zero
+    if (!t.flag_clear) {
+        if ((e = cudaMemsetAsync(t.flag.p, 0, 2 * (size_t)t.leafBase * sizeof(int), st))) return e;
+        t.flag_clear = true;
+    }
     int threads = 128;
     int blocks = (t.leafBase + threads - 1) / threads;
     bool nb = t.blo.n < 2 * (size_t)t.leafBase || t.bhi.n < 2 * (size_t)t.leafBase;
@@ -205,8 +216,7 @@ cudaError_t tree_refit(Tree &t, const float4 *pos, const float4 *aux, const int 
                                               t.n, d_n, t.leafBase, t.lo.p, t.hi.p,
                                               nb ? nullptr : t.blo.p, nb ? nullptr : t.bhi.p,
                                               t.flag.p, d_dirty); skid::note_launch();
-    if (d_dirty) e = cudaMemsetAsync(d_dirty, 0, sizeof(int), st);
-    return e ? e : cudaGetLastError();
+    return cudaGetLastError();
 }
 
 cudaError_t tree_shape(Tree &t, int n, bool balls)
@@ -218,6 +228,7 @@ cudaError_t tree_shape(Tree &t, int n, bool balls)
     size_t nodes = 2 * (size_t)t.leafBase;
     if ((e = dalloc(t.lo, nodes)) || (e = dalloc(t.hi, nodes)) || (e = dalloc(t.flag, nodes)))
         return e;
+    t.flag_clear = false;
     if (balls && ((e = dalloc(t.blo, nodes)) || (e = dalloc(t.bhi, nodes)))) return e;
     return cudaSuccess;
 }
