@@ -82,6 +82,7 @@ struct UnbindParams {
 
 struct UnbindScratch {
     DBuf<float4> qr, qv, slist;
+    DBuf<float4> qw;                 // large groups: (a v + aH r, softening) per member
     DBuf<long long> pot, pot_save;
     DBuf<int> qid, scnt, soff, nt, toff, cnt, grp_save;
     DBuf<uint32_t> order;
@@ -339,7 +340,7 @@ struct skid_ctx {
         dfree(parent);
         dfree(G.start); dfree(G.count); dfree(G.members); dfree(G.rec); dfree(G.sums);
         dfree(G.map); dfree(G.gtmp); dfree(G.gtmp2); dfree(G.gof); dfree(G.rec2);
-        dfree(U.qr); dfree(U.qv); dfree(U.slist); dfree(U.pot); dfree(U.qid); dfree(U.scnt);
+        dfree(U.qr); dfree(U.qv); dfree(U.qw); dfree(U.slist); dfree(U.pot); dfree(U.qid); dfree(U.scnt);
         dfree(U.soff); dfree(U.nt); dfree(U.toff); dfree(U.cnt); dfree(U.items); dfree(U.ssoft);
         dfree(unfused_acc);
         dfree(U.usoft); dfree(U.pot_save); dfree(U.grp_save); dfree(U.order); dfree(U.rec_save);

@@ -127,6 +127,17 @@ __device__ __forceinline__ float ll2f_approx(long long p)
     return p < 0 ? -f : f;
 }
 
+// int64 -> float within three roundings (relative error below 2^-22), from
+// the two 32-bit halves of |p| and one fused multiply-add: the FP32 energies
+// of large groups only.
+__device__ __forceinline__ float ll2f_fast(long long p)
+{
+    const unsigned long long a = p < 0 ? (unsigned long long)(-p) : (unsigned long long)p;
+    const float f = __fmaf_rn(__uint2float_rn((unsigned)(a >> 32)), 4294967296.0f,
+                              __uint2float_rn((unsigned)a));
+    return p < 0 ? -f : f;
+}
+
 // Fixed-point quantum of a float term (scale = 2^S, exact multiply), equal to
 // __float2ll_rn(t * scale).  Terms are non-negative: below 2^23 adding 2^23
 // rounds to the nearest integer (ties to even) in the float adder, at or above
@@ -443,6 +454,7 @@ struct RemoveArgs {
     const int *gstart, *gcount;
     int ng, nmax;
     float4 *qr, *qv;
+    float4 *qw;                     // large groups' staged a v + aH r (w: softening)
     int *qid;
     long long *pot;
     skid_group *rec;
@@ -665,6 +677,7 @@ struct BlockShared {
     double d_cm[6], d_mass;
     double part[BS / 32][7];
     float ext[BS / 32][3];      // per-warp FP32 energy max, min, error bound
+    float s_w[3];               // a vcm + aH rcm (large groups' FP32 energies)
 };
 
 // A large group, the whole block.
@@ -708,11 +721,26 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         S.s_n = n0;
         S.s_have = 0;
         S.s_go = 1;
+        for (int d = 0; d < 3; ++d)
+            S.s_w[d] = (float)((double)A.fShift * S.d_cm[3 + d] + (double)A.fCosmo * S.d_cm[d]);
     }
     __syncthreads();
     int nrem = 0;
     const bool exact = n0 <= EXACT_E_MAX;
     const double opz_d = 1.0 + (double)A.z, inv_d = 1.0 / (double)A.scale;
+    float4 *qw = A.qw + s;
+    if (!exact) {
+        // E_i = 1/2 |w_i - W|^2 - pot_i (1+z), w_i = a v_i + aH r_i fixed per
+        // member, W = a vcm + aH rcm per pass (kd.c:1392-1400 in FP32)
+        for (int i = tid; i < n0; i += BS) {
+            float4 r = qr[i], v = qv[i];
+            qw[i] = make_float4(__fmaf_rn(A.fShift, v.x, A.fCosmo * r.x),
+                                __fmaf_rn(A.fShift, v.y, A.fCosmo * r.y),
+                                __fmaf_rn(A.fShift, v.z, A.fCosmo * r.z), v.w);
+        }
+        __syncthreads();
+    }
+    const float epot = A.inv_scale * A.opz;
     for (;;) {
         const int n = S.s_n;
         const bool have = S.s_have != 0;
@@ -723,21 +751,49 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         for (int d = 0; d < 6; ++d) { dcm[d] = S.d_cm[d]; scm[d] = S.s_cm[d]; }
         ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
         float emax = -FLT_MAX, emin = FLT_MAX, dmax = 0.0f;
-        for (int i = tid; i < n; i += BS) {
-            float4 r = qr[i], v = qv[i];
-            long long p = pot[i];
-            if (have && A.subpot) {
-                p = sub_pot(A, rs, es, r, v, p);
-                pot[i] = p;
-            }
-            float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-            if (exact) {
+        if (exact) {
+            for (int i = tid; i < n; i += BS) {
+                float4 r = qr[i], v = qv[i];
+                long long p = pot[i];
+                if (have && A.subpot) {
+                    p = sub_pot(A, rs, es, r, v, p);
+                    pot[i] = p;
+                }
+                float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
                 emax = fmaxf(emax, E);
                 emin = fminf(emin, E);
                 dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
-            } else {
-                if (E > mx.v) { mx.v = E; mx.i = i; }
-                if (E < mn.v) { mn.v = E; mn.i = i; }
+            }
+        } else {
+            const float wx = S.s_w[0], wy = S.s_w[1], wz = S.s_w[2];
+            const float gms = fmul(A.G, rs.w) * A.scale;   // the removed member's G m 2^S
+            const bool sub = have && A.subpot;
+            // RB members per thread per batch, all loaded before any is used,
+            // so their memory latencies overlap
+            constexpr int RB = BS >= 1024 ? 2 : 4;
+            for (int i0 = tid; i0 < n; i0 += RB * BS) {
+                float4 r[RB], w[RB];
+                long long p[RB];
+#pragma unroll
+                for (int k = 0; k < RB; ++k) {
+                    const int i = i0 + k * BS;
+                    if (i < n) { r[k] = qr[i]; w[k] = qw[i]; p[k] = pot[i]; }
+                }
+#pragma unroll
+                for (int k = 0; k < RB; ++k) {
+                    const int i = i0 + k * BS;
+                    if (i >= n) break;
+                    if (sub) {
+                        // kdSubPot (grav.c:44-59): the term the potentials added
+                        float d2 = d2of(fsub(rs.x, r[k].x), fsub(rs.y, r[k].y), fsub(rs.z, r[k].z));
+                        p[k] -= fx(fmul(gms, pair_dir(d2, fadd(es, w[k].w), A.plummer)), 1.0f);
+                        pot[i] = p[k];
+                    }
+                    float dx = w[k].x - wx, dy = w[k].y - wy, dz = w[k].z - wz;
+                    float E = 0.5f * __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) - ll2f_fast(p[k]) * epot;
+                    if (E > mx.v) { mx.v = E; mx.i = i; }
+                    if (E < mn.v) { mn.v = E; mn.i = i; }
+                }
             }
         }
         if (exact) {
@@ -805,11 +861,18 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                         S.d_cm[d] = dcm[d];
                         S.s_cm[d] = (float)dcm[d];
                     }
+                    for (int d = 0; d < 3; ++d)
+                        S.s_w[d] = (float)((double)A.fShift * dcm[3 + d] + (double)A.fCosmo * dcm[d]);
                     float4 rl = qr[nn], vl = qv[nn];
                     int il = qid[nn], ir = qid[ib];
                     long long pl = pot[nn], pb = pot[ib];
                     qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
                     qr[nn] = r; qv[nn] = v; qid[nn] = ir; pot[nn] = pb;
+                    if (!exact) {
+                        float4 wl = qw[nn], wb = qw[ib];
+                        qw[ib] = wl;
+                        qw[nn] = wb;
+                    }
                     S.s_r = r;
                     S.s_eps = v.w;
                     S.s_have = 1;
@@ -899,7 +962,8 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
 {
     cudaError_t e;
     int ng = G.nGroup;
-    if ((e = dalloc(U.qr, nslots)) || (e = dalloc(U.qv, nslots)) || (e = dalloc(U.qid, nslots)) ||
+    if ((e = dalloc(U.qr, nslots)) || (e = dalloc(U.qv, nslots)) || (e = dalloc(U.qw, nslots)) ||
+        (e = dalloc(U.qid, nslots)) ||
         (e = dalloc(U.pot, nslots)) || (e = dalloc(U.scnt, ng)) || (e = dalloc(U.soff, ng + 1)) ||
         (e = dalloc(U.nt, ng)) || (e = dalloc(U.toff, ng + 1)) || (e = dalloc(U.cnt, 8)) ||
         (e = dalloc(U.order, ng)))
@@ -957,6 +1021,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     A.nmax = P.nmax;
     A.qr = U.qr.p;
     A.qv = U.qv.p;
+    A.qw = U.qw.p;
     A.qid = U.qid.p;
     A.pot = U.pot.p;
     A.rec = G.rec.p;
