@@ -84,12 +84,46 @@ __global__ void clique_kernel(float4 *lo, float4 *hi, int leafBase, int n, float
     }
 }
 
-__global__ void __launch_bounds__(F_WARPS * 32)
-link_kernel(TreeView t, float tau2, float3 L, float3 hL, bool per, int *par, int *work,
-            unsigned *status)
+// Lower bound of the float squared distance between any point of box a and
+// any point of box b (periodic images included): box_lb over every point of
+// a, with the slack of a's largest coordinate.
+__device__ __forceinline__ float boxbox_lb1(float alo, float ahi, float blo, float bhi, float L,
+                                            bool per)
+{
+    float d = fmaxf(fmaxf(blo - ahi, alo - bhi), 0.0f);
+    if (per) {
+        d = fminf(d, fmaxf(fmaxf(blo - (ahi + L), (alo + L) - bhi), 0.0f));
+        d = fminf(d, fmaxf(fmaxf(blo - (ahi - L), (alo - L) - bhi), 0.0f));
+    }
+    float slack = 4.8e-7f * (fmaxf(fabsf(alo), fabsf(ahi)) + (per ? L : 0.0f) +
+                             fmaxf(fabsf(blo), fabsf(bhi)));
+    return fmaxf(d - slack, 0.0f);
+}
+
+__device__ __forceinline__ float boxbox_lb(float4 alo, float4 ahi, float4 blo, float4 bhi, float3 L,
+                                           bool per)
+{
+    float dx = boxbox_lb1(alo.x, ahi.x, blo.x, bhi.x, L.x, per);
+    float dy = boxbox_lb1(alo.y, ahi.y, blo.y, bhi.y, L.y, per);
+    float dz = boxbox_lb1(alo.z, ahi.z, blo.z, bhi.z, L.z, per);
+    return (dx * dx + dy * dy + dz * dz) * (1.0f - 4e-6f);
+}
+
+// One warp per leaf of queries; each pair is linked from its lower slot, so
+// subtrees wholly below the query leaf are skipped.  The last 2^subShift
+// leaves under a node are tested one per lane against the query leaf's box;
+// at a visited leaf, only candidates above the first query slot within tau
+// of the query box are compacted and tested.  A clique node (box diagonal
+// below tau) is skipped by a lane already in its component.
+__global__ void __launch_bounds__(F_WARPS * 32, 8)
+link_kernel(TreeView t, float tau2, float3 L, float3 hL, bool per, int subShift, int *par,
+            int *work, unsigned *status)
 {
     __shared__ float4 cand[F_WARPS][SKID_LEAF];
+    __shared__ int cslot[F_WARPS][SKID_LEAF];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int rootLo = t.leafBase >> subShift;
+    const int logLeafBase = 31 - __clz(t.leafBase);
     for (;;) {
         int leaf = 0;
         if (lane == 0) leaf = atomicAdd(work, 1);
@@ -100,43 +134,75 @@ link_kernel(TreeView t, float tau2, float3 L, float3 hL, bool per, int *par, int
         bool valid = qi < t.n;
         float4 qp = t.pos[valid ? qi : base];
         float3 q = make_float3(qp.x, qp.y, qp.z);
+        const int own = t.leafBase + leaf;
+        const float4 qlo = t.lo[own], qhi = t.hi[own];
         int cp = 1;
         for (;;) {
-            float4 blo = t.lo[cp], bhi = t.hi[cp];
-            bool want = valid && box_lb(q, blo, bhi, L, per) < tau2;
-            if (want && bhi.w != 0.0f) {
-                int f = first_slot(cp, t.leafBase);
-                if (uf_find(par, qi) == uf_find(par, f)) want = false;
-            }
-            if (__any_sync(SKID_FULL, want)) {
-                if (cp < t.leafBase) { cp <<= 1; continue; }
-                int lf = cp - t.leafBase;
-                int cb = lf * SKID_LEAF;
-                int cnt = min(SKID_LEAF, t.n - cb);
-                __syncwarp();
-                if (lane < cnt) cand[w][lane] = t.pos[cb + lane];
-                __syncwarp();
-                int cx = img_class(q.x, blo.x, bhi.x, hL.x);
-                int cy = img_class(q.y, blo.y, bhi.y, hL.y);
-                int cz = img_class(q.z, blo.z, bhi.z, hL.z);
-                bool noshift = (cx == 0) & (cy == 0) & (cz == 0);
-                if (want) {
-                    for (int j = 0; j < cnt; ++j) {
-                        int sj = cb + j;
-                        if (sj <= qi) continue;
-                        float4 c = cand[w][j];
-                        float d;
-                        if (noshift) {
-                            d = d2of(fsub(q.x, c.x), fsub(q.y, c.y), fsub(q.z, c.z));
-                        } else {
-                            float d1 = d2of(img_dx(q.x, c.x, L.x, hL.x), img_dx(q.y, c.y, L.y, hL.y),
-                                            img_dx(q.z, c.z, L.z, hL.z));
-                            float d2v = d2of(img_dx(c.x, q.x, L.x, hL.x), img_dx(c.y, q.y, L.y, hL.y),
-                                             img_dx(c.z, q.z, L.z, hL.z));
-                            d = fminf(d1, d2v);
+            // the last leaf under cp (its subtree is skipped when below ours)
+            const int last = ((cp + 1) << (logLeafBase - (31 - __clz(cp)))) - 1;
+            if (last >= own) {
+                if (cp >= rootLo) {
+                    const int first = cp << subShift;
+                    bool pass = false;
+                    if (lane < (1 << subShift) && first + lane >= own &&
+                        first + lane - t.leafBase < t.nLeaf)
+                        pass = boxbox_lb(qlo, qhi, t.lo[first + lane], t.hi[first + lane], L, per) < tau2;
+                    for (unsigned lm = __ballot_sync(SKID_FULL, pass); lm; lm &= lm - 1) {
+                        const int node = first + __ffs(lm) - 1;
+                        float4 blo = t.lo[node], bhi = t.hi[node];
+                        bool want = valid && box_lb(q, blo, bhi, L, per) < tau2;
+                        if (want && bhi.w != 0.0f) {
+                            int f = first_slot(node, t.leafBase);
+                            if (uf_find(par, qi) == uf_find(par, f)) want = false;
                         }
-                        if (d < tau2) uf_union(par, qi, sj, status);
+                        if (!__any_sync(SKID_FULL, want)) continue;
+                        const int cb = (node - t.leafBase) * SKID_LEAF;
+                        const int cnt = min(SKID_LEAF, t.n - cb);
+                        bool rel = false;
+                        float4 c4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        if (lane < cnt && cb + lane > base) {
+                            c4 = t.pos[cb + lane];
+                            rel = box_lb(make_float3(c4.x, c4.y, c4.z), qlo, qhi, L, per) < tau2;
+                        }
+                        const unsigned R = __ballot_sync(SKID_FULL, rel);
+                        const int nR = __popc(R);
+                        __syncwarp();
+                        if (rel) {
+                            const int k = __popc(R & ((1u << lane) - 1u));
+                            cand[w][k] = c4;
+                            cslot[w][k] = cb + lane;
+                        }
+                        __syncwarp();
+                        if (!want) continue;
+                        int cx = img_class(q.x, blo.x, bhi.x, hL.x);
+                        int cy = img_class(q.y, blo.y, bhi.y, hL.y);
+                        int cz = img_class(q.z, blo.z, bhi.z, hL.z);
+                        bool noshift = (cx == 0) & (cy == 0) & (cz == 0);
+                        for (int j = 0; j < nR; ++j) {
+                            const int sj = cslot[w][j];
+                            if (sj <= qi) continue;
+                            float4 c = cand[w][j];
+                            float d;
+                            if (noshift) {
+                                d = d2of(fsub(q.x, c.x), fsub(q.y, c.y), fsub(q.z, c.z));
+                            } else {
+                                float d1 = d2of(img_dx(q.x, c.x, L.x, hL.x), img_dx(q.y, c.y, L.y, hL.y),
+                                                img_dx(q.z, c.z, L.z, hL.z));
+                                float d2v = d2of(img_dx(c.x, q.x, L.x, hL.x), img_dx(c.y, q.y, L.y, hL.y),
+                                                 img_dx(c.z, q.z, L.z, hL.z));
+                                d = fminf(d1, d2v);
+                            }
+                            if (d < tau2) uf_union(par, qi, sj, status);
+                        }
                     }
+                } else {
+                    float4 blo = t.lo[cp], bhi = t.hi[cp];
+                    bool want = valid && box_lb(q, blo, bhi, L, per) < tau2;
+                    if (want && bhi.w != 0.0f) {
+                        int f = first_slot(cp, t.leafBase);
+                        if (uf_find(par, qi) == uf_find(par, f)) want = false;
+                    }
+                    if (__any_sync(SKID_FULL, want)) { cp <<= 1; continue; }
                 }
             }
             cp = next_node(cp);
@@ -205,7 +271,10 @@ cudaError_t fof_run(Tree &t, const float4 *pts, int np, const int *mio, int nior
     int blocks = num_sms() * perSM;
     int need = (t.nLeaf + F_WARPS - 1) / F_WARPS;
     if (blocks > need) blocks = need;
-    link_kernel<<<blocks, F_WARPS * 32, 0, st>>>(t.view(), tau2, L, hL, per, par.p, d_work, d_status); skid::note_launch();
+    int subShift = 0;
+    while (subShift < 5 && (2 << subShift) <= t.leafBase) ++subShift;
+    link_kernel<<<blocks, F_WARPS * 32, 0, st>>>(t.view(), tau2, L, hL, per, subShift, par.p, d_work,
+                                                 d_status); skid::note_launch();
     fill_int<<<grid_for(np), 256, 0, st>>>(minio.p, 0x7fffffff, np); skid::note_launch();
     root_min_iorder<<<grid_for(np), 256, 0, st>>>(par.p, np, t.perm.p, mio, minio.p); skid::note_launch();
     int *fl = flag.p, *rank = flag.p + niorder;
