@@ -114,12 +114,14 @@ __device__ __forceinline__ void h_term(float *gi, float *grad, int K, float H, c
 
 __global__ void __launch_bounds__(A_WARPS * 32)
 density_adjoint_walk(TreeView t, const float *__restrict__ ball2, const float *__restrict__ wsort,
-                     float3 L, float3 hL, bool per, float *__restrict__ grad, int *work,
-                     unsigned *status)
+                     float3 L, float3 hL, bool per, int subShift, float *__restrict__ grad,
+                     int *work, unsigned *status)
 {
     __shared__ float4 cpos[A_WARPS][SKID_LEAF];
     __shared__ float4 caux[A_WARPS][SKID_LEAF];   // fBall2, 1/h^2, 1/(pi h^5), w
+    __shared__ int cslot[A_WARPS][SKID_LEAF];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int rootLo = t.leafBase >> subShift;
     for (;;) {
         int leaf = 0;
         if (lane == 0) leaf = atomicAdd(work, 1);
@@ -132,38 +134,59 @@ density_adjoint_walk(TreeView t, const float *__restrict__ ball2, const float *_
         float3 q = make_float3(qp.x, qp.y, qp.z);
         Ball bi = ball_of(ball2[valid ? qi : base]);
         float wi = wsort[valid ? qi : base], mi = qp.w;
+        // the query leaf's box (its points) and largest ball
+        const float4 qlo = t.lo[t.leafBase + leaf], qhi = t.hi[t.leafBase + leaf];
         float g[3] = {0.0f, 0.0f, 0.0f};
         float H = 0.0f;
         int K = -1;
         float kx = 0.0f, ky = 0.0f, kz = 0.0f;
         int cp = 1;
         for (;;) {
-            float4 blo = t.lo[cp], bhi = t.hi[cp];
-            float bd = box_lb(q, blo, bhi, L, per);
-            bool want = bd < fmaxf(bi.b, blo.w);
-            if (__any_sync(SKID_FULL, want)) {
-                if (cp < t.leafBase) { cp <<= 1; continue; }
-                int lf = cp - t.leafBase;
-                if (lf < t.nLeaf) {
-                    int cb = lf * SKID_LEAF;
-                    int cnt = min(SKID_LEAF, t.n - cb);
-                    __syncwarp();
+            if (cp >= rootLo) {
+                // the subtree's leaves one per lane against the query box, then
+                // each passing leaf in order; at a leaf only candidates whose
+                // distance to the query box is below max(their ball, the
+                // largest query ball) can enter either half
+                const int first = cp << subShift;
+                bool pass = false;
+                if (lane < (1 << subShift) && first + lane - t.leafBase < t.nLeaf) {
+                    float4 bl = t.lo[first + lane];
+                    pass = boxbox_lb(qlo, qhi, bl, t.hi[first + lane], L, per) < fmaxf(qlo.w, bl.w);
+                }
+                for (unsigned lm = __ballot_sync(SKID_FULL, pass); lm; lm &= lm - 1) {
+                    const int node = first + __ffs(lm) - 1;
+                    float4 blo = t.lo[node], bhi = t.hi[node];
+                    bool want = box_lb(q, blo, bhi, L, per) < fmaxf(bi.b, blo.w);
+                    if (!__any_sync(SKID_FULL, want)) continue;
+                    const int cb = (node - t.leafBase) * SKID_LEAF;
+                    const int cnt = min(SKID_LEAF, t.n - cb);
+                    bool rel = false;
+                    float4 c4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    float b = 0.0f;
                     if (lane < cnt) {
-                        float b = ball2[cb + lane];
+                        c4 = t.pos[cb + lane];
+                        b = ball2[cb + lane];
+                        rel = box_lb(make_float3(c4.x, c4.y, c4.z), qlo, qhi, L, per) < fmaxf(b, qlo.w);
+                    }
+                    const unsigned R = __ballot_sync(SKID_FULL, rel);
+                    const int nR = __popc(R);
+                    __syncwarp();
+                    if (rel) {
+                        const int k = __popc(R & ((1u << lane) - 1u));
                         float ih2 = 4.0f / b;
-                        cpos[w][lane] = t.pos[cb + lane];
-                        caux[w][lane] = make_float4(b, ih2, INV_PI * ih2 * ih2 * sqrtf(ih2),
-                                                    wsort[cb + lane]);
+                        cpos[w][k] = c4;
+                        caux[w][k] = make_float4(b, ih2, INV_PI * ih2 * ih2 * sqrtf(ih2), wsort[cb + lane]);
+                        cslot[w][k] = cb + lane;
                     }
                     __syncwarp();
+                    if (!want) continue;
                     int cx = img_class(q.x, blo.x, bhi.x, hL.x);
                     int cy = img_class(q.y, blo.y, bhi.y, hL.y);
                     int cz = img_class(q.z, blo.z, bhi.z, hL.z);
-                    bool mixed = (cx == 2) | (cy == 2) | (cz == 2);
-                    bool slow = __any_sync(SKID_FULL, mixed);
+                    bool slow = (cx == 2) | (cy == 2) | (cz == 2);
                     float sx = img_shift(q.x, cx, L.x), sy = img_shift(q.y, cy, L.y),
                           sz = img_shift(q.z, cz, L.z);
-                    for (int j = 0; j < cnt; ++j) {
+                    for (int j = 0; j < nR; ++j) {
                         float4 cj = cpos[w][j];
                         float4 aj = caux[w][j];
                         // (ax, ay, az): x_i - x_j in i's frame; (bx, by, bz): in j's frame
@@ -191,13 +214,18 @@ density_adjoint_walk(TreeView t, const float *__restrict__ ball2, const float *_
                             add3(g, P * bi.c5 * kern_F(q2), ax, ay, az);
                             H += P * bi.c4 * kern_g(q2);
                         }
-                        if (dik == bi.b && cb + j != qi) {
-                            K = cb + j;
+                        const int sj = cslot[w][j];
+                        if (dik == bi.b && sj != qi) {
+                            K = sj;
                             kx = ax; ky = ay; kz = az;
                         }
                         if (dki < aj.x) add3(g, P * aj.z * kern_F(dki * aj.y), bx, by, bz);
                     }
                 }
+            } else {
+                float4 blo = t.lo[cp], bhi = t.hi[cp];
+                bool want = box_lb(q, blo, bhi, L, per) < fmaxf(bi.b, blo.w);
+                if (__any_sync(SKID_FULL, want)) { cp <<= 1; continue; }
             }
             cp = next_node(cp);
             if (cp == 1) break;
@@ -491,8 +519,10 @@ cudaError_t density_adjoint(const Tree &t, const float *ball2_sorted, const int 
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, density_adjoint_walk, A_WARPS * 32, 0);
         int blocks = num_sms() * (perSM > 0 ? perSM : 1);
         if (blocks > need) blocks = need;
+        int subShift = 0;
+        while (subShift < 5 && (2 << subShift) <= t.leafBase) ++subShift;
         density_adjoint_walk<<<blocks, A_WARPS * 32, 0, st>>>(t.view(), ball2_sorted, A.w.p, L, hL, per,
-                                                             A.g.p, d_work, d_status); note_launch();
+                                                             subShift, A.g.p, d_work, d_status); note_launch();
     } else {
         if (!A.lists) {
             A.cap = k + 16;

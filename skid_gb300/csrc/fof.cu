@@ -84,31 +84,6 @@ __global__ void clique_kernel(float4 *lo, float4 *hi, int leafBase, int n, float
     }
 }
 
-// Lower bound of the float squared distance between any point of box a and
-// any point of box b (periodic images included): box_lb over every point of
-// a, with the slack of a's largest coordinate.
-__device__ __forceinline__ float boxbox_lb1(float alo, float ahi, float blo, float bhi, float L,
-                                            bool per)
-{
-    float d = fmaxf(fmaxf(blo - ahi, alo - bhi), 0.0f);
-    if (per) {
-        d = fminf(d, fmaxf(fmaxf(blo - (ahi + L), (alo + L) - bhi), 0.0f));
-        d = fminf(d, fmaxf(fmaxf(blo - (ahi - L), (alo - L) - bhi), 0.0f));
-    }
-    float slack = 4.8e-7f * (fmaxf(fabsf(alo), fabsf(ahi)) + (per ? L : 0.0f) +
-                             fmaxf(fabsf(blo), fabsf(bhi)));
-    return fmaxf(d - slack, 0.0f);
-}
-
-__device__ __forceinline__ float boxbox_lb(float4 alo, float4 ahi, float4 blo, float4 bhi, float3 L,
-                                           bool per)
-{
-    float dx = boxbox_lb1(alo.x, ahi.x, blo.x, bhi.x, L.x, per);
-    float dy = boxbox_lb1(alo.y, ahi.y, blo.y, bhi.y, L.y, per);
-    float dz = boxbox_lb1(alo.z, ahi.z, blo.z, bhi.z, L.z, per);
-    return (dx * dx + dy * dy + dz * dz) * (1.0f - 4e-6f);
-}
-
 // One warp per leaf of queries; each pair is linked from its lower slot, so
 // subtrees wholly below the query leaf are skipped.  The last 2^subShift
 // leaves under a node are tested one per lane against the query leaf's box;

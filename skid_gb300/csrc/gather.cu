@@ -57,31 +57,6 @@ __device__ __forceinline__ float shifted(float x, int s, float L)
     return s == 0 ? x : (s < 0 ? fsub(x, L) : fadd(x, L));
 }
 
-// Lower bound of the float squared distance between any point of box a
-// (any periodic image) and any point of box b: the box_lb bound taken over
-// every point of a, with the slack of a's largest coordinate.
-__device__ __forceinline__ float boxbox_lb1(float alo, float ahi, float blo, float bhi, float L,
-                                            bool per)
-{
-    float d = fmaxf(fmaxf(blo - ahi, alo - bhi), 0.0f);
-    if (per) {
-        d = fminf(d, fmaxf(fmaxf(blo - (ahi + L), (alo + L) - bhi), 0.0f));
-        d = fminf(d, fmaxf(fmaxf(blo - (ahi - L), (alo - L) - bhi), 0.0f));
-    }
-    float slack = 4.8e-7f * (fmaxf(fabsf(alo), fabsf(ahi)) + (per ? L : 0.0f) +
-                             fmaxf(fabsf(blo), fabsf(bhi)));
-    return fmaxf(d - slack, 0.0f);
-}
-
-__device__ __forceinline__ float boxbox_lb(float4 alo, float4 ahi, float4 blo, float4 bhi, float3 L,
-                                           bool per)
-{
-    float dx = boxbox_lb1(alo.x, ahi.x, blo.x, bhi.x, L.x, per);
-    float dy = boxbox_lb1(alo.y, ahi.y, blo.y, bhi.y, L.y, per);
-    float dz = boxbox_lb1(alo.z, ahi.z, blo.z, bhi.z, L.z, per);
-    return (dx * dx + dy * dy + dz * dz) * (1.0f - 4e-6f);
-}
-
 // One warp per leaf of queries.  The walk descends a node while some lane's
 // ball reaches its box or some ball below may hold the lane (box distance
 // below max(b_i, max ball2 below)); the last 2^subShift leaves of a subtree
