@@ -368,10 +368,13 @@ __global__ void scatter_grad(const int *__restrict__ sidx, const float *__restri
 constexpr int PA_TILE = 128;
 
 // psi(r, e) as kdCellPot evaluates it (grav.h:11-31) and psi'(r)/r.
+// Beyond the softening (r >= 2h, certain once d2 clears (2h)^2 by the margin
+// below) and for Plummer softening, psi comes from the hardware reciprocal
+// square root (2 ulp).
 __device__ __forceinline__ void pair_psi(float d2, float twoh, int plummer, float &psi, float &gr)
 {
-    if (plummer) {
-        float t = 1.0f / sqrtf(d2 + 0.25f * twoh * twoh);
+    if (plummer || d2 >= twoh * twoh * 1.000001f) {
+        float t = rsqrtf(plummer ? d2 + 0.25f * twoh * twoh : d2);
         psi = t;
         gr = -t * t * t;
         return;
@@ -418,74 +421,105 @@ struct PotAdjArgs {
     float *grad;                // 3n by iOrder (zeroed) or null
 };
 
-__global__ void __launch_bounds__(PA_TILE) potential_adjoint_kernel(PotAdjArgs a)
+// One (selection slot, row tile) per block iteration: PA_TILE / 2 threads,
+// each with rows t and t + PA_TILE / 2, over every column tile of the group.
+constexpr int PA_THREADS = PA_TILE / 2;
+
+struct PaRow {
+    float3 r;
+    float e, m;
+    int io;
+    bool v;
+    float phi, phic, gx, gy, gz;   // Kahan-compensated sum_j m_j psi_ij; sum_j m_j psi'/r (x_i - x_j)
+};
+
+__device__ __forceinline__ void pa_row_init(PaRow &w, const PotAdjArgs &a, int s, int n, int i,
+                                            const float *rel)
+{
+    w.v = i < n;
+    w.io = w.v ? a.members[s + i] : 0;
+    float4 p = a.pos4[w.io];
+    w.m = p.w;
+    w.e = a.vel4[w.io].w;
+    w.r = make_float3(wrap_rel(fsub(p.x, rel[0]), a.hP.x), wrap_rel(fsub(p.y, rel[1]), a.hP.y),
+                      wrap_rel(fsub(p.z, rel[2]), a.hP.z));
+    w.phi = w.phic = w.gx = w.gy = w.gz = 0.0f;
+}
+
+__device__ __forceinline__ void pa_row_add(PaRow &w, float4 rj, float ej, int plummer)
+{
+    float dx = w.r.x - rj.x, dy = w.r.y - rj.y, dz = w.r.z - rj.z;
+    float psi, gr;
+    pair_psi(dx * dx + dy * dy + dz * dz, w.e + ej, plummer, psi, gr);
+    float y = rj.w * psi - w.phic;
+    float tt = w.phi + y;
+    w.phic = (tt - w.phi) - y;
+    w.phi = tt;
+    float c = rj.w * gr;
+    w.gx += c * dx;
+    w.gy += c * dy;
+    w.gz += c * dz;
+}
+
+__global__ void __launch_bounds__(PA_THREADS) potential_adjoint_kernel(PotAdjArgs a)
 {
     __shared__ float4 sr[PA_TILE];
     __shared__ float ss[PA_TILE];
-    __shared__ double red[PA_TILE / 32];
-    int tid = threadIdx.x;
+    __shared__ double red[PA_THREADS / 32];
+    const int tid = threadIdx.x;
     for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
         int2 item = a.items[it];
         int slot = item.x;
         int g = a.gsel[slot];
         int s = a.gstart[g], n = a.gcount[g];
         const float *rel = a.rec[g].rel;
-        int i = item.y * PA_TILE + tid;
-        bool valid = i < n;
-        int io = valid ? a.members[s + i] : 0;
-        float4 p = a.pos4[io];
-        float ei = a.vel4[io].w;
-        float3 ri = make_float3(wrap_rel(fsub(p.x, rel[0]), a.hP.x), wrap_rel(fsub(p.y, rel[1]), a.hP.y),
-                                wrap_rel(fsub(p.z, rel[2]), a.hP.z));
-        float phi = 0.0f, phic = 0.0f;
-        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+        const int i0 = item.y * PA_TILE + tid, i1 = i0 + PA_THREADS;
+        PaRow r0, r1;
+        pa_row_init(r0, a, s, n, i0, rel);
+        pa_row_init(r1, a, s, n, i1, rel);
         for (int jb = 0; jb < n; jb += PA_TILE) {
             __syncthreads();
-            int j = jb + tid;
-            if (j < n) {
-                int jo = a.members[s + j];
-                float4 q = a.pos4[jo];
-                sr[tid] = make_float4(wrap_rel(fsub(q.x, rel[0]), a.hP.x), wrap_rel(fsub(q.y, rel[1]), a.hP.y),
-                                      wrap_rel(fsub(q.z, rel[2]), a.hP.z), q.w);
-                ss[tid] = a.vel4[jo].w;
+            for (int c = tid; c < PA_TILE; c += PA_THREADS) {
+                int j = jb + c;
+                if (j < n) {
+                    int jo = a.members[s + j];
+                    float4 q = a.pos4[jo];
+                    sr[c] = make_float4(wrap_rel(fsub(q.x, rel[0]), a.hP.x), wrap_rel(fsub(q.y, rel[1]), a.hP.y),
+                                        wrap_rel(fsub(q.z, rel[2]), a.hP.z), q.w);
+                    ss[c] = a.vel4[jo].w;
+                }
             }
             __syncthreads();
-            int cnt = min(PA_TILE, n - jb);
-            if (valid) {
-                for (int k = 0; k < cnt; ++k) {
-                    if (jb + k == i) continue;
-                    float4 rj = sr[k];
-                    float dx = ri.x - rj.x, dy = ri.y - rj.y, dz = ri.z - rj.z;
-                    float psi, gr;
-                    pair_psi(dx * dx + dy * dy + dz * dz, ei + ss[k], a.plummer, psi, gr);
-                    // Kahan-compensated phi_i / (G) = sum_j m_j psi_ij
-                    float y = rj.w * psi - phic;
-                    float tt = phi + y;
-                    phic = (tt - phi) - y;
-                    phi = tt;
-                    float c = rj.w * gr;
-                    gx += c * dx;
-                    gy += c * dy;
-                    gz += c * dz;
-                }
+            const int cnt = min(PA_TILE, n - jb);
+            for (int k = 0; k < cnt; ++k) {
+                const float4 rj = sr[k];
+                const float ej = ss[k];
+                if (r0.v && jb + k != i0) pa_row_add(r0, rj, ej, a.plummer);
+                if (r1.v && jb + k != i1) pa_row_add(r1, rj, ej, a.plummer);
             }
         }
         // E contribution -1/2 G m_i phi_i, summed over the tile in FP64
-        double e = valid ? -0.5 * (double)a.G * (double)p.w * (double)phi : 0.0;
+        double e = (r0.v ? -0.5 * (double)a.G * (double)r0.m * (double)r0.phi : 0.0) +
+                   (r1.v ? -0.5 * (double)a.G * (double)r1.m * (double)r1.phi : 0.0);
         for (int o = 16; o; o >>= 1) e += __shfl_xor_sync(SKID_FULL, e, o);
         if ((tid & 31) == 0) red[tid >> 5] = e;
         __syncthreads();
         if (tid == 0) {
             double t = 0.0;
-            for (int k = 0; k < PA_TILE / 32; ++k) t += red[k];
+            for (int k = 0; k < PA_THREADS / 32; ++k) t += red[k];
             atomicAdd(a.E + slot, t);
         }
-        if (valid && a.grad) {
-            float c = -a.G * p.w * a.v[slot];
-            float *o = a.grad + 3 * (size_t)io;
-            o[0] = c * gx;
-            o[1] = c * gy;
-            o[2] = c * gz;
+        if (a.grad) {
+            const PaRow *rows[2] = {&r0, &r1};
+            for (int q = 0; q < 2; ++q) {
+                const PaRow &w = *rows[q];
+                if (!w.v) continue;
+                float c = -a.G * w.m * a.v[slot];
+                float *o = a.grad + 3 * (size_t)w.io;
+                o[0] = c * w.gx;
+                o[1] = c * w.gy;
+                o[2] = c * w.gz;
+            }
         }
     }
 }
@@ -590,8 +624,8 @@ cudaError_t potential_adjoint(const GroupState &G, const float4 *pos4, const flo
     a.plummer = plummer;
     a.E = A.E.p;
     a.grad = want_grad ? A.out.p : nullptr;
-    int blocks = (int)(ni < (size_t)num_sms() * 16 ? ni : (size_t)num_sms() * 16);
-    potential_adjoint_kernel<<<blocks, PA_TILE, 0, st>>>(a); note_launch();
+    int blocks = (int)(ni < (size_t)num_sms() * 32 ? ni : (size_t)num_sms() * 32);
+    potential_adjoint_kernel<<<blocks, PA_THREADS, 0, st>>>(a); note_launch();
     return cudaGetLastError();
 }
 
