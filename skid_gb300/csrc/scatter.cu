@@ -122,9 +122,18 @@ __global__ void copy_permute_kernel(const uint32_t *__restrict__ perm, int n,
 
 // ---- the cut, in tiles of CT_TILE slots: keep flags and per-tile counts,
 // then each tile compacts itself from the counts before it ----
+// A tile is CT_TILE slots for one block; warp w owns the CT_ITEMS x 32
+// consecutive slots from w * CT_WSPAN, read 32 at a time (coalesced), with
+// its in-tile offsets from ballots.
 constexpr int CT_THREADS = 256;
 constexpr int CT_ITEMS = 16;
 constexpr int CT_TILE = CT_THREADS * CT_ITEMS;   // matches the blk sizing (4096)
+constexpr int CT_WSPAN = CT_ITEMS * 32;
+
+__device__ __forceinline__ int ct_slot(int tile, int r)
+{
+    return tile * CT_TILE + (threadIdx.x >> 5) * CT_WSPAN + r * 32 + (threadIdx.x & 31);
+}
 
 // Sum over the block (every thread gets it).
 __device__ __forceinline__ int block_sum(int v, int *sh)
@@ -140,23 +149,17 @@ __device__ __forceinline__ int block_sum(int v, int *sh)
     return t;
 }
 
-// Exclusive prefix over the block's threads in thread order.
-__device__ __forceinline__ int block_excl(int v, int *sh)
+// Exclusive prefix of per-warp counts in warp order (every thread gets its
+// warp's).
+__device__ __forceinline__ int warp_offset(int wc, int *sh)
 {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(SKID_FULL, x, o);
-        if (lane >= o) x += y;
-    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     __syncthreads();
-    if (lane == 31) sh[w] = x;
+    if (lane == 0) sh[w] = wc;
     __syncthreads();
     int before = 0;
     for (int k = 0; k < w; ++k) before += sh[k];
-    (void)nw;
-    return before + x - v;
+    return before;
 }
 
 // The density floor over touched copies (smooth1.c:460-461).
@@ -184,10 +187,9 @@ cut_tiles_kernel(const float4 *__restrict__ ccoef, unsigned char *__restrict__ t
     const int n = *d_n;
     const unsigned fl = *d_floor;
     const float fScatDens = fl == 0xffffffffu ? 0.0f : ord2f(fl);
-    const int base = blockIdx.x * CT_TILE + threadIdx.x * CT_ITEMS;
     int kept = 0;
     for (int j = 0; j < CT_ITEMS; ++j) {
-        const int i = base + j;
+        const int i = ct_slot(blockIdx.x, j);
         if (i >= n) break;
         float4 c = ccoef[i];
         bool t = touched[i] != 0;
@@ -243,16 +245,25 @@ compact_tiles_kernel(const int *__restrict__ keep, const int *__restrict__ blk, 
         *d_floor = 0xffffffffu;
     }
     if (all == n) return;
-    const int base = b * CT_TILE + threadIdx.x * CT_ITEMS;
-    int cnt = 0;
-    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) cnt += keep[base + j];
-    int o = pre + block_excl(cnt, sh);
-    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) {
-        const int i = base + j;
-        if (!keep[i]) continue;
-        cpos2[o] = cpos[i];
-        ccoef2[o] = ccoef[i];
-        ++o;
+    const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+    unsigned m[CT_ITEMS];
+    int wc = 0;
+#pragma unroll
+    for (int j = 0; j < CT_ITEMS; ++j) {
+        const int i = ct_slot(b, j);
+        m[j] = __ballot_sync(SKID_FULL, i < n && keep[i]);
+        wc += __popc(m[j]);
+    }
+    int o = pre + warp_offset(wc, sh);
+#pragma unroll
+    for (int j = 0; j < CT_ITEMS; ++j) {
+        const int i = ct_slot(b, j);
+        if ((m[j] >> (threadIdx.x & 31)) & 1u) {
+            const int d = o + __popc(m[j] & lt);
+            cpos2[d] = cpos[i];
+            ccoef2[d] = ccoef[i];
+        }
+        o += __popc(m[j]);
     }
 }
 
@@ -290,10 +301,9 @@ prune_flag_kernel(const float4 *__restrict__ mpos, const float4 *__restrict__ mo
 {
     __shared__ int sh[32];
     const int n = *d_nA;
-    const int base = blockIdx.x * CT_TILE + threadIdx.x * CT_ITEMS;
     int kept = 0;
     for (int j = 0; j < CT_ITEMS; ++j) {
-        const int i = base + j;
+        const int i = ct_slot(blockIdx.x, j);
         if (i >= n) break;
         int m = act[i];
         float4 r = mpos[m], o = mold[m];
@@ -334,21 +344,30 @@ prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ blk, 
     pre = block_sum(pre, sh);
     all = block_sum(all, sh);
     if (b == 0 && threadIdx.x == 0) *d_nA2 = all;
-    const int base = b * CT_TILE + threadIdx.x * CT_ITEMS;
-    int cnt = 0;
-    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) cnt += keep[base + j];
-    int o = pre + block_excl(cnt, sh);
-    for (int j = 0; j < CT_ITEMS && base + j < n; ++j) {
-        const int i = base + j;
-        if (!keep[i]) continue;
-        int m = act[i];
-        float4 p = mpos[m];
-        mold[m] = p;
-        // the top 32 bits of the Morton key (10 to 11 bits per axis) are
-        // enough to give each warp a compact set of movers
-        keys[o] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
-        vals[o] = (uint32_t)m;
-        ++o;
+    const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+    unsigned msk[CT_ITEMS];
+    int wc = 0;
+#pragma unroll
+    for (int j = 0; j < CT_ITEMS; ++j) {
+        const int i = ct_slot(b, j);
+        msk[j] = __ballot_sync(SKID_FULL, i < n && keep[i]);
+        wc += __popc(msk[j]);
+    }
+    int o = pre + warp_offset(wc, sh);
+#pragma unroll
+    for (int j = 0; j < CT_ITEMS; ++j) {
+        const int i = ct_slot(b, j);
+        if ((msk[j] >> (threadIdx.x & 31)) & 1u) {
+            const int d = o + __popc(msk[j] & lt);
+            int m = act[i];
+            float4 p = mpos[m];
+            mold[m] = p;
+            // the top 32 bits of the Morton key (10 to 11 bits per axis) are
+            // enough to give each warp a compact set of movers
+            keys[d] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
+            vals[d] = (uint32_t)m;
+        }
+        o += __popc(msk[j]);
     }
 }
 
