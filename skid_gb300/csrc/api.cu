@@ -280,7 +280,7 @@ FieldArgs skid_ctx::field_args(float fStep, bool initial, float *acc_out)
 
 // One move pass: field + move, cut, refit.  Stream-ordered, no host sync.
 // `slot` picks the event pair that times this step's field kernel.
-int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int G)
+int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int G, bool compact)
 {
     skid_ctx *ctx = this;
     FieldArgs a = field_args(fStep, initial, nullptr);
@@ -301,7 +301,7 @@ int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int 
         CK(field_move(a, nMove, st));
     }
     CK(cudaEventRecordWithFlags(fev[2 * slot + 1], st, evflags));
-    CK(scatter_cut(C, initial, nocut, rho_final.p, M.d_nA, d_fbytes, st));
+    CK(scatter_cut(C, initial, nocut, rho_final.p, M.d_nA, d_fbytes, compact, st));
     CK(tree_refit(ctree, C.cpos.p, nullptr, C.d_n, st, true, C.d_dirty));
     return 0;
 }
@@ -690,7 +690,7 @@ int skid_move_step(skid_ctx *ctx, float fStep, int bInitial, int bNoCut, int *nS
         if (rc) return rc;
     }
     int live = 0;
-    if (int rc = ctx->read_int(ctx->C.d_n, &live)) return rc;
+    if (int rc = ctx->read_int(ctx->C.d_n2, &live)) return rc;
     if (ran) ctx->collect_field_times(1);
     float ms = ctx->timer_stop();
     if (ctx->stage >= STAGE_FOF) ctx->tim.micro_ms += ms;
@@ -736,7 +736,8 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
         if (!ctx->iter_eager_done) {
             // the first iteration runs eagerly; it sizes every scratch buffer
             for (int i = 0; i < PRUNE_STEPS; ++i)
-                if (int rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G)) return rc;
+                if (int rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G, i == PRUNE_STEPS - 1))
+                    return rc;
             CK(mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st));
             ctx->iter_eager_done = true;
             ran = true;
@@ -748,8 +749,10 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             set_capturing(true);
             int rc = 0;
+            // the cut copies are compacted (and the tree refit) once, at the
+            // iteration's last step
             for (int i = 0; i < PRUNE_STEPS && !rc; ++i)
-                rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G);
+                rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G, i == PRUNE_STEPS - 1);
             const int bound = ctx->slot_bound(G);
             if (!rc && mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st, bound))
                 rc = SKID_ECUDA;
@@ -783,7 +786,7 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
     }
     int vals[2];
     CK(cudaMemcpyAsync(&vals[0], ctx->M.d_nA, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&vals[1], ctx->C.d_n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&vals[1], ctx->C.d_n2, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (int rc = ctx->sync_check()) return rc;
     ctx->collect_field_times(PRUNE_STEPS);
     ctx->tim.moving_ms += ctx->timer_stop();

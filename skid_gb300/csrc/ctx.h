@@ -233,7 +233,7 @@ struct skid_ctx {
         if (S > 60) S = 60;
         return ldexpf(1.0f, S);
     }
-    int enqueue_step(float fStep, bool initial, bool nocut, int slot, int G);
+    int enqueue_step(float fStep, bool initial, bool nocut, int slot, int G, bool compact = true);
     // Crossovers measured on GB300 with the 2^21-particle workload: per-step
     // move-field time is lowest with 32 movers per warp above ~600k active
     // movers, 16 down to ~400k, 8 down to ~50k, 4 down to ~25k, one below.

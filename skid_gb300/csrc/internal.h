@@ -136,7 +136,7 @@ struct CopyState {
     DBuf<unsigned> mask;            // build-time image masks
     DBuf<int> cnt, off;             // build-time copy counts / offsets
     int *d_n = nullptr;             // live copies (device)
-    int *d_n2 = nullptr;
+    int *d_n2 = nullptr;            // live copies after the last cut
     unsigned *d_floor = nullptr;    // ordered-uint min density (fScatDens)
     int *d_dirty = nullptr;         // copies changed since the last refit
     int *d_done = nullptr;          // finished write-back blocks (zero between steps)
@@ -196,8 +196,10 @@ cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rh
                          int ns, float3 L, float3 boxlo, float3 boxhi, bool periodic,
                          CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st);
 // After a move pass: density floor, cut, stable compaction, counts.
+// compact = false defers the compaction: cut copies stay marked in their
+// slots (empty ball, density -inf) and only the live count is published.
 cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, const int *d_nA,
-                        double *d_fbytes, cudaStream_t st);
+                        double *d_fbytes, bool compact, cudaStream_t st);
 // Prune converged movers, then re-sort the active ones by Morton key.
 // bound: active movers at most (the sort and tiles are sized for it).
 cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,

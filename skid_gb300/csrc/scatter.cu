@@ -178,10 +178,10 @@ __global__ void floor_kernel(const float4 *__restrict__ ccoef,
 // Keep flags (smooth1.c:460-470 with the floor over the touched copies), first-step zeroed densities, touched reset; per-tile kept
 // counts.  Block 0 also accumulates the step's algorithmic field bytes.
 __global__ void __launch_bounds__(CT_THREADS)
-cut_tiles_kernel(const float4 *__restrict__ ccoef, unsigned char *__restrict__ touched,
-                 const int *d_n, const unsigned *d_floor, int initial, int nocut,
-                 int *__restrict__ keep, float *__restrict__ final_rho, int *__restrict__ blk,
-                 const int *d_nA, double *fbytes)
+cut_tiles_kernel(float4 *__restrict__ cpos, float4 *__restrict__ ccoef,
+                 unsigned char *__restrict__ touched, const int *d_n, const unsigned *d_floor,
+                 int initial, int nocut, int *__restrict__ keep, float *__restrict__ final_rho,
+                 int *__restrict__ blk, const int *d_nA, double *fbytes)
 {
     __shared__ int sh[32];
     const int n = *d_n;
@@ -205,6 +205,13 @@ cut_tiles_kernel(const float4 *__restrict__ ccoef, unsigned char *__restrict__ t
             } else {
                 k = c.z >= fScatDens;
             }
+            // a copy cut now stays in its slot until the next compaction: an
+            // empty ball (no mover is inside it) and density -inf (never
+            // kept again)
+            if (!k && c.z != -INFINITY) {
+                cpos[i].w = 0.0f;
+                ccoef[i].z = -INFINITY;
+            }
         }
         keep[i] = k;
         kept += k;
@@ -220,12 +227,13 @@ cut_tiles_kernel(const float4 *__restrict__ ccoef, unsigned char *__restrict__ t
 }
 
 // Stable compaction into the spare arrays: tile b starts at the sum of the
-// counts of tiles before it.  Block 0 publishes the new count in *d_n2 and
+// counts of tiles before it.  Block 0 publishes the live count in *d_n2 and
 // resets the density floor for the next step.  Nothing is written when
-// nothing was cut.
+// nothing was cut, or when compaction is deferred (compact = 0, one block:
+// the cut copies stay marked in their slots).
 __global__ void __launch_bounds__(CT_THREADS)
 compact_tiles_kernel(const int *__restrict__ keep, const int *__restrict__ blk, int nb,
-                     const int *d_n, int *d_n2, unsigned *d_floor,
+                     const int *d_n, int *d_n2, unsigned *d_floor, int compact,
                      const float4 *__restrict__ cpos, const float4 *__restrict__ ccoef,
                      float4 *__restrict__ cpos2, float4 *__restrict__ ccoef2)
 {
@@ -244,7 +252,7 @@ compact_tiles_kernel(const int *__restrict__ keep, const int *__restrict__ blk, 
         *d_n2 = all;
         *d_floor = 0xffffffffu;
     }
-    if (all == n) return;
+    if (!compact || all == n) return;
     const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
     unsigned m[CT_ITEMS];
     int wc = 0;
@@ -424,24 +432,30 @@ cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rh
     if ((e = cudaMemsetAsync(C.touched.p, 0, C.cap, st))) return e;
     if ((e = cudaMemsetAsync(C.d_dirty, 0, sizeof(int), st))) return e;
     if ((e = cudaMemsetAsync(C.d_floor, 0xff, sizeof(unsigned), st))) return e;
+    if ((e = cudaMemcpyAsync(C.d_n2, C.d_n, sizeof(int), cudaMemcpyDeviceToDevice, st))) return e;
     *nCopies = nc;
     return cudaGetLastError();
 }
 
 cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, const int *d_nA,
-                        double *d_fbytes, cudaStream_t st)
+                        double *d_fbytes, bool compact, cudaStream_t st)
 {
     const int nb = (C.cap + CT_TILE - 1) / CT_TILE;
     if (C.blk.n < (size_t)nb) return cudaErrorInvalidValue;
     floor_kernel<<<grid_for(C.cap), 256, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, C.d_floor); skid::note_launch();
-    cut_tiles_kernel<<<nb, CT_THREADS, 0, st>>>(C.ccoef.p, C.touched.p, C.d_n, C.d_floor,
+    cut_tiles_kernel<<<nb, CT_THREADS, 0, st>>>(C.cpos.p, C.ccoef.p, C.touched.p, C.d_n, C.d_floor,
                                                 initial ? 1 : 0, nocut ? 1 : 0, C.keep.p, final_rho,
                                                 C.blk.p, d_nA, d_fbytes); skid::note_launch();
     cudaError_t e = cudaGetLastError();
     if (e) return e;
-    if (nocut) return cudaMemsetAsync(C.d_floor, 0xff, sizeof(unsigned), st);
-    compact_tiles_kernel<<<nb, CT_THREADS, 0, st>>>(C.keep.p, C.blk.p, nb, C.d_n, C.d_n2, C.d_floor,
-                                                    C.cpos.p, C.ccoef.p, C.cpos2.p, C.ccoef2.p); skid::note_launch();
+    if (nocut) {
+        if ((e = cudaMemsetAsync(C.d_floor, 0xff, sizeof(unsigned), st))) return e;
+        return cudaMemcpyAsync(C.d_n2, C.d_n, sizeof(int), cudaMemcpyDeviceToDevice, st);
+    }
+    compact_tiles_kernel<<<compact ? nb : 1, CT_THREADS, 0, st>>>(C.keep.p, C.blk.p, nb, C.d_n, C.d_n2,
+                                                                  C.d_floor, compact ? 1 : 0, C.cpos.p,
+                                                                  C.ccoef.p, C.cpos2.p, C.ccoef2.p); skid::note_launch();
+    if (!compact) return cudaGetLastError();
     copyback_tiles_kernel<<<grid_for(C.cap), 256, 0, st>>>(C.d_n, C.d_n2, C.cpos.p, C.ccoef.p, C.cpos2.p,
                                                            C.ccoef2.p, C.d_dirty, C.d_done); skid::note_launch();
     return cudaGetLastError();
