@@ -274,6 +274,8 @@ FieldArgs skid_ctx::field_args(float fStep, bool initial, float *acc_out)
     a.d_work = d_scal + SC_WORK;
     a.d_status = d_status;
     a.stats = field_stats_on ? d_fstats : nullptr;
+    a.part_acc = split_acc.p;
+    a.part_cnt = split_cnt.p;
     a.G = movers_per_warp();
     return a;
 }
@@ -339,6 +341,8 @@ static int field_probe(skid_ctx *ctx, int nm, const float *mpos)
     a.d_nA = act.p + nm;
     a.G = ctx->opt_G ? ctx->opt_G : 32;   // a forced movers-per-warp applies here too
     a.stats = nullptr;
+    a.part_acc = nullptr;   // a probe walks each position in one warp
+    a.part_cnt = nullptr;
     a.touched = ctx->probe_touched();
     if (!a.touched) return ctx->fail(SKID_ENOMEM);
     CK(field_move(a, nm, st));

@@ -207,6 +207,8 @@ struct skid_ctx {
     skid::DBuf<float4> probe_p4;
     skid::DBuf<int> probe_i, probe_i2;
     skid::DBuf<unsigned char> probe_t;
+    skid::DBuf<float> split_acc;     // field parts of split movers
+    skid::DBuf<int> split_cnt;       // parts finished per split mover (zero between steps)
 
     skid_timings tim{};
     long long gather_launches = 0, kernel_launches = 0;
@@ -318,6 +320,13 @@ struct skid_ctx {
         if (dalloc(M.mpos, m) || dalloc(M.mold, m) || dalloc(M.mio, m) || dalloc(M.act, m) ||
             dalloc(M.act2, m) || dalloc(M.keep, m) || dalloc(M.kpos, m))
             return -1;
+        if (!split_cnt.p) {
+            // split one-mover-per-warp steps: partial fields and part counters
+            if (dalloc(split_acc, 3 * (size_t)skid::FIELD_SPLIT_CAP) ||
+                dalloc(split_cnt, skid::FIELD_SPLIT_CAP))
+                return -1;
+            if (cudaMemsetAsync(split_cnt.p, 0, skid::FIELD_SPLIT_CAP * sizeof(int), st)) return -1;
+        }
         M.cap = (int)m;
         return 0;
     }
@@ -348,7 +357,7 @@ struct skid_ctx {
         dfree(ss.k0); dfree(ss.k1); dfree(ss.v0); dfree(ss.v1); dfree(ss.hist); dfree(ss.blk);
         dfree(ss.box);
         dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);
-        dfree(probe_t); dfree(knn_heap);
+        dfree(probe_t); dfree(knn_heap); dfree(split_acc); dfree(split_cnt);
         dfree(adj.win); dfree(adj.w); dfree(adj.g); dfree(adj.out); dfree(adj.nbr); dfree(adj.ncnt);
         dfree(adj.items); dfree(adj.gsel); dfree(adj.v); dfree(adj.E);
         std::lock_guard<std::recursive_mutex> lk(skid::device_mutex());

@@ -36,6 +36,9 @@ constexpr int G_WARPS = 4;
 #define SKID_FIELD_MINB 12
 #endif
 constexpr int FIELD_UNROLL = SKID_FIELD_UNROLL;
+// Warps a split one-mover-per-warp step aims for (at most FIELD_SPLIT_CAP).
+constexpr int FIELD_SPLIT_ITEMS = 8192;
+static_assert(FIELD_SPLIT_ITEMS <= FIELD_SPLIT_CAP, "split buffers too small");
 
 __device__ __forceinline__ float w_m4(float r2)
 {
@@ -184,7 +187,15 @@ field_kernel(FieldArgs a)
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nA = *a.d_nA;
     const int nC = *a.d_nC;
-    const int nItems = (nA + G - 1) / G;
+    // One mover per warp and few movers: each mover's walk is split over S
+    // warps (about FIELD_SPLIT_ITEMS warps in all); all walk the inner nodes,
+    // and of each 32 leaves under a node, part p takes every S-th from p.
+    int S = 1;
+    if (G == 1 && a.part_acc && a.logLeafBase >= 5) {
+        const int t = FIELD_SPLIT_ITEMS / (nA > 0 ? nA : 1);
+        S = t >= 16 ? 16 : t >= 8 ? 8 : t >= 4 ? 4 : t >= 2 ? 2 : 1;
+    }
+    const int nItems = G == 1 ? nA * S : (nA + G - 1) / G;
     const int sub = lane % L;
     unsigned long long st_nodes = 0, st_leaves = 0, st_tests = 0, st_hits = 0;
     for (;;) {
@@ -192,6 +203,11 @@ field_kernel(FieldArgs a)
         if (lane == 0) item = atomicAdd(a.d_work, 1);
         item = __shfl_sync(SKID_FULL, item, 0);
         if (item >= nItems) break;
+        int part = 0;
+        if (G == 1) {
+            part = item % S;
+            item /= S;
+        }
         int slot = item * G + lane / L;
         bool valid = slot < nA;
         int mi = a.act[valid ? slot : item * G];
@@ -243,7 +259,10 @@ field_kernel(FieldArgs a)
                 if (!__any_sync(SKID_FULL, want)) continue;
                 if (node < a.leafBase) {
                     const int cf = node << 5;
-                    const unsigned cm = __ballot_sync(SKID_FULL, reach(cf + lane));
+                    unsigned cm = __ballot_sync(SKID_FULL, reach(cf + lane));
+                    if (G == 1 && S > 1 && cf >= a.leafBase)
+                        cm &= (S == 2 ? 0x55555555u : S == 4 ? 0x11111111u
+                               : S == 8 ? 0x01010101u : 0x00010001u) << part;
                     if (cm) {
                         ++sp;
                         if (lane == sp) { smask = cm; sfirst = cf; }
@@ -323,6 +342,24 @@ field_kernel(FieldArgs a)
             az = fadd(az, __shfl_xor_sync(SKID_FULL, az, o));
         }
         if (!valid || sub != 0) continue;
+        if (G == 1 && S > 1) {
+            // the last of the mover's S parts sums them in part order
+            float *pa = a.part_acc + 3 * ((size_t)slot * S + part);
+            pa[0] = ax;
+            pa[1] = ay;
+            pa[2] = az;
+            __threadfence();
+            if (atomicAdd(&a.part_cnt[slot], 1) != S - 1) continue;
+            __threadfence();
+            ax = ay = az = 0.0f;
+            for (int p = 0; p < S; ++p) {
+                const float *q = a.part_acc + 3 * ((size_t)slot * S + p);
+                ax = fadd(ax, __ldcg(q));
+                ay = fadd(ay, __ldcg(q + 1));
+                az = fadd(az, __ldcg(q + 2));
+            }
+            a.part_cnt[slot] = 0;
+        }
         if (a.acc_out) {
             a.acc_out[3 * (size_t)slot + 0] = ax;
             a.acc_out[3 * (size_t)slot + 1] = ay;

@@ -165,6 +165,10 @@ struct MoverState {
     int *d_nA2 = nullptr;
 };
 
+// Capacity of the split-mover buffers: one-mover-per-warp steps split each
+// mover's walk over S warps while (active movers x S) fits in it.
+constexpr int FIELD_SPLIT_CAP = 16384;
+
 struct FieldArgs {
     const float4 *cpos, *ccoef;      // copies
     const float4 *blo, *bhi;         // ball boxes of the copy tree
@@ -182,6 +186,8 @@ struct FieldArgs {
     int *d_work;
     unsigned *d_status;
     unsigned long long *stats;       // optional: nodes, leaves, candidate tests, hits
+    float *part_acc;                 // split movers' partial fields [FIELD_SPLIT_CAP x 3] (or null)
+    int *part_cnt;                   // parts finished per mover [FIELD_SPLIT_CAP], zero between steps
     int G;                           // movers per warp: 32, 8 or 1
 };
 cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st);
