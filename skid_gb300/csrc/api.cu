@@ -443,6 +443,54 @@ int skid_destroy(skid_ctx *ctx)
     return 0;
 }
 
+// Total |mass| (FP64) and smallest softening of the input, in a fixed order:
+// block b reduces its contiguous chunk (thread-strided, then a fixed tree),
+// and one warp adds the block partials in block order.
+constexpr int MS_BLOCKS = 128;
+constexpr int MS_THREADS = 256;
+
+__global__ void __launch_bounds__(MS_THREADS)
+mass_soft_partials(const float *__restrict__ mass, const float *__restrict__ soft, int n,
+                   double *__restrict__ out)
+{
+    __shared__ double sm[MS_THREADS];
+    __shared__ float ss[MS_THREADS];
+    const int chunk = (n + MS_BLOCKS - 1) / MS_BLOCKS;
+    const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+    double m = 0.0;
+    float e = FLT_MAX;
+    for (int i = b0 + threadIdx.x; i < b1; i += MS_THREADS) {
+        m += fabs((double)mass[i]);
+        e = fminf(e, soft[i]);
+    }
+    sm[threadIdx.x] = m;
+    ss[threadIdx.x] = e;
+    __syncthreads();
+    for (int h = MS_THREADS / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            sm[threadIdx.x] += sm[threadIdx.x + h];
+            ss[threadIdx.x] = fminf(ss[threadIdx.x], ss[threadIdx.x + h]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[2 + 2 * blockIdx.x] = sm[0];
+        out[3 + 2 * blockIdx.x] = (double)ss[0];
+    }
+}
+
+__global__ void mass_soft_total(double *out)
+{
+    if (threadIdx.x != 0) return;
+    double m = 0.0, e = (double)FLT_MAX;
+    for (int b = 0; b < MS_BLOCKS; ++b) {
+        m += out[2 + 2 * b];
+        e = fmin(e, out[3 + 2 * b]);
+    }
+    out[0] = m;
+    out[1] = e;
+}
+
 int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double time,
                        const float *pos, const float *vel, const float *mass, const float *soft,
                        const float *temp)
@@ -461,15 +509,12 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
     ctx->time = time;
     ctx->inType = (nDark ? 1 : 0) | (nGas ? 2 : 0) | (nStar ? 4 : 0);
     ctx->mass_total = 0.0;
-    ctx->soft_min = n > 0 ? soft[0] : 0.0f;
-    for (int i = 0; i < n; ++i) {
-        ctx->mass_total += fabs((double)mass[i]);
-        if (soft[i] < ctx->soft_min) ctx->soft_min = soft[i];
-    }
-    ctx->soft_min_input = ctx->soft_min;
+    ctx->soft_min = ctx->soft_min_input = 0.0f;
+    ctx->ms_pending = false;
     ctx->soft_changed = false;
     if (ctx->alloc_particles(n)) return ctx->fail(SKID_ENOMEM);
     if (n == 0) { ctx->stage = STAGE_LOADED; return 0; }
+    if (dalloc(ctx->ms_dev, 2 * (size_t)MS_BLOCKS + 2)) return ctx->fail(SKID_ENOMEM);
     // staging: raw host arrays -> device, then pack to float4 records
     float *d_raw = ctx->raw.p;
     size_t n3 = 3 * (size_t)n;
@@ -486,6 +531,11 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
                                                      temp ? d_raw + 2 * n3 + 2 * (size_t)n : nullptr,
                                                      n, ctx->pos4.p, ctx->vel4.p, ctx->temp.p); skid::note_launch();
     CK(cudaGetLastError());
+    // total |mass| and smallest softening for the potential scale (fixed order)
+    mass_soft_partials<<<MS_BLOCKS, MS_THREADS, 0, ctx->st>>>(d_raw + 2 * n3, d_raw + 2 * n3 + n, n,
+                                                             ctx->ms_dev.p); skid::note_launch();
+    mass_soft_total<<<1, 32, 0, ctx->st>>>(ctx->ms_dev.p); skid::note_launch();
+    ctx->ms_pending = true;
     fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho.p, 0.0f, n); skid::note_launch();
     fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho_final.p, 0.0f, n); skid::note_launch();
     fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->ball2.p, -1.0f, n); skid::note_launch();
@@ -506,6 +556,7 @@ int skid_restart(skid_ctx *ctx)
     if (!ctx) return SKID_EINVAL;
     if (ctx->stage < STAGE_LOADED) return ctx->fail(SKID_ESTATE);
     int n = ctx->n;
+    if (ctx->ensure_mass_soft()) return ctx->fail(SKID_ECUDA);
     double mt = ctx->mass_total;
     float sm = ctx->soft_min_input;
     ctx->reset_pipeline();

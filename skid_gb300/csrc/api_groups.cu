@@ -236,6 +236,7 @@ int skid_unbind(skid_ctx *ctx, int iSoftType, float fScoop, int bGasAndDark, int
     P.plummer = iSoftType == SKID_SOFT_PLUMMER;
     P.subpot = ctx->inType == 1 || ctx->inType == 4;   // kd.c:1441
     P.nounbind = bNoUnbind != 0;
+    if (ctx->ensure_mass_soft()) return ctx->fail(SKID_ECUDA);
     P.scale = ctx->pot_scale(G);
     P.n = ctx->n;
     P.tw = ctx->opt_unbind_tw;

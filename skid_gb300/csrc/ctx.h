@@ -147,9 +147,11 @@ struct skid_ctx {
 
     int n = 0, nGas = 0, nDark = 0, nStar = 0, inType = 0;
     double time = 0.0;
-    double mass_total = 0.0;        // host-side, for the fixed-point potential scale
+    double mass_total = 0.0;        // host copy, for the fixed-point potential scale
     float soft_min = 0.0f;
     float soft_min_input = 0.0f;
+    skid::DBuf<double> ms_dev;      // device reduction: [MS_BLOCKS partials x 2], then (sum |m|, min soft)
+    bool ms_pending = false;        // mass_total / soft_min_input not yet read back
     int stage = skid::STAGE_NONE;
     int last_error = 0;
     int last_cuda = 0;              // first CUDA runtime error seen
@@ -226,6 +228,22 @@ struct skid_ctx {
     // 2^S such that |potential| * 2^S < 2^62: the spline potential is at most
     // 1.4 * 2/(eps_i+eps_j) <= 1.4/eps_min per unit G*mass (grav.h:11-31), and
     // the Plummer form at most 2/(eps_i+eps_j).
+    // The input's total |mass| and smallest softening, reduced on the device
+    // when the particles were set; read back here the first time they are
+    // needed.
+    int ensure_mass_soft()
+    {
+        if (!ms_pending) return 0;
+        double v[2];
+        if (cudaMemcpyAsync(v, ms_dev.p, sizeof(v), cudaMemcpyDeviceToHost, st) ||
+            cudaStreamSynchronize(st))
+            return -1;
+        mass_total = v[0];
+        soft_min_input = (float)v[1];
+        if (!soft_changed) soft_min = soft_min_input;
+        ms_pending = false;
+        return 0;
+    }
     float pot_scale(float G) const
     {
         if (!(soft_min > 0.0f)) return ldexpf(1.0f, 40);
@@ -357,7 +375,7 @@ struct skid_ctx {
         dfree(ss.k0); dfree(ss.k1); dfree(ss.v0); dfree(ss.v1); dfree(ss.hist); dfree(ss.blk);
         dfree(ss.box);
         dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);
-        dfree(probe_t); dfree(knn_heap); dfree(split_acc); dfree(split_cnt);
+        dfree(probe_t); dfree(knn_heap); dfree(split_acc); dfree(split_cnt); dfree(ms_dev);
         dfree(adj.win); dfree(adj.w); dfree(adj.g); dfree(adj.out); dfree(adj.nbr); dfree(adj.ncnt);
         dfree(adj.items); dfree(adj.gsel); dfree(adj.v); dfree(adj.E);
         std::lock_guard<std::recursive_mutex> lk(skid::device_mutex());
