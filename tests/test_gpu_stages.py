@@ -112,3 +112,50 @@ def test_schedules_and_unfused_forms_agree(gpu_ready, name):
         assert np.array_equal(grp, base_grp), setting
         for f in ("nMembers", "fMass", "rCenter", "rBound", "vcm", "fRadius"):
             assert np.array_equal(rec[f], base_rec[f]), (setting, f)
+
+
+def test_unbind_large_groups_fp32_path(gpu_ready):
+    """Groups above 1024 members take the FP32-energy removal path (staged
+    a v + aH r per member, member loads batched per thread): unbind-only mode
+    on three groups of 1790-4075 members, with a twelfth of their members
+    sped up fourfold so that each loses 89-203 of them one by one, must
+    unbind exactly the particles the oracle's FP64 loop unbinds."""
+    from skid_gb300 import gpu, tipsy
+    from skid_gb300.options import Options
+    from tests.helpers import small_snapshot
+    snap = small_snapshot(n=12288, n_halo=3, seed=41, r200=0.1, frac=0.85, dex=0.5)
+    opts = Options.parse(["-tau", "0.012", "-s", "64", "-m", "16", "-p", "1", "-O", "0.3",
+                          "-Lambda", "0.7", "-H", "5.28444", "-z", "0.5"])
+    r1 = oracle.run(snap, opts, stop_after=1)
+    cnt = np.bincount(r1["grp"])
+    big = np.nonzero(cnt[1:] > 1024)[0] + 1
+    assert len(big) >= 2
+    rng = np.random.default_rng(5)
+    vel = snap.vel.copy()
+    for g in big:
+        m = np.nonzero(r1["grp"] == g)[0]
+        vel[rng.choice(m, len(m) // 12, replace=False)] *= 4.0
+    snap = tipsy.Snapshot(snap.time, snap.n_gas, snap.n_dark, snap.n_star, snap.pos, vel,
+                          snap.mass, snap.soft, snap.temp)
+    centers = np.concatenate([r1["groups"]["rCenter"][1:], r1["groups"]["vcm"][1:]], axis=1)
+    r2 = oracle.run_unbind(snap, opts, r1["grp"], centers, stop_after=2)
+    ng = r1["nGroupFoF"]
+    cen = np.zeros(ng + 1, gpu.GROUP_DTYPE)
+    cen["rCenter"] = r1["groups"]["rCenter"]
+    cen["vcm"] = r1["groups"]["vcm"]
+    removed = cnt[big] - np.bincount(r2["grp"], minlength=len(cnt))[big]
+    assert removed.min() >= 50
+    for bs in (256, 512, 1024):
+        with _ctx(opts) as ctx:
+            ctx.set_option("unbind_warp_max", 1024)
+            ctx.set_option("unbind_block", bs)
+            ctx.set_particles(snap)
+            ctx.set_groups(r1["grp"], cen)
+            nu = ctx.unbind(opts.iSoftType, opts.fScoop, opts.bGasAndDark, opts.bNoUnbind,
+                            opts.nMaxMembers, opts.G, opts.z, opts.a_shift, opts.a_hubble)
+            grp, rec = ctx.get_groups(ng)
+        assert nu == r2["nUnbound"], bs
+        assert np.array_equal(grp, r2["grp"]), bs
+        og = r2["groups"]
+        np.testing.assert_allclose(rec["fMass"][big], og["fMass"][big], rtol=1e-6)
+        np.testing.assert_allclose(rec["vcm"][big], og["vcm"][big], rtol=1e-4, atol=1e-6)
