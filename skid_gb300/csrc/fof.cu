@@ -10,7 +10,8 @@
 // moved particles of a group sit inside a ball of radius ~fCvg.  Here a node
 // whose box diagonal is below tau is a clique; a pre-pass links each clique
 // to its children's first points, and a query skips a clique subtree as soon
-// as it is already in that clique's component.
+// as it is already in that clique's component.  Each pair is linked from its
+// lower slot, so a query skips every subtree below its own leaf.
 #include <cfloat>
 
 #include "ctx.h"

@@ -188,7 +188,7 @@ struct FieldArgs {
     unsigned long long *stats;       // optional: nodes, leaves, candidate tests, hits
     float *part_acc;                 // split movers' partial fields [FIELD_SPLIT_CAP x 3] (or null)
     int *part_cnt;                   // parts finished per mover [FIELD_SPLIT_CAP], zero between steps
-    int G;                           // movers per warp: 32, 8 or 1
+    int G;                           // movers per warp: 32, 16, 8, 4 or 1
 };
 cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st);
 // The move step alone, from a field computed with fStep = 0 into acc.

@@ -9,7 +9,10 @@
 // lane l at i*32+l, so every heap access is bank-conflict free).  The warp
 // first scans its own leaf, then climbs to the root visiting each sibling
 // subtree depth-first (the search order of smBallSearch, smooth1.c:89-127),
-// entering a node when any lane's heap bound reaches its box.
+// entering a node when any lane's heap bound reaches its box.  The last five
+// levels of a subtree are tested one leaf per lane against the query leaf's
+// box and the warp's largest bound; at a leaf only candidates within that
+// bound of the query box are compacted and tested.
 #include <cfloat>
 
 #include <mutex>

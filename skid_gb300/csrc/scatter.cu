@@ -13,8 +13,10 @@
 //  - cut: the heuristic scatterer removal (smooth1.c:460-470, 387-405,
 //    509-513).  fScatDens = min density over copies that reached an active
 //    mover; copies below it go.  On the first step (dark-only input or -fic)
-//    copies that reached no mover count as density 0.  Survivors are
-//    compacted in slot order, which keeps them Morton-sorted.
+//    copies that reached no mover count as density 0.  A copy cut is marked
+//    dead in its slot (empty ball, density -inf); the survivors are compacted
+//    in slot order, which keeps them Morton-sorted, at the last step of each
+//    outer iteration (and after every single step), followed by a refit.
 //  - prune: kdPruneInactive (kd.c:735-793), stable, then the active movers
 //    are re-sorted by the Morton key of their current positions so that each
 //    warp's movers stay close together as the active set thins out.
