@@ -207,6 +207,9 @@ cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rh
 cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, const int *d_nA,
                         double *d_fbytes, bool compact, cudaStream_t st);
 // Prune converged movers, then re-sort the active ones by Morton key.
+// Re-sort the active movers by the Morton key of their current positions.
+cudaError_t mover_resort(MoverState &m, float3 keylo, float3 keyinv, SortScratch &ss,
+                         cudaStream_t st, int bound);
 // bound: active movers at most (the sort and tiles are sized for it).
 cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,
                         SortScratch &ss, cudaStream_t st, int bound = -1);

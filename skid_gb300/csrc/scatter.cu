@@ -381,6 +381,21 @@ prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ blk, 
     }
 }
 
+// Keys (top 32 bits of the Morton key) of the active movers' current
+// positions, in active order.
+__global__ void resort_keys_kernel(const int *__restrict__ act, const int *d_nA,
+                                   const float4 *__restrict__ mpos, float3 lo, float3 inv,
+                                   uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
+{
+    const int n = *d_nA;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int m = act[i];
+        float4 p = mpos[m];
+        keys[i] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
+        vals[i] = (uint32_t)m;
+    }
+}
+
 // The sorted movers become the active list; block 0 publishes the count
 // (the other blocks read only *d_n2).
 __global__ void act_from_sorted(const uint32_t *__restrict__ vals, const int *d_n2,
@@ -460,6 +475,23 @@ cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho
     if (!compact) return cudaGetLastError();
     copyback_tiles_kernel<<<grid_for(C.cap), 256, 0, st>>>(C.d_n, C.d_n2, C.cpos.p, C.ccoef.p, C.cpos2.p,
                                                            C.ccoef2.p, C.d_dirty, C.d_done); skid::note_launch();
+    return cudaGetLastError();
+}
+
+// Global re-sort of the active movers between prunes by the Morton key of
+// their current positions (the same 32-bit key as the prune's; equal keys keep
+// their order).  A mover that crosses a high-level Morton boundary has to move
+// far in the order, which only a global sort does: a tile-local sort, or a
+// coarser key, loses most of the gain.
+cudaError_t mover_resort(MoverState &m, float3 keylo, float3 keyinv, SortScratch &ss,
+                         cudaStream_t st, int bound)
+{
+    cudaError_t e;
+    int cap = bound > 0 && bound < m.cap ? bound : m.cap;
+    resort_keys_kernel<<<grid_for(cap), 256, 0, st>>>(m.act.p, m.d_nA, m.mpos.p, keylo, keyinv,
+                                                      ss.k0.p, ss.v0.p); skid::note_launch();
+    if ((e = radix_sort(ss, cap, 32, st, m.d_nA))) return e;
+    act_from_sorted<<<grid_for(cap), 256, 0, st>>>(ss.v0.p, m.d_nA, m.act.p, m.d_nA); skid::note_launch();
     return cudaGetLastError();
 }
 
