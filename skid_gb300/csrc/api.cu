@@ -305,9 +305,9 @@ int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int 
     CK(cudaEventRecordWithFlags(fev[2 * slot + 1], st, evflags));
     CK(scatter_cut(C, initial, nocut, rho_final.p, M.d_nA, d_fbytes, compact, st));
     CK(tree_refit(ctree, C.cpos.p, nullptr, C.d_n, st, true, C.d_dirty));
-    // between prunes, re-sort the active movers while they are many (8 or
+    // between prunes, re-sort the active movers while they are many (16 or
     // more per warp): the warps' boxes stay tight as the movers drift
-    if (!compact && G >= 8) CK(mover_resort(M, mkey_lo, mkey_inv, ss, st, slot_bound(G)));
+    if (!compact && G >= 16) CK(mover_resort(M, mkey_lo, mkey_inv, ss, st, slot_bound(G)));
     return 0;
 }
 
