@@ -91,6 +91,20 @@ def field_traffic():
         return None
 
 
+def field_issue():
+    """Instruction-issue utilisation of one full-activity field_kernel launch
+    (fraction of peak issue slots, ncu `issue active`), from the committed
+    full-section capture, or None.  The kernel is issue-bound; this is its
+    roofline in the resource that binds it."""
+    import re
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            m = re.search(r"\|\s*issue active\s*\|\s*([0-9.]+)\s*%", f.read())
+        return float(m.group(1)) / 100.0 if m else None
+    except OSError:
+        return None
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -431,7 +445,10 @@ def run_gpu(args):
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": field_traffic(),
                      "launches": f_launch, "avg_launch_ms": f_ms / max(f_launch, 1),
-                     "algorithmic_bytes_per_launch": f_bytes / max(f_launch, 1)},
+                     "algorithmic_bytes_per_launch": f_bytes / max(f_launch, 1),
+                     "issue": {"frac": field_issue(), "unit": "fraction of peak issue slots",
+                               "source": "ncu issue active, one launch at full activity "
+                                         "(profiles/field_kernel_skid_config1_2e21.md)"}},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
