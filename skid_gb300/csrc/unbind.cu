@@ -305,12 +305,15 @@ struct PotRow {
     bool v;       // a member of the tile
 };
 
-// The terms of row a and column j (tr: on a, tc: on j).
+// The terms of row a and column j (tr: on a, tc: on j).  far is at or above
+// every pair's (2h)^2 (1 + 1e-6) in the tile pair (infinite for Plummer
+// softening): beyond it pair_dir is 1/r, taken without forming the pair's
+// softening, with the same value.
 __device__ __forceinline__ void pot_pair(const PotRow &a, float4 rj, float ej, int plummer,
-                                         long long &tr, long long &tc)
+                                         float far, long long &tr, long long &tc)
 {
     float d2 = d2of(fsub(a.r.x, rj.x), fsub(a.r.y, rj.y), fsub(a.r.z, rj.z));
-    float dir = pair_dir(d2, fadd(a.e, ej), plummer);
+    float dir = d2 >= far ? rsqrtf(d2) : pair_dir(d2, fadd(a.e, ej), plummer);
     tr = fx(fmul(rj.w, dir), 1.0f);
     // equal masses (all-dark runs): both ends get the same term
     tc = rj.w == a.r.w ? tr : fx(fmul(a.r.w, dir), 1.0f);
@@ -328,6 +331,7 @@ pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_h
     __shared__ float4 sr[T];
     __shared__ float ss[T];
     __shared__ long long acc_w[NW][T];
+    __shared__ float emax_w[2][NW];
     const int t = threadIdx.x, wid = t >> 5;
     const int nitems = nitems_host >= 0 ? nitems_host : *d_nitems;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
@@ -359,6 +363,30 @@ pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_h
             for (int k = 0; k < NW; ++k) acc_w[k][c] = 0;
         }
         __syncthreads();
+        // the far bound: (largest row softening + largest column softening)^2,
+        // above every pair's own (softenings are non-negative, so their bit
+        // patterns order like their values)
+        float far = INFINITY;
+        if (!plummer) {
+            float er = fmaxf(ra.v ? ra.e : 0.0f, rb.v ? rb.e : 0.0f), ec = 0.0f;
+            for (int c = t; c < nj; c += POT_THREADS) ec = fmaxf(ec, ss[c]);
+            er = __uint_as_float(__reduce_max_sync(SKID_FULL, __float_as_uint(er)));
+            ec = __uint_as_float(__reduce_max_sync(SKID_FULL, __float_as_uint(ec)));
+            if ((t & 31) == 0) {
+                emax_w[0][wid] = er;
+                emax_w[1][wid] = ec;
+            }
+            __syncthreads();
+            er = emax_w[0][0];
+            ec = emax_w[1][0];
+#pragma unroll
+            for (int k = 1; k < NW; ++k) {
+                er = fmaxf(er, emax_w[0][k]);
+                ec = fmaxf(ec, emax_w[1][k]);
+            }
+            const float twoh = er + ec;
+            far = twoh * twoh * 1.000001f;
+        }
         long long acca = 0, accb = 0;
         if (I != J) {
             for (int k = 0; k < T; ++k) {
@@ -367,8 +395,8 @@ pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_h
                     const float4 rj = sr[jl];
                     const float ej = ss[jl];
                     long long tr, tc, col = 0;
-                    if (ra.v) { pot_pair(ra, rj, ej, plummer, tr, tc); acca += tr; col += tc; }
-                    if (rb.v) { pot_pair(rb, rj, ej, plummer, tr, tc); accb += tr; col += tc; }
+                    if (ra.v) { pot_pair(ra, rj, ej, plummer, far, tr, tc); acca += tr; col += tc; }
+                    if (rb.v) { pot_pair(rb, rj, ej, plummer, far, tr, tc); accb += tr; col += tc; }
                     acc_w[wid][jl] += col;
                 }
                 __syncwarp();
@@ -381,7 +409,7 @@ pot_sym_kernel(const int2 *__restrict__ items, const int *d_nitems, int nitems_h
                 const PotRow &a = k <= H ? ra : rb;
                 if (jl < nj && a.v) {
                     long long tr, tc;
-                    pot_pair(a, sr[jl], ss[jl], plummer, tr, tc);
+                    pot_pair(a, sr[jl], ss[jl], plummer, far, tr, tc);
                     if (k <= H) acca += tr; else accb += tr;
                     acc_w[wid][jl] += tc;
                 }
