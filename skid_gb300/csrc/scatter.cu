@@ -488,6 +488,12 @@ cudaError_t mover_resort(MoverState &m, float3 keylo, float3 keyinv, SortScratch
 {
     cudaError_t e;
     int cap = bound > 0 && bound < m.cap ? bound : m.cap;
+    // sort scratch for cap keys: the eager first iteration can re-sort before
+    // its prune has sized it (no allocation happens in a captured graph, whose
+    // sizes the eager iteration already set)
+    if ((e = dalloc(ss.k0, cap)) || (e = dalloc(ss.k1, cap)) || (e = dalloc(ss.v0, cap)) ||
+        (e = dalloc(ss.v1, cap)))
+        return e;
     resort_keys_kernel<<<grid_for(cap), 256, 0, st>>>(m.act.p, m.d_nA, m.mpos.p, keylo, keyinv,
                                                       ss.k0.p, ss.v0.p); skid::note_launch();
     if ((e = radix_sort(ss, cap, 32, st, m.d_nA))) return e;
