@@ -12,9 +12,15 @@
 # the handful of XDR routines the reference calls.  -ffp-contract=off keeps
 # a*b+c unfused on hosts whose gcc contracts to FMA by default (aarch64).
 #
-# Usage: sh oracle/build_ref.sh [reference-dir]   (default /root/reference)
+# Usage: sh oracle/build_ref.sh <reference-source-dir>
+#   (or SKID_REF_DIR=<dir> sh oracle/build_ref.sh); oracle.py passes the
+#   staged copy baseline/_ref/src.
 set -eu
-REF=${1:-/root/reference}
+REF=${1:-${SKID_REF_DIR:-}}
+if [ -z "$REF" ]; then
+    echo "build_ref: give the reference source directory (argument or SKID_REF_DIR)" >&2
+    exit 2
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/kd.c" ]; then

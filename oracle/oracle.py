@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import shutil
 import subprocess
 
 import numpy as np
@@ -17,6 +18,14 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libskidoracle.so")
 SRC = os.path.join(HERE, "skid_oracle.c")
 REF_SKID = os.path.join(HERE, "_ref", "skid")
+REF_NSP = os.path.join(HERE, "_ref", "skid_nsp")
+# Staged copy of the reference's sources: untracked (gitignored), it travels
+# with the working tree to hosts that have no reference checkout, where
+# build_ref.sh compiles it for that host.
+REF_SRC = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "src")
+REF_FILES = ("main.c", "kd.c", "kd.h", "smooth1.c", "smooth1.h", "grav.c", "grav.h", "cosmo.c",
+             "cosmo.h", "romberg.c", "runge.c", "runge.h", "tipsydefs.h", "totipnat.c",
+             "Makefile", "README", "demo", "dark.std")
 
 FLT_MAX = float(np.finfo(np.float32).max)
 
@@ -33,12 +42,44 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_reference(ref_dir: str = "/root/reference") -> str | None:
-    """Build the unmodified reference into oracle/_ref when its sources exist."""
-    if not os.path.exists(os.path.join(ref_dir, "kd.c")):
+def stage_reference(checkout: str | None = None) -> str | None:
+    """Copy the reference checkout's files into baseline/_ref/src, unchanged.
+
+    The checkout is $SKID_REF_CHECKOUT, else the read-only checkout mounted
+    at /root/reference where this repository is developed.  Returns the
+    staged directory, or None when neither a checkout nor a staged copy
+    exists."""
+    checkout = checkout or os.environ.get("SKID_REF_CHECKOUT") or "/root/reference"
+    if os.path.exists(os.path.join(checkout, "kd.c")):
+        os.makedirs(REF_SRC, exist_ok=True)
+        for f in REF_FILES:
+            src = os.path.join(checkout, f)
+            dst = os.path.join(REF_SRC, f)
+            if os.path.exists(src) and (not os.path.exists(dst)
+                                        or os.path.getmtime(dst) < os.path.getmtime(src)):
+                shutil.copyfile(src, dst)
+    return REF_SRC if os.path.exists(os.path.join(REF_SRC, "kd.c")) else None
+
+
+def _ref_stale() -> bool:
+    if not (os.path.exists(REF_SKID) and os.path.exists(REF_NSP)):
+        return True
+    t = min(os.path.getmtime(REF_SKID), os.path.getmtime(REF_NSP))
+    deps = [os.path.join(REF_SRC, f) for f in REF_FILES if f.endswith((".c", ".h"))]
+    deps += [os.path.join(HERE, "build_ref.sh"), os.path.join(HERE, "nsp_shim.c")]
+    return any(os.path.exists(d) and os.path.getmtime(d) > t for d in deps)
+
+
+def build_reference(force: bool = False) -> str | None:
+    """Build the unmodified reference into oracle/_ref from the staged sources
+    (staging them first when a checkout is present).  Returns the binary, or
+    None when no sources are available on this host."""
+    src = stage_reference()
+    if src is None:
         return None
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), ref_dir],
-                          stdout=subprocess.DEVNULL)
+    if force or _ref_stale():
+        subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), src],
+                              stdout=subprocess.DEVNULL)
     return REF_SKID
 
 

@@ -50,6 +50,16 @@ CONFIGS = {
 }
 
 
+def config1_spec(n: int) -> HaloSpec:
+    """The 2^21 clustered workload's generator at another particle count in the
+    same unit box: halos in proportion to N (800 at 2^21), the same mass
+    range, concentrations, largest r200 and seed."""
+    if n == CONFIGS[1].n:
+        return CONFIGS[1]
+    return HaloSpec(n, max(1, round(800 * n / CONFIGS[1].n)), 3.0, (4.0, 20.0), 0.02, 0.55,
+                    SEED_BASE + 1)
+
+
 def hubble_for(omega0: float) -> float:
     """Self-consistent H0 for G=1, mean density 1: H0 = sqrt(8 pi / (3 Omega0))."""
     return math.sqrt(8.0 * math.pi / (3.0 * omega0))
@@ -180,6 +190,69 @@ def subvolume_specs(n_vol: int = 96, seed: int = SEED_BASE + 2, lo: int = 14, hi
         spec = HaloSpec(n, n_halo, 3.0, (4.0, 20.0), 0.02, 0.55, seed * 1000 + i)
         out.append((spec, k, tau))
     return out
+
+
+def config1_subvolume(index: int, parts: int = 16):
+    """One of `parts` independent periodic cubes that together sample the
+    2^21 clustered workload: each holds 2^21 / parts particles in a cube of
+    side L = parts^(-1/3) centred on 0, so the particle mass (2^-21), number
+    density, softening and flags other than -p are the full workload's.
+
+    Halos follow the full workload's population rather than being
+    renormalised per cube: 800 / parts halos per cube, masses log-uniform
+    over 3 decades with the full box's expected particles per unit mass
+    (so a cube's halo fraction fluctuates about 55 %), r200 = 0.02 (M /
+    10^3)^(1/3), concentrations 4-20; the rest of the cube is uniform
+    background.  Returns (snapshot, L as float32)."""
+    full = CONFIGS[1]
+    n = full.n // parts
+    L = np.float32((1.0 / parts) ** (1.0 / 3.0))
+    rng = np.random.default_rng(full.seed * 1000 + 7 * parts + index)
+    n_halo = max(1, round(full.n_halo / parts))
+    logm = rng.uniform(0.0, full.dex, n_halo)
+    m = 10.0 ** logm
+    mean_m = (10.0 ** full.dex - 1.0) / (full.dex * math.log(10.0))
+    per_m = full.halo_frac * full.n / (full.n_halo * mean_m)
+    counts = np.maximum(1, np.round(m * per_m)).astype(np.int64)
+    while counts.sum() > n:                       # a cube never overfills
+        counts[np.argmax(counts)] -= counts.sum() - n
+    n_halo_p = int(counts.sum())
+    r200 = full.r200_max * (m / 10.0 ** full.dex) ** (1.0 / 3.0)
+    conc = rng.uniform(full.conc[0], full.conc[1], n_halo)
+    centres = rng.uniform(-0.5, 0.5, (n_halo, 3)) * float(L)
+    bulk = rng.normal(0.0, 0.1, (n_halo, 3))
+    hid = np.repeat(np.arange(n_halo), counts)
+    x = _nfw_x(rng.uniform(0.0, 1.0, n_halo_p), conc[hid])
+    r = x * (r200[hid] / conc[hid])
+    costh = rng.uniform(-1.0, 1.0, n_halo_p)
+    phi = rng.uniform(0.0, 2.0 * math.pi, n_halo_p)
+    sinth = np.sqrt(1.0 - costh * costh)
+    d = np.stack([sinth * np.cos(phi), sinth * np.sin(phi), costh], axis=1)
+    hpos = centres[hid] + r[:, None] * d
+    sig = np.sqrt((counts.astype(np.float64) / full.n) / (2.0 * r200))
+    hvel = bulk[hid] + rng.normal(0.0, 1.0, (n_halo_p, 3)) * sig[hid][:, None]
+    nb = n - n_halo_p
+    bpos = rng.uniform(-0.5, 0.5, (nb, 3)) * float(L)
+    bvel = rng.normal(0.0, 0.05, (nb, 3))
+    perm = rng.permutation(n)
+    pos = np.concatenate([hpos, bpos])[perm] / float(L)
+    vel = np.concatenate([hvel, bvel])[perm]
+    pos = (_wrap32(pos).astype(np.float64) * float(L)).astype(np.float32)
+    half = np.float32(0.5) * L
+    pos[pos >= half] = -half
+    pos[pos < -half] = -half
+    eps = 0.02 * full.n ** (-1.0 / 3.0)
+    snap = tipsy.Snapshot(1.0, 0, n, 0, pos, vel.astype(np.float32),
+                          np.full(n, 1.0 / full.n, np.float32), np.full(n, eps, np.float32),
+                          np.zeros(n, np.float32))
+    return snap, L
+
+
+def config1_subvolume_flags(L) -> list:
+    """The 2^21 workload's flags for one of its periodic sub-volume cubes."""
+    f = list(WORKLOAD_FLAGS[1])
+    f[f.index("-p") + 1] = repr(float(L))
+    return f
 
 
 # skid command-line flags for each workload (the reference's own flag names).

@@ -71,14 +71,13 @@ def _flags_for(meta, case_dir):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["dark4k_periodic", "mixed6k", "dark8k_lcdm", "dark6k_nsp", "dark4k_unbind_gtp",
-                                  "mixed6k_unbind_com"])
+                                  "mixed6k_unbind_com", "demo_dark_std", "config0_32k",
+                                  "mixed6k_go", "dark4k_center"])
 def test_cli_vs_reference(gpu_ready, cli, tmp_path, name):
     from skid_gb300 import tipsy
     snap, opts, ref, counts, meta = gc.load(name)
     case_dir = os.path.join(gc.GOLDEN, name)
-    src = os.path.join(gc.GOLDEN, meta.get("input_from", name), "input.bin")
-    with open(src, "rb") as f:
-        data = f.read()
+    data = gc.input_bytes(name, meta)
     r = _run(cli, [*_flags_for(meta, case_dir), "-o", "out"], data, tmp_path)
     assert r.returncode == 0, r.stderr.decode()
     got = _stdout_counts(r.stdout.decode())
@@ -108,7 +107,7 @@ def test_cli_vs_reference(gpu_ready, cli, tmp_path, name):
             np.testing.assert_allclose(st[:, 2:], ref["stat"][:, 2:], rtol=2e-4, atol=2e-5)
     if "ray" in ref:
         ray = np.loadtxt(tmp_path / "out.ray", dtype=np.float64)
-        want = np.loadtxt(os.path.join(case_dir, "ref.ray"), dtype=np.float64)
+        want = np.loadtxt(gc.ref_path(name, "ray", meta), dtype=np.float64)
         assert ray[0] == want[0]
         assert np.abs(ray[1:] - want[1:]).max() < 0.2 * opts.fStep
 
