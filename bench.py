@@ -27,11 +27,13 @@ and reported under ``config.plain`` with its per-particle catalogue agreement
 with the default form.  A run with ``-nsp`` (every scatterer kept) is
 reported under ``config.nsp``.
 
-``--impl reference`` times the reference algorithm on the host cores: the
-reference's own binary cannot be built on this host (its sources are not
-here), so the oracle's C restatement of it runs: skid is single-threaded, so
-each host core runs one independent copy of the sample and the value is the
-aggregate particles/s.
+``--impl reference`` times reference skid itself on the host cores, built
+from its own sources (staged untracked under baseline/_ref/src, compiled by
+oracle/build_ref.sh for the host).  skid is single-threaded, so each step
+runs the 2^21 workload as 16 independent periodic sub-volume cubes of 2^17
+particles with the workload's density, halo population and flags, one
+process per core; value = 2^21 / the step's wall time.  The same step, once,
+is the default run's ``cpu_baseline``.
 """
 from __future__ import annotations
 
@@ -52,7 +54,6 @@ import numpy as np  # noqa: E402
 METRIC = "particles/s end-to-end SKID @2^21: batched+adjoint vs plain GPU, same accuracy"
 UNIT = "particles/s"
 N_DEFAULT = 1 << 21
-CPU_SAMPLE_N = 1 << 16
 FALLBACK_HBM = 6800.0
 
 
@@ -167,25 +168,123 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n_sample=CPU_SAMPLE_N, repeats=1):
-    """The oracle's restatement of skid on a bounded sample, one host core."""
+REF_PARTS = 16     # periodic sub-volume cubes that together make one 2^21 step
+
+
+def reference_binary():
+    """Reference skid built from its own sources for this host (staged under
+    baseline/_ref/src), or None with the reason."""
     from oracle import oracle
+    try:
+        exe = oracle.build_reference()
+    except Exception as e:          # a compiler error on this host
+        return None, f"reference build failed: {e}"
+    if exe is None or not os.path.exists(exe):
+        return None, "reference sources not present on this host"
+    return exe, None
+
+
+def write_subvolumes(dirpath, parts=REF_PARTS):
+    """The 2^21 workload as `parts` independent periodic cubes of 2^21/parts
+    particles each (synth.config1_subvolume), written as native TIPSY files.
+    Returns [(path, flags)]."""
     from skid_gb300 import synth
+    out = []
+    for i in range(parts):
+        snap, L = synth.config1_subvolume(i, parts)
+        path = os.path.join(dirpath, f"sub{i:02d}.bin")
+        synth.write_snapshot(path, snap)
+        out.append((path, synth.config1_subvolume_flags(L)))
+    return out
+
+
+def _run_reference_file(exe, path, fl, cwd):
+    """One reference skid process on one input file (stdin), outputs written
+    to cwd.  Returns (seconds, stdout counts)."""
+    t = time.perf_counter()
+    with open(path, "rb") as f:
+        r = subprocess.run([exe, *fl, "-o", os.path.splitext(os.path.basename(path))[0]],
+                           stdin=f, cwd=cwd, capture_output=True, text=True)
+    dt = time.perf_counter() - t
+    if r.returncode:
+        raise RuntimeError(f"reference skid failed on {path}: {r.stderr[-400:]}")
+    counts = {}
+    for line in r.stdout.splitlines():
+        for key, tag in (("groups_before_unbind", "Groups before Unbind:"),
+                         ("unbound", "Number of particles Unbound:"),
+                         ("groups", "Number of Groups:")):
+            if line.startswith(tag):
+                counts[key] = int(line.split(":")[1])
+    return dt, counts
+
+
+def _run_port_file(path, fl):
+    """The oracle's C restatement on one input file (fallback when the
+    reference binary cannot be built here)."""
+    from oracle import oracle
+    from skid_gb300 import tipsy
     from skid_gb300.options import Options
-    oracle.build()
-    snap = synth.make_snapshot(workload(n_sample))
-    opts = Options.parse(flags())
-    best = None
-    for _ in range(repeats):
-        t = time.perf_counter()
-        oracle.run(snap, opts)
-        dt = time.perf_counter() - t
-        best = dt if best is None else min(best, dt)
-    return {"value": n_sample / best, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"oracle C restatement of skid, single-threaded, one run on a "
-                      f"{n_sample}-particle box generated like the 2^21 workload "
-                      f"({max(1, round(800 * n_sample / N_DEFAULT))} halos), same flags; "
-                      f"{best:.1f} s"}
+    snap = tipsy.read_tipsy(path)
+    t = time.perf_counter()
+    r = oracle.run(snap, Options.parse(fl))
+    return time.perf_counter() - t, {"groups_before_unbind": r["nGroupFoF"],
+                                     "unbound": r["nUnbound"], "groups": r["nGroup"]}
+
+
+def reference_step(exe, inputs, workers, cwd):
+    """All sub-volumes through reference skid (or the port when exe is None),
+    `workers` processes at a time.  Returns (wall seconds, per-run seconds,
+    summed counts)."""
+    import concurrent.futures as cf
+    t = time.perf_counter()
+    if exe is not None:
+        with cf.ThreadPoolExecutor(workers) as ex:
+            res = list(ex.map(lambda a: _run_reference_file(exe, a[0], a[1], cwd), inputs))
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            res = pool.starmap(_run_port_file, inputs, chunksize=1)
+    wall = time.perf_counter() - t
+    tot = {}
+    for _, c in res:
+        for k, v in c.items():
+            tot[k] = tot.get(k, 0) + v
+    return wall, [r[0] for r in res], tot
+
+
+def _subvolume_sample_text(kind, parts, workers, per_run, why=None):
+    from skid_gb300 import synth
+    n_sub = synth.CONFIGS[1].n // parts
+    what = ("reference skid v1.4.1 built from its own sources on this host (gcc -O2 "
+            "-ffp-contract=off)" if kind == "reference" else
+            f"the oracle's C restatement of skid ({why})")
+    return (f"{what}: the 2^21 workload as {parts} independent periodic cubes of {n_sub} "
+            f"particles (side {parts}^(-1/3), the workload's particle density, halo population "
+            f"and flags, -p set to the side), {workers} processes at a time, each "
+            f"single-threaded; {statistics.mean(per_run):.1f} s per cube")
+
+
+def cpu_baseline(steps=1):
+    """Reference skid on the host cores over one 2^21 step of sub-volumes
+    (about 15 s of wall time with 16 cores)."""
+    import tempfile
+    exe, why = reference_binary()
+    cores = os.cpu_count() or 1
+    workers = min(cores, REF_PARTS)
+    with tempfile.TemporaryDirectory() as tmp:
+        inputs = write_subvolumes(tmp)
+        walls, per_run = [], []
+        for _ in range(steps):
+            w, pr, counts = reference_step(exe, inputs, workers, tmp)
+            walls.append(w)
+            per_run += pr
+    kind = "reference" if exe else "port"
+    n = N_DEFAULT
+    return {"value": n * len(walls) / sum(walls), "unit": UNIT, "cores": workers, "kind": kind,
+            "per_core_value": (n / REF_PARTS) / statistics.mean(per_run),
+            "n_particles": n, "sample": _subvolume_sample_text(kind, REF_PARTS, workers,
+                                                               per_run, why),
+            "catalogue": counts}
 
 
 def reduce_max(x: float, world: int, device="cpu") -> float:
@@ -211,61 +310,44 @@ def dist_setup():
     return world, rank, local
 
 
-REF_SAMPLE_N = 1 << 15
-_ref_snap = None
-
-
-def _ref_init(n):
-    """Pool worker: build this core's copy of the sample once."""
-    global _ref_snap
-    from skid_gb300 import synth
-    _ref_snap = synth.make_snapshot(workload(n))
-
-
-def _ref_task(_):
-    from oracle import oracle
-    from skid_gb300.options import Options
-    t = time.perf_counter()
-    oracle.run(_ref_snap, Options.parse(flags()))
-    return time.perf_counter() - t
-
-
 def run_reference(args):
-    """The reference algorithm (oracle C restatement, single-threaded like
-    skid) on every host core: each core runs one copy of a bounded sample of
-    the workload per step; value = cores x particles / wall time."""
-    import multiprocessing as mp
+    """Reference skid itself on the host cores: each step runs the 2^21
+    workload as REF_PARTS periodic sub-volume cubes, one single-threaded
+    process per core; value = 2^21 particles / wall time of the step.  Falls
+    back to the oracle's C restatement (labelled "port") only where the
+    reference cannot be built."""
+    import tempfile
     world, rank, local = dist_setup()
     if rank != 0:
         return 0
-    from oracle import oracle
-    oracle.build()
-    n = REF_SAMPLE_N
+    exe, why = reference_binary()
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores, initializer=_ref_init, initargs=(n,)) as pool:
-        for _ in range(min(args.warmup, 1)):
-            pool.map(_ref_task, range(cores), chunksize=1)
-        walls, per_core = [], []
+    workers = min(cores, REF_PARTS)
+    n = N_DEFAULT
+    with tempfile.TemporaryDirectory() as tmp:
+        inputs = write_subvolumes(tmp)
+        for _ in range(min(args.warmup, 1)):     # page cache; the CPU needs no warm-up
+            reference_step(exe, inputs, workers, tmp)
+        walls, per_run = [], []
         for _ in range(args.steps):
-            t = time.perf_counter()
-            ts = pool.map(_ref_task, range(cores), chunksize=1)
-            walls.append(time.perf_counter() - t)
-            per_core.extend(ts)
+            w, pr, counts = reference_step(exe, inputs, workers, tmp)
+            walls.append(w)
+            per_run += pr
     tot = sum(walls)
-    value = cores * n * len(walls) / tot
-    sample = (f"{cores} concurrent copies (one per host core) of a {n}-particle box generated "
-              f"like the 2^21 workload ({max(1, round(800 * n / N_DEFAULT))} halos), same flags, "
-              f"oracle C restatement of skid (the reference binary cannot be built on this "
-              f"host); {statistics.mean(per_core):.1f} s per copy")
+    value = n * len(walls) / tot
+    kind = "reference" if exe else "port"
+    sample = _subvolume_sample_text(kind, REF_PARTS, workers, per_run, why)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / len(walls),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"skid on {cores} x {n}-particle samples of the 2^21 workload "
-                                   f"(NFW halos + background), periodic unit box",
-                       "flags": " ".join(flags()), "n_particles": n, "copies": cores},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "config": {"workload": f"skid config 1 (N=2^21 clustered, 800 NFW halos + uniform "
+                                   f"background) as {REF_PARTS} periodic sub-volume cubes of "
+                                   f"{n // REF_PARTS} particles",
+                       "flags": " ".join(flags()) + f" (-p = cube side)", "n_particles": n,
+                       "sub_volumes": REF_PARTS, "processes": workers, "catalogue": counts},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": kind,
+                             "per_core_value": (n / REF_PARTS) / statistics.mean(per_run),
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
