@@ -12,6 +12,10 @@
 
 namespace skid {
 
+// Per-device tables (SM counts, kernel attributes, static scratch addresses)
+// are indexed by the CUDA device ordinal below this bound.
+constexpr int SKID_MAX_DEVICES = 64;
+
 // Device buffer that remembers its size.
 // Device allocation, freeing and graph capture take this process-wide lock:
 // cudaMalloc/cudaFree may synchronise the device, which must not happen while

@@ -195,18 +195,24 @@ cudaError_t knn_ball2(const Tree &t, int k, float3 L, bool per, float *ball2_sor
     while (nw > 1 && (size_t)nw * (candBytes + heapBytes) > (size_t)optin) nw >>= 1;
     bool global = (size_t)nw * (candBytes + heapBytes) > (size_t)optin;
     size_t smem = (size_t)nw * candBytes + (global ? 0 : (size_t)nw * heapBytes);
-    // The attribute is process-wide and only an upper bound: raise it to the
-    // opt-in maximum once (contexts on other threads launch with other k).
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [&] {
-        cudaFuncAttributes fa;
-        attr_err = cudaFuncGetAttributes(&fa, knn_kernel);
-        if (!attr_err)
-            attr_err = cudaFuncSetAttribute(knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            optin - (int)fa.sharedSizeBytes);
-    });
-    cudaError_t e = attr_err;
+    // The attribute belongs to the device and is only an upper bound: raise it
+    // to the opt-in maximum once per device (contexts on other threads launch
+    // with other k).
+    static std::mutex attr_mu;
+    static bool attr_done[SKID_MAX_DEVICES] = {};
+    if (dev < 0 || dev >= SKID_MAX_DEVICES) return cudaErrorInvalidDevice;
+    cudaError_t e = cudaSuccess;
+    {
+        std::lock_guard<std::mutex> lk(attr_mu);
+        if (!attr_done[dev]) {
+            cudaFuncAttributes fa;
+            e = cudaFuncGetAttributes(&fa, knn_kernel);
+            if (!e)
+                e = cudaFuncSetAttribute(knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         optin - (int)fa.sharedSizeBytes);
+            if (!e) attr_done[dev] = true;
+        }
+    }
     if (e) return e;
     int perSM = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, knn_kernel, nw * 32, smem);

@@ -18,7 +18,9 @@
 // stream capture.  All calls share the array and it keeps the last call's
 // contents: every buffer is rewritten or cleared before use, and two calls
 // whose work overlaps on the GPU (different streams, or different host
-// threads) race on it.
+// threads) race on it.  A call that fails with SKID_ECUDA has consumed the
+// device's last-error state (cudaGetLastError), including an error that
+// something else on this thread left pending.
 #include <cfloat>
 #include <mutex>
 
@@ -61,7 +63,7 @@ static_assert(NA_BYTES < (8u << 20), "scratch must stay modest");
 __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 std::mutex g_mu;
-unsigned char *g_addr[64] = {};
+unsigned char *g_addr[SKID_MAX_DEVICES] = {};
 
 __global__ void na_xyz_to_pos4(const float *__restrict__ xyz, int n, float4 *__restrict__ out)
 {
@@ -90,7 +92,7 @@ DBuf<T> view(unsigned char *base, size_t off, size_t count)
 int scratch_address(unsigned char **out)
 {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= SKID_MAX_DEVICES) {
         cudaGetLastError();
         return SKID_ENODEV;
     }

@@ -177,14 +177,23 @@ __global__ void scan_apply(const int *in, int *out, int n, const int *blk, int n
 
 int num_sms()
 {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
+    // per device: a process may drive several GPUs (one context per thread)
+    static std::atomic<int> sms[SKID_MAX_DEVICES];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= SKID_MAX_DEVICES) {
+        cudaGetLastError();
+        dev = 0;
     }
-    return sms;
+    int v = sms[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            v <= 0) {
+            cudaGetLastError();
+            v = 1;
+        }
+        sms[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
 }
 
 cudaError_t radix_sort(SortScratch &s, int n, int bits, cudaStream_t st, const int *d_n)

@@ -146,8 +146,10 @@ __global__ void upward_kernel(const float4 *__restrict__ pos, const float *__res
 
 cudaError_t bbox_of(const float4 *pts, int n, unsigned *d_box6, cudaStream_t st)
 {
-    static const unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
-    cudaError_t e = cudaMemcpyAsync(d_box6, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    // order-preserving bit patterns: the three minima start at all ones, the
+    // three maxima at zero (set on the device, no host memory involved)
+    cudaError_t e = cudaMemsetAsync(d_box6, 0xff, 3 * sizeof(unsigned), st);
+    if (!e) e = cudaMemsetAsync(d_box6 + 3, 0, 3 * sizeof(unsigned), st);
     if (e) return e;
     int blocks = min((n + 255) / 256, num_sms() * 4);
     if (blocks < 1) blocks = 1;

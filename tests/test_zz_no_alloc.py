@@ -7,7 +7,9 @@ that cannot afford cudaMalloc's implicit synchronisation -- so this test
 hands it device buffers it allocated elsewhere (torch) and checks the
 results against the ordinary entry point on two calls in a row (the second
 reuses the static scratch the first one left behind).  fBall2 is compared
-exactly, the tolerance every fBall2 test here uses.
+exactly, the tolerance every fBall2 test here uses.  It also checks the
+promise itself: after a first call on the device, a further call on a side
+stream leaves the device's free memory unchanged.
 """
 import ctypes as C
 
@@ -17,6 +19,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 FLT_MAX = float(np.finfo(np.float32).max)
+EINVAL = -1
 ETOOLARGE = -8
 MAX_POINTS = 65536
 MAX_K = 256
@@ -66,3 +69,39 @@ def test_noalloc_refuses_sizes_beyond_its_scratch(gpu_ready):
     assert fn(big.data_ptr(), MAX_POINTS + 1, 16, per, out.data_ptr(), None) == ETOOLARGE
     assert fn(big.data_ptr(), 1000, MAX_K + 1, per, out.data_ptr(), None) == ETOOLARGE
     torch.cuda.synchronize()
+
+
+def test_noalloc_allocates_nothing_on_a_side_stream(gpu_ready):
+    torch = pytest.importorskip("torch")
+    from skid_gb300 import gpu
+    fn = _entry()
+    rng = np.random.default_rng(77)
+    n, k = 40000, 48
+    pos = _points(rng, n)
+    with gpu.Context(period=1.0, nSmooth=k) as ctx:
+        want = ctx.knn_ball2(pos, k)
+    d_pos = torch.from_numpy(pos.reshape(-1)).cuda()
+    d_out = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
+    per = (C.c_float * 3)(1.0, 1.0, 1.0)
+    side = torch.cuda.Stream()
+    assert fn(d_pos.data_ptr(), n, k, per, d_out.data_ptr(), side.cuda_stream) == 0
+    side.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    d_out.fill_(-1.0)
+    torch.cuda.synchronize()
+    assert fn(d_pos.data_ptr(), n, k, per, d_out.data_ptr(), side.cuda_stream) == 0
+    side.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"device free memory changed by {free0 - free1} bytes"
+    assert np.array_equal(d_out.cpu().numpy(), want)
+
+
+def test_noalloc_rejects_bad_k(gpu_ready):
+    torch = pytest.importorskip("torch")
+    fn = _entry()
+    per = (C.c_float * 3)(1.0, 1.0, 1.0)
+    pts = torch.zeros(3 * 100, dtype=torch.float32, device="cuda")
+    out = torch.zeros(100, dtype=torch.float32, device="cuda")
+    assert fn(pts.data_ptr(), 100, 0, per, out.data_ptr(), None) == EINVAL
+    assert fn(pts.data_ptr(), 100, 101, per, out.data_ptr(), None) == EINVAL
+    assert fn(pts.data_ptr(), -1, 8, per, out.data_ptr(), None) == EINVAL
