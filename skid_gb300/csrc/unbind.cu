@@ -43,39 +43,90 @@ namespace skid {
 namespace {
 
 constexpr int POT_TILE = 128;   // power of two
-// Groups up to this size evaluate E exactly as the reference does (FP64
-// expression rounded to float, kd.c:1396-1399), so equal-energy members are
-// ordered by the reference's own rounding; larger groups use FP32 (GB300's
-// FP64 rate is a small fraction of its FP32 rate).
+// Every removal decision is the reference's: each pass computes FP32 energies
+// with an error bound, and only members within twice the bound of the
+// largest or smallest energy are evaluated exactly (the reference's FP64
+// expression rounded to float, kd.c:1396-1399), so the arg-max and arg-min,
+// ties included, are those of the reference's loop.  Groups up to this size
+// use the plain FP32 form with a per-member bound; larger ones the staged
+// a v + aH r form with one bound per pass (GB300's FP64 rate is a small
+// fraction of its FP32 rate, so FP64 is kept to the few candidates).
 constexpr int EXACT_E_MAX = 1024;
 
-__device__ __forceinline__ float spline_pot(float d2, float twoh, int plummer)
+// The reference's pair factor, bit for bit.  grav.c:25-30 forms it as a float
+// assigned from FP64 arithmetic (gcc, no contraction): Plummer
+// 1.0/sqrt(d2 + 0.25*twoh*twoh); spline SPLINE_POT (grav.h:11-31) with
+// r = sqrt(d2) in FP64, the polynomials evaluated left to right, and 1/r
+// beyond the softening.  The FP64 forms below spell every operation out with
+// round-to-nearest intrinsics so the compiler cannot fuse them.
+__device__ __noinline__ float ref_dir_fp64(float d2f, float twohf, int plummer)
 {
-    if (plummer) return 1.0f / sqrtf(d2 + 0.25f * twoh * twoh);
-    float r = sqrtf(d2);
+    const double r2 = (double)d2f, twoh = (double)twohf;
+    if (plummer)
+        return (float)__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(r2, __dmul_rn(__dmul_rn(0.25, twoh), twoh))));
+    const double r = __dsqrt_rn(r2);
     if (r < twoh) {
-        float dih = 2.0f / twoh;
-        float u = r * dih;
-        float u2 = u * u;
-        if (u < 1.0f) {
-            return dih * (1.4f - (2.0f / 3.0f) * u2 + 0.3f * u2 * u2 - 0.1f * u2 * u2 * u);
+        const double dih = __ddiv_rn(2.0, twoh);
+        const double u = __dmul_rn(r, dih);
+        if (u < 1.0) {
+            // dih*(7/5 - 2/3*u*u + 3/10*u*u*u*u - 1/10*u*u*u*u*u)
+            const double a = __dmul_rn(__dmul_rn(2.0 / 3.0, u), u);
+            const double b = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(3.0 / 10.0, u), u), u), u);
+            const double c =
+                __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(1.0 / 10.0, u), u), u), u), u);
+            return (float)__dmul_rn(dih, __dsub_rn(__dadd_rn(__dsub_rn(7.0 / 5.0, a), b), c));
         }
-        return -(1.0f / 15.0f) / r +
-               dih * (1.6f - (4.0f / 3.0f) * u2 + u2 * u - 0.3f * u2 * u2 + (1.0f / 30.0f) * u2 * u2 * u);
+        // -1/15*dir + dih*(8/5 - 4/3*u*u + u*u*u - 3/10*u*u*u*u + 1/30*u*u*u*u*u)
+        const double dir = __ddiv_rn(1.0, r);
+        const double a = __dmul_rn(__dmul_rn(4.0 / 3.0, u), u);
+        const double b = __dmul_rn(__dmul_rn(u, u), u);
+        const double c = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(3.0 / 10.0, u), u), u), u);
+        const double e =
+            __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(1.0 / 30.0, u), u), u), u), u);
+        const double poly = __dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(8.0 / 5.0, a), b), c), e);
+        return (float)__dadd_rn(__dmul_rn(-1.0 / 15.0, dir), __dmul_rn(dih, poly));
     }
-    return 1.0f / r;
+    return (float)__ddiv_rn(1.0, r);
 }
 
-// The pair factor used for every potential term, added (potentials) and
-// subtracted (removal) alike.  Beyond the softening (r >= 2h, certain once
-// d2 clears (2h)^2 by the margin below) it is 1/r, taken as the correctly
-// rounded reciprocal square root of d2 -- one rounding, as the FP64 1/sqrt
-// of grav.h:11-31 rounded to float; inside, the spline above.
+// 1/r beyond the softening as the reference rounds it: float(1.0/sqrt(d2)),
+// two correctly rounded FP64 operations then a rounding to float.  That float
+// is the one nearest the real 1/sqrt(d2) unless 1/sqrt(d2) lies within about
+// 2^-52 (relative) of a midpoint between floats.  Here 1/sqrt(d2) is formed
+// as the unevaluated float pair y + d, within 2^-43 of it: y the hardware
+// reciprocal square root (within 2^-22) and d = y r / 2 one Newton
+// correction, whose residual r = 1 - x y^2 comes from the error-free product
+// x y = ph + pl (pl by a fused multiply-add) as fma(-pl, y, fma(-ph, y, 1)),
+// each fused step rounding only the small result.  The float s nearest
+// y + d is returned unless y + d lies within 2^-17 ulp(s) of a midpoint
+// (|(y + d) - s|, exact by Dekker's fast two-sum, at or above
+// (1/2 - 2^-17) ulp), or s is a power of two; those few pairs in a hundred
+// thousand take the FP64 expression itself.
+__device__ __forceinline__ float ref_rsqrt(float x)
+{
+    if (!(x >= 1e-30f && x <= 1e30f)) return ref_dir_fp64(x, 0.0f, 0);
+    const float y = rsqrtf(x);
+    const float ph = __fmul_rn(x, y);
+    const float pl = __fmaf_rn(x, y, -ph);
+    const float r = __fmaf_rn(-pl, y, __fmaf_rn(-ph, y, 1.0f));
+    const float d = __fmul_rn(__fmul_rn(0.5f, y), r);
+    const float s = __fadd_rn(y, d);
+    const float e = __fsub_rn(d, __fsub_rn(s, y));
+    const unsigned sb = __float_as_uint(s);
+    // (1/2 - 2^-17) ulp(s): exponent of ulp/4, mantissa 2 - 2^-15
+    const float near = __uint_as_float(((sb & 0x7f800000u) - (25u << 23)) | 0x7fff00u);
+    if ((sb & 0x7fffffu) == 0u || fabsf(e) >= near) return ref_dir_fp64(x, 0.0f, 0);
+    return s;
+}
+
+// The pair factor of every potential term, added (potentials, scoop) and
+// subtracted (removal) alike, equal to the reference's float dir.  Beyond
+// the softening (r >= 2h, certain once d2 clears (2h)^2 by the margin below)
+// it is ref_rsqrt; inside, and for Plummer softening, the FP64 form.
 __device__ __forceinline__ float pair_dir(float d2, float twoh, int plummer)
 {
-    if (plummer) return rsqrtf(d2 + 0.25f * twoh * twoh);
-    if (d2 >= twoh * twoh * 1.000001f) return rsqrtf(d2);
-    return spline_pot(d2, twoh, 0);
+    if (!plummer && d2 >= twoh * twoh * 1.000001f) return ref_rsqrt(d2);
+    return ref_dir_fp64(d2, twoh, plummer);
 }
 
 __device__ __forceinline__ float wrap_h(float d, float h)
@@ -313,7 +364,7 @@ __device__ __forceinline__ void pot_pair(const PotRow &a, float4 rj, float ej, i
                                          float far, long long &tr, long long &tc)
 {
     float d2 = d2of(fsub(a.r.x, rj.x), fsub(a.r.y, rj.y), fsub(a.r.z, rj.z));
-    float dir = d2 >= far ? rsqrtf(d2) : pair_dir(d2, fadd(a.e, ej), plummer);
+    float dir = d2 >= far ? ref_rsqrt(d2) : pair_dir(d2, fadd(a.e, ej), plummer);
     tr = fx(fmul(rj.w, dir), 1.0f);
     // equal masses (all-dark runs): both ends get the same term
     tc = rj.w == a.r.w ? tr : fx(fmul(a.r.w, dir), 1.0f);
@@ -478,6 +529,20 @@ __device__ __forceinline__ ArgRed warp_argmin(ArgRed a)
     return a;
 }
 
+// A thread's two largest (a, then b) or two smallest energies, the first
+// index kept on ties (members are visited in increasing index).
+__device__ __forceinline__ void keep_top2(ArgRed &a, ArgRed &b, float E, int i)
+{
+    if (E > a.v) { b = a; a.v = E; a.i = i; }
+    else if (E > b.v) { b.v = E; b.i = i; }
+}
+
+__device__ __forceinline__ void keep_bot2(ArgRed &a, ArgRed &b, float E, int i)
+{
+    if (E < a.v) { b = a; a.v = E; a.i = i; }
+    else if (E < b.v) { b.v = E; b.i = i; }
+}
+
 struct RemoveArgs {
     const int *gstart, *gcount;
     int ng, nmax;
@@ -499,20 +564,32 @@ struct RemoveArgs {
     int single;                     // > 0: process only this group (per-group mode)
 };
 
-// E_i of kd.c:1392-1400: exact form (FP64 expression rounded to float, as the
-// reference computes it) or FP32 form for large groups.
+// E_i of kd.c:1392-1400: exact form (the reference's FP64 expression with
+// each operation rounded as gcc rounds it, no fused multiply-adds, then
+// rounded to float) or FP32 form.  Exact form:
+//   dv_j = (float)(a * ((double)v_j - vcm_j) + aH * ((double)r_j - rcm_j))
+//   dv2  = dv_0^2 + dv_1^2 + dv_2^2                      (float)
+//   E    = (float)(0.5 * dv2 - pot * (1.0 + z))
+__device__ __forceinline__ float exact_energy(const RemoveArgs &A, float4 r, float4 v, long long p,
+                                              const double *dcm, double inv_d, double opz_d)
+{
+    const double fs = A.fShift, fc = A.fCosmo;
+    const float dv0 = (float)__dadd_rn(__dmul_rn(fs, __dsub_rn((double)v.x, dcm[3])),
+                                       __dmul_rn(fc, __dsub_rn((double)r.x, dcm[0])));
+    const float dv1 = (float)__dadd_rn(__dmul_rn(fs, __dsub_rn((double)v.y, dcm[4])),
+                                       __dmul_rn(fc, __dsub_rn((double)r.y, dcm[1])));
+    const float dv2 = (float)__dadd_rn(__dmul_rn(fs, __dsub_rn((double)v.z, dcm[5])),
+                                       __dmul_rn(fc, __dsub_rn((double)r.z, dcm[2])));
+    const float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
+    // pot * 2^-S is exact (a power-of-two scale of an integer below 2^53)
+    return (float)__dsub_rn(__dmul_rn(0.5, (double)dd), __dmul_rn(__dmul_rn((double)p, inv_d), opz_d));
+}
+
 __device__ __forceinline__ float member_energy(bool exact, const RemoveArgs &A, float4 r, float4 v,
                                                long long p, const double *dcm, const float *scm,
                                                double inv_d, double opz_d)
 {
-    if (exact) {
-        double fs = A.fShift, fc = A.fCosmo;
-        float dv0 = (float)(fs * ((double)v.x - dcm[3]) + fc * ((double)r.x - dcm[0]));
-        float dv1 = (float)(fs * ((double)v.y - dcm[4]) + fc * ((double)r.y - dcm[1]));
-        float dv2 = (float)(fs * ((double)v.z - dcm[5]) + fc * ((double)r.z - dcm[2]));
-        float dd = fadd(fadd(fmul(dv0, dv0), fmul(dv1, dv1)), fmul(dv2, dv2));
-        return (float)(0.5 * (double)dd - ((double)p * inv_d) * opz_d);
-    }
+    if (exact) return exact_energy(A, r, v, p, dcm, inv_d, opz_d);
     float dv0 = A.fShift * (v.x - scm[3]) + A.fCosmo * (r.x - scm[0]);
     float dv1 = A.fShift * (v.y - scm[4]) + A.fCosmo * (r.y - scm[1]);
     float dv2 = A.fShift * (v.z - scm[5]) + A.fCosmo * (r.z - scm[2]);
@@ -550,17 +627,17 @@ __device__ __forceinline__ long long sub_pot(const RemoveArgs &A, float4 rs, flo
     return p - fx(fmul(fmul(A.G, rs.w) * A.scale, dir), 1.0f);
 }
 
-// centre of mass: kd.c:1360-1375 (FP64 sums of float products)
+// centre of mass after removing (r, v): kd.c:1424-1431,
+//   dMass -= m;  rcm_j += m/dMass * (rcm_j - r_j);  vcm_j likewise,
+// each FP64 operation rounded separately as the reference's are.
 __device__ __forceinline__ void rcm_update(double &mass, double *dcm, float4 r, float4 v)
 {
-    mass -= r.w;
-    double f = (double)r.w / mass;
-    dcm[0] += f * (dcm[0] - r.x);
-    dcm[1] += f * (dcm[1] - r.y);
-    dcm[2] += f * (dcm[2] - r.z);
-    dcm[3] += f * (dcm[3] - v.x);
-    dcm[4] += f * (dcm[4] - v.y);
-    dcm[5] += f * (dcm[5] - v.z);
+    mass = __dsub_rn(mass, (double)r.w);
+    const double f = __ddiv_rn((double)r.w, mass);
+    const float x[6] = {r.x, r.y, r.z, v.x, v.y, v.z};
+#pragma unroll
+    for (int d = 0; d < 6; ++d)
+        dcm[d] = __dadd_rn(dcm[d], __dmul_rn(f, __dsub_rn(dcm[d], (double)x[d])));
 }
 
 __device__ __forceinline__ void write_record(const RemoveArgs &A, int g, int n, double mass,
@@ -615,8 +692,9 @@ __device__ void warp_group(const RemoveArgs &A, int g)
     float es = 0.0f;
     for (;;) {
         ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
-        // FP32 energies (with error bounds for the exact form)
-        float emax = -FLT_MAX, emin = FLT_MAX, dmax = 0.0f;
+        ArgRed mx2 = mx, mn2 = mn;
+        // FP32 energies with error bounds
+        float dmax = 0.0f;
         for (int i = lane; i < n; i += 32) {
             float4 r = qr[i], v = qv[i];
             long long p = pot[i];
@@ -625,19 +703,16 @@ __device__ void warp_group(const RemoveArgs &A, int g)
                 pot[i] = p;
             }
             float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-            if (exact) {
-                emax = fmaxf(emax, E);
-                emin = fminf(emin, E);
-                dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
-            } else {
-                if (E > mx.v) { mx.v = E; mx.i = i; }
-                if (E < mn.v) { mn.v = E; mn.i = i; }
-            }
+            keep_top2(mx, mx2, E, i);
+            keep_bot2(mn, mn2, E, i);
+            if (exact) dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
         }
         if (exact) {
             // only members whose FP32 energy is within twice the error bound
             // of the extremes can be the exact arg-max / arg-min: evaluate
-            // those exactly (FP64, as the reference does)
+            // those exactly (FP64, as the reference does) -- usually just the
+            // lane's own extreme, else its members again
+            float emax = mx.v, emin = mn.v;
 #pragma unroll
             for (int o = 16; o; o >>= 1) {
                 emax = fmaxf(emax, __shfl_xor_sync(SKID_FULL, emax, o));
@@ -645,14 +720,29 @@ __device__ void warp_group(const RemoveArgs &A, int g)
                 dmax = fmaxf(dmax, __shfl_xor_sync(SKID_FULL, dmax, o));
             }
             const float hi = emax - 2.0f * dmax, lo = emin + 2.0f * dmax;
-            for (int i = lane; i < n; i += 32) {
-                float4 r = qr[i], v = qv[i];
-                long long p = pot[i];
-                float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-                if (E >= hi || E <= lo) {
-                    float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
-                    if (E >= hi && X > mx.v) { mx.v = X; mx.i = i; }
-                    if (E <= lo && X < mn.v) { mn.v = X; mn.i = i; }
+            const ArgRed t1 = mx, b1 = mn;
+            mx = ArgRed{-FLT_MAX, 0x7fffffff};
+            mn = ArgRed{FLT_MAX, 0x7fffffff};
+            if (t1.v >= hi && mx2.v < hi) {
+                mx.v = member_energy(true, A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, scm, inv_d, opz_d);
+                mx.i = t1.i;
+            }
+            if (b1.v <= lo && mn2.v > lo) {
+                mn.v = member_energy(true, A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, scm, inv_d, opz_d);
+                mn.i = b1.i;
+            }
+            const bool scan_hi = mx2.v >= hi, scan_lo = mn2.v <= lo;
+            if (scan_hi || scan_lo) {
+                for (int i = lane; i < n; i += 32) {
+                    float4 r = qr[i], v = qv[i];
+                    long long p = pot[i];
+                    float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
+                    const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
+                    if (ch || cl) {
+                        float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
+                        if (ch && X > mx.v) { mx.v = X; mx.i = i; }
+                        if (cl && X < mn.v) { mn.v = X; mn.i = i; }
+                    }
                 }
             }
         }
@@ -704,9 +794,21 @@ struct BlockShared {
     int s_n, s_go, s_have, s_imin;
     double d_cm[6], d_mass;
     double part[BS / 32][7];
-    float ext[BS / 32][3];      // per-warp FP32 energy max, min, error bound
+    float ext[BS / 32][4];      // per-warp FP32 energy max, min, error-bound terms
     float s_w[3];               // a vcm + aH rcm (large groups' FP32 energies)
+    float s_mW;                 // max_j |a vcm_j| + |aH rcm_j|
+    float s_mg;                 // max over members and axes of |a v_j| + |aH r_j|
 };
+
+// max_j |a c_j| + |aH c_{j-3}| of a centre (rcm, vcm)
+__device__ __forceinline__ float centre_mag(const RemoveArgs &A, const double *dcm)
+{
+    float m = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        m = fmaxf(m, fabsf(A.fShift * (float)dcm[3 + d]) + fabsf(A.fCosmo * (float)dcm[d]));
+    return m * 1.0000002f;
+}
 
 // A large group, the whole block.
 template <int BS>
@@ -758,13 +860,27 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
     const double opz_d = 1.0 + (double)A.z, inv_d = 1.0 / (double)A.scale;
     float4 *qw = A.qw + s;
     if (!exact) {
-        // E_i = 1/2 |w_i - W|^2 - pot_i (1+z), w_i = a v_i + aH r_i fixed per
-        // member, W = a vcm + aH rcm per pass (kd.c:1392-1400 in FP32)
+        // FP32 filter energies E_i = 1/2 |w_i - W|^2 - pot_i (1+z), with
+        // w_i = a v_i + aH r_i fixed per member and W = a vcm + aH rcm per
+        // pass; their error bound needs the largest |a v_j| + |aH r_j|
+        float mg = 0.0f;
         for (int i = tid; i < n0; i += BS) {
             float4 r = qr[i], v = qv[i];
             qw[i] = make_float4(__fmaf_rn(A.fShift, v.x, A.fCosmo * r.x),
                                 __fmaf_rn(A.fShift, v.y, A.fCosmo * r.y),
                                 __fmaf_rn(A.fShift, v.z, A.fCosmo * r.z), v.w);
+            mg = fmaxf(mg, fabsf(A.fShift * v.x) + fabsf(A.fCosmo * r.x));
+            mg = fmaxf(mg, fabsf(A.fShift * v.y) + fabsf(A.fCosmo * r.y));
+            mg = fmaxf(mg, fabsf(A.fShift * v.z) + fabsf(A.fCosmo * r.z));
+        }
+        mg = __uint_as_float(__reduce_max_sync(SKID_FULL, __float_as_uint(mg)));
+        if (lane == 0) S.ext[w][0] = mg;
+        __syncthreads();
+        if (tid == 0) {
+            float t = 0.0f;
+            for (int k = 0; k < BS / 32; ++k) t = fmaxf(t, S.ext[k][0]);
+            S.s_mg = t * 1.0000002f;
+            S.s_mW = centre_mag(A, S.d_cm);
         }
         __syncthreads();
     }
@@ -778,7 +894,8 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         float scm[6];
         for (int d = 0; d < 6; ++d) { dcm[d] = S.d_cm[d]; scm[d] = S.s_cm[d]; }
         ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
-        float emax = -FLT_MAX, emin = FLT_MAX, dmax = 0.0f;
+        ArgRed ex2 = mx, en2 = mn;     // the thread's second largest / smallest (exact path)
+        float dmax = 0.0f;
         if (exact) {
             for (int i = tid; i < n; i += BS) {
                 float4 r = qr[i], v = qv[i];
@@ -788,14 +905,16 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                     pot[i] = p;
                 }
                 float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-                emax = fmaxf(emax, E);
-                emin = fminf(emin, E);
+                keep_top2(mx, ex2, E, i);
+                keep_bot2(mn, en2, E, i);
                 dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
             }
         } else {
             const float wx = S.s_w[0], wy = S.s_w[1], wz = S.s_w[2];
             const float gms = fmul(A.G, rs.w) * A.scale;   // the removed member's G m 2^S
             const bool sub = have && A.subpot;
+            float ddmx = 0.0f, pemx = 0.0f;
+            ArgRed mx2{-FLT_MAX, 0x7fffffff}, mn2{FLT_MAX, 0x7fffffff};
             // RB members per thread per batch, all loaded before any is used,
             // so their memory latencies overlap
             constexpr int RB = BS >= 1024 ? 2 : 4;
@@ -817,15 +936,92 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                         p[k] -= fx(fmul(gms, pair_dir(d2, fadd(es, w[k].w), A.plummer)), 1.0f);
                         pot[i] = p[k];
                     }
-                    float dx = w[k].x - wx, dy = w[k].y - wy, dz = w[k].z - wz;
-                    float E = 0.5f * __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) - ll2f_fast(p[k]) * epot;
-                    if (E > mx.v) { mx.v = E; mx.i = i; }
-                    if (E < mn.v) { mn.v = E; mn.i = i; }
+                    const float dx = w[k].x - wx, dy = w[k].y - wy, dz = w[k].z - wz;
+                    const float dd = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+                    const float pe = ll2f_fast(p[k]) * epot;
+                    const float E = 0.5f * dd - pe;
+                    // the thread's two largest and two smallest, first index first
+                    if (E > mx.v) { mx2 = mx; mx.v = E; mx.i = i; }
+                    else if (E > mx2.v) { mx2.v = E; mx2.i = i; }
+                    if (E < mn.v) { mn2 = mn; mn.v = E; mn.i = i; }
+                    else if (E < mn2.v) { mn2.v = E; mn2.i = i; }
+                    ddmx = fmaxf(ddmx, dd);
+                    pemx = fmaxf(pemx, fabsf(pe));
+                }
+            }
+            // Filtered exact decisions, as for the smaller groups.  Bound on
+            // |E_i(FP32) - E_i(reference)|: with C = max |a v| + |aH r| over
+            // members plus the same for the centre, each component of
+            // w_i - W is within 2^-21 C of the reference's dv, so
+            // 2^-19 (C (sqrt(3 dd) + 3 C) + 1.5 dd + 2 |pe|) over the pass's
+            // largest dd and |pe| covers every member, several times over.
+            float tmax = mx.v, tmin = mn.v;
+            float a0 = tmax, a1 = tmin;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                a0 = fmaxf(a0, __shfl_xor_sync(SKID_FULL, a0, o));
+                a1 = fminf(a1, __shfl_xor_sync(SKID_FULL, a1, o));
+                ddmx = fmaxf(ddmx, __shfl_xor_sync(SKID_FULL, ddmx, o));
+                pemx = fmaxf(pemx, __shfl_xor_sync(SKID_FULL, pemx, o));
+            }
+            if (lane == 0) {
+                S.ext[w][0] = a0;
+                S.ext[w][1] = a1;
+                S.ext[w][2] = ddmx;
+                S.ext[w][3] = pemx;
+            }
+            __syncthreads();
+            float gmax = -FLT_MAX, gmin = FLT_MAX, gdd = 0.0f, gpe = 0.0f;
+            for (int k = 0; k < BS / 32; ++k) {
+                gmax = fmaxf(gmax, S.ext[k][0]);
+                gmin = fminf(gmin, S.ext[k][1]);
+                gdd = fmaxf(gdd, S.ext[k][2]);
+                gpe = fmaxf(gpe, S.ext[k][3]);
+            }
+            const float C = S.s_mg + S.s_mW;
+            const float bound =
+                1.9073486e-06f * (C * (1.7320509f * sqrtf(gdd) + 3.0f * C) + 1.5f * gdd + 2.0f * gpe) +
+                1e-30f;
+            const float hi = gmax - 2.0f * bound, lo = gmin + 2.0f * bound;
+            const ArgRed t1 = mx, b1 = mn;
+            mx = ArgRed{-FLT_MAX, 0x7fffffff};
+            mn = ArgRed{FLT_MAX, 0x7fffffff};
+            if ((tmax >= hi && mx2.v < hi) || (tmin <= lo && mn2.v > lo)) {
+                // usually only the thread's own extreme is a candidate: that
+                // one member exactly (when both its first and second are
+                // candidates on a side, the rescan below takes that side)
+                if (tmax >= hi && mx2.v < hi) {
+                    mx.v = exact_energy(A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, inv_d, opz_d);
+                    mx.i = t1.i;
+                }
+                if (tmin <= lo && mn2.v > lo) {
+                    mn.v = exact_energy(A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, inv_d, opz_d);
+                    mn.i = b1.i;
+                }
+            }
+            const bool scan_hi = tmax >= hi && mx2.v >= hi, scan_lo = tmin <= lo && mn2.v <= lo;
+            if (scan_hi || scan_lo) {
+                // this thread holds several candidates on a side: its members
+                // again, in the same order, with the same FP32 energies, the
+                // candidates exactly
+                for (int i = tid; i < n; i += BS) {
+                    const float4 wi = qw[i];
+                    const long long pi = pot[i];
+                    const float dx = wi.x - wx, dy = wi.y - wy, dz = wi.z - wz;
+                    const float E =
+                        0.5f * __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) - ll2f_fast(pi) * epot;
+                    const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
+                    if (ch || cl) {
+                        const float X = exact_energy(A, qr[i], qv[i], pi, dcm, inv_d, opz_d);
+                        if (ch && X > mx.v) { mx.v = X; mx.i = i; }
+                        if (cl && X < mn.v) { mn.v = X; mn.i = i; }
+                    }
                 }
             }
         }
         if (exact) {
             // filtered exact evaluation, as in warp_group
+            float emax = mx.v, emin = mn.v;
 #pragma unroll
             for (int o = 16; o; o >>= 1) {
                 emax = fmaxf(emax, __shfl_xor_sync(SKID_FULL, emax, o));
@@ -845,14 +1041,29 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 dmax = fmaxf(dmax, S.ext[k][2]);
             }
             const float hi = emax - 2.0f * dmax, lo = emin + 2.0f * dmax;
-            for (int i = tid; i < n; i += BS) {
-                float4 r = qr[i], v = qv[i];
-                long long p = pot[i];
-                float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-                if (E >= hi || E <= lo) {
-                    float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
-                    if (E >= hi && X > mx.v) { mx.v = X; mx.i = i; }
-                    if (E <= lo && X < mn.v) { mn.v = X; mn.i = i; }
+            const ArgRed t1 = mx, b1 = mn;
+            mx = ArgRed{-FLT_MAX, 0x7fffffff};
+            mn = ArgRed{FLT_MAX, 0x7fffffff};
+            if (t1.v >= hi && ex2.v < hi) {
+                mx.v = member_energy(true, A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, scm, inv_d, opz_d);
+                mx.i = t1.i;
+            }
+            if (b1.v <= lo && en2.v > lo) {
+                mn.v = member_energy(true, A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, scm, inv_d, opz_d);
+                mn.i = b1.i;
+            }
+            const bool scan_hi = ex2.v >= hi, scan_lo = en2.v <= lo;
+            if (scan_hi || scan_lo) {
+                for (int i = tid; i < n; i += BS) {
+                    float4 r = qr[i], v = qv[i];
+                    long long p = pot[i];
+                    float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
+                    const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
+                    if (ch || cl) {
+                        float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
+                        if (ch && X > mx.v) { mx.v = X; mx.i = i; }
+                        if (cl && X < mn.v) { mn.v = X; mn.i = i; }
+                    }
                 }
             }
         }
@@ -891,6 +1102,7 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                     }
                     for (int d = 0; d < 3; ++d)
                         S.s_w[d] = (float)((double)A.fShift * dcm[3 + d] + (double)A.fCosmo * dcm[d]);
+                    S.s_mW = centre_mag(A, dcm);
                     float4 rl = qr[nn], vl = qv[nn];
                     int il = qid[nn], ir = qid[ib];
                     long long pl = pot[nn], pb = pot[ib];

@@ -159,3 +159,53 @@ def test_unbind_large_groups_fp32_path(gpu_ready):
         og = r2["groups"]
         np.testing.assert_allclose(rec["fMass"][big], og["fMass"][big], rtol=1e-6)
         np.testing.assert_allclose(rec["vcm"][big], og["vcm"][big], rtol=1e-4, atol=1e-6)
+
+
+def test_unbind_isolated_config1_2e21(gpu_ready):
+    """Unbinding at the benchmarked size: the 2^21 clustered workload's
+    friends-of-friends groups and centres (from the GPU's own move phase) go
+    into the GPU's unbind-only path and the oracle's; both must unbind
+    exactly the same particles.  Hundreds of its groups hold more than 1024
+    members (up to about 10^4, with hundreds of removals each), so this
+    covers the staged FP32-filtered removal path at scale, every pair factor
+    against the oracle's FP64 one, and the scoop terms."""
+    from skid_gb300 import gpu, pipeline
+    snap, opts, ref, counts, meta = gc.load("config1_2e21")
+    with _ctx(opts) as ctx:
+        ctx.set_particles(snap)
+        ctx.scatter_active(opts.bGasAndDark, opts.bGasOnly)
+        ctx.density()
+        na = ctx.init_move(opts.fDensMin, opts.fTempMax, opts.fMassMax, opts.bGasAndDark,
+                           opts.bGasOnly)
+        ctx.move_step(opts.fStep, True, opts.bNoScatterCut)
+        while na:
+            na, _ = ctx.move_iterate(opts.fStep, opts.fCvg, opts.bNoScatterCut)
+        ng = ctx.fof(opts.fTau)
+        ctx.reactivate_move()
+        for _ in range(pipeline.PRUNE_STEPS):
+            ctx.move_step(np.float32(pipeline.MICRO_STEP * opts.fStep), False, opts.bNoScatterCut)
+        ctx.group_centers()
+        grp0, rec0 = ctx.get_groups(ng)
+    assert ng == counts["nGroupFoF"]
+    sizes = np.bincount(grp0, minlength=ng + 1)[1:]
+    assert np.count_nonzero(sizes > 1024) >= 100
+    centers = np.concatenate([rec0["rCenter"][1:], rec0["vcm"][1:]], axis=1)
+    r2 = oracle.run_unbind(snap, opts, grp0, centers, stop_after=2)
+    cen = np.zeros(ng + 1, gpu.GROUP_DTYPE)
+    cen["rCenter"] = rec0["rCenter"]
+    cen["vcm"] = rec0["vcm"]
+    with _ctx(opts) as ctx:
+        ctx.set_particles(snap)
+        ctx.set_groups(grp0, cen)
+        nu = ctx.unbind(opts.iSoftType, opts.fScoop, opts.bGasAndDark, opts.bNoUnbind,
+                        opts.nMaxMembers, opts.G, opts.z, opts.a_shift, opts.a_hubble)
+        grp, rec = ctx.get_groups(ng)
+    big = np.nonzero(sizes > 1024)[0] + 1
+    lost_big = int(np.sum(sizes[big - 1] - np.bincount(r2["grp"], minlength=ng + 1)[big]))
+    assert lost_big > 10000
+    assert nu == r2["nUnbound"]
+    assert np.array_equal(grp, r2["grp"])
+    og = r2["groups"]
+    keep = og["nMembers"][1:] > 0
+    np.testing.assert_allclose(rec["fMass"][1:][keep], og["fMass"][1:][keep], rtol=1e-6)
+    assert np.abs(rec["rBound"][1:][keep] - og["rBound"][1:][keep]).max() < 1e-5
