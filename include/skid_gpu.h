@@ -105,6 +105,20 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
  * counterpart: the reference reads its input once). */
 int skid_restart(skid_ctx *ctx);
 
+/* The snapshot straight from its TIPSY particle records (kdReadTipsy,
+ * kd.c:122-222): `records` holds the nGas gas (12 words), nDark dark (9)
+ * and nStar star (11) records that follow the header, in file order, XDR
+ * big-endian when bStandard.  One copy to the device and a kernel unpacks
+ * them (pinned host memory from skid_host_alloc makes the copy a single
+ * DMA).  bytes must equal the records' size exactly. */
+int skid_set_tipsy(skid_ctx *ctx, int nGas, int nDark, int nStar, double time, int bStandard,
+                   const void *records, size_t bytes);
+
+/* Page-locked host memory for input buffers (no context needed); returns
+ * SKID_ENOMEM where it cannot be had (no device), *ptr = NULL. */
+int skid_host_alloc(size_t bytes, void **ptr);
+int skid_host_free(void *ptr);
+
 /* kdScatterActive (kd.c:669-693) with ScatterCriterion (kd.c:600-627). */
 int skid_scatter_active(skid_ctx *ctx, int bGasAndDark, int bGasOnly, int *nScatter);
 
@@ -167,6 +181,29 @@ int skid_too_small(skid_ctx *ctx, int nMembers, int *nGroup);
  * (kdWriteGroup, kd.c:1611-1687; fRadius computed here).  groups has room
  * for nGroup+1 records (index 0 = ungrouped).  Either may be NULL. */
 int skid_get_groups(skid_ctx *ctx, int *grp, skid_group *groups);
+
+/* Per-group columns 2-12 of the .stat table (kdOutStats, kd.c:1703-1839),
+ * computed on the device after skid_too_small with the reference's own
+ * float and FP64 roundings.  The reference prints sqrt of the three
+ * fVcirc2 values and of fROuter2 (kd.c:1819-1833); columns 13-21 are the
+ * records' rCenter, vcm and rBound. */
+typedef struct skid_stat {
+    int nMembers;
+    float fTotMass, fGasMass, fStarMass;
+    float fVcirc2Max;    /* G M(<r)/r at its maximum outside 2 eps (fVcirc)     */
+    float fVcirc2Half;   /* G M/r where the enclosed mass first exceeds half    */
+    float fVcirc2Outer;  /* G M/r at the outermost member (flVcirc)              */
+    float fRVmax, fRHalf;
+    float fROuter2;      /* squared radius of the outermost member              */
+    float fVdisp;        /* 1-D velocity dispersion, Hubble flow included       */
+} skid_stat;
+
+/* kdOutStats' per-group statistics for groups 1..nGroup (stats[0] unused;
+ * stats holds nGroup+1 records).  G, fExp = 1/(1+z) and fExpHub = a H(a) as
+ * for skid_unbind; fDensMin and fTempMax select the gas mass that counts.
+ * Replaces kd.c:1703-1839 (the file writing stays with the caller). */
+int skid_group_stats(skid_ctx *ctx, float G, float fExp, float fExpHub, float fDensMin,
+                     float fTempMax, skid_stat *stats);
 
 /* Moved positions by iOrder (kdOutVector's data, kd.c:1550-1608); input
  * position for particles that never moved. */

@@ -209,6 +209,9 @@ struct skid_ctx {
     skid::DBuf<float4> probe_p4;
     skid::DBuf<int> probe_i, probe_i2;
     skid::DBuf<unsigned char> probe_t;
+    skid::DBuf<uint32_t> tipsy_raw;   // TIPSY record words as read (skid_set_tipsy)
+    skid::DBuf<int> stat_start;      // .stat: first sorted slot of each group
+    skid::DBuf<skid_stat> stat_out;  // .stat: per-group columns
     skid::DBuf<float> split_acc;     // field parts of split movers
     skid::DBuf<int> split_cnt;       // parts finished per split mover (zero between steps)
 
@@ -375,7 +378,7 @@ struct skid_ctx {
         dfree(ss.k0); dfree(ss.k1); dfree(ss.v0); dfree(ss.v1); dfree(ss.hist); dfree(ss.blk);
         dfree(ss.box);
         dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);
-        dfree(probe_t); dfree(knn_heap); dfree(split_acc); dfree(split_cnt); dfree(ms_dev);
+        dfree(probe_t); dfree(stat_start); dfree(stat_out); dfree(tipsy_raw); dfree(knn_heap); dfree(split_acc); dfree(split_cnt); dfree(ms_dev);
         dfree(adj.win); dfree(adj.w); dfree(adj.g); dfree(adj.out); dfree(adj.nbr); dfree(adj.ncnt);
         dfree(adj.items); dfree(adj.gsel); dfree(adj.v); dfree(adj.E);
         std::lock_guard<std::recursive_mutex> lk(skid::device_mutex());

@@ -72,6 +72,11 @@ GROUP_DTYPE = np.dtype([("nMembers", "<i4"), ("fMass", "<f4"), ("rel", "<f4", 3)
                         ("rCenter", "<f4", 3), ("rBound", "<f4", 3), ("vcm", "<f4", 3),
                         ("fRadius", "<f4")])
 assert GROUP_DTYPE.itemsize == C.sizeof(Group)
+# skid_stat (kdOutStats' per-group columns)
+STAT_DTYPE = np.dtype([("nMembers", "<i4"), ("fTotMass", "<f4"), ("fGasMass", "<f4"),
+                       ("fStarMass", "<f4"), ("fVcirc2Max", "<f4"), ("fVcirc2Half", "<f4"),
+                       ("fVcirc2Outer", "<f4"), ("fRVmax", "<f4"), ("fRHalf", "<f4"),
+                       ("fROuter2", "<f4"), ("fVdisp", "<f4")])
 
 _I = C.POINTER(C.c_int)
 _F = C.POINTER(C.c_float)
@@ -100,6 +105,7 @@ SIGNATURES = {
                     C.c_float, C.c_float, _I],
     "skid_too_small": [_V, C.c_int, _I],
     "skid_get_groups": [_V, _I, C.c_void_p],
+    "skid_group_stats": [_V, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p],
     "skid_get_moved": [_V, _F],
     "skid_get_final_density": [_V, _F],
     "skid_get_timings": [_V, C.POINTER(Timings)],
@@ -328,6 +334,13 @@ class Context:
         rec = np.zeros(ngroups + 1, GROUP_DTYPE)
         self._call("skid_get_groups", self.h, _i(grp), rec.ctypes.data_as(C.c_void_p))
         return grp, rec
+
+    def group_stats(self, ngroups: int, G, fExp, fExpHub, fDensMin, fTempMax):
+        """kdOutStats' per-group columns (skid_stat records, index 0 unused)."""
+        out = np.zeros(ngroups + 1, STAT_DTYPE)
+        self._call("skid_group_stats", self.h, float(G), float(fExp), float(fExpHub),
+                   float(fDensMin), float(fTempMax), out.ctypes.data_as(C.c_void_p))
+        return out
 
     def get_moved(self):
         out = np.empty((self.n, 3), np.float32)

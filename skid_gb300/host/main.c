@@ -168,101 +168,36 @@ static void die_on(int rc, const char *what)
     exit(2);
 }
 
-/* ---- .stat: per-group statistics (kdOutStats, kd.c:1703-1839) ---- */
+/* ---- .stat: per-group statistics (kdOutStats, kd.c:1703-1839) ----
+ * The statistics are computed on the device (skid_group_stats); the host
+ * prints them in the reference's format, with sqrt of the squared columns
+ * taken in double as the reference's printf arguments are. */
 
-typedef struct stat_item {
-    float r2, r[3];
-    int io;
-} stat_item;
-
-static int cmp_stat(const void *pa, const void *pb)
+static int write_stats(const char *path, const options *o, skid_ctx *ctx, const skid_group *gr,
+                       int nGroup)
 {
-    const stat_item *a = pa, *b = pb;
-    if (a->r2 != b->r2) return a->r2 < b->r2 ? -1 : 1;
-    return (a->io > b->io) - (a->io < b->io);
-}
-
-static int particle_type(const snapshot *s, int io)
-{
-    return io < s->nGas ? T_GAS : (io < s->nGas + s->nDark ? T_DARK : T_STAR);
-}
-
-static int write_stats(const char *path, const options *o, const snapshot *s, const int *grp,
-                       const skid_group *gr, int nGroup, const float *rho)
-{
-    FILE *fp = fopen(path, "w");
-    if (!fp) return -1;
     float fExp, fExpHub;
     expansion(o, &fExp, &fExpHub);
-    float h[3];
-    for (int d = 0; d < 3; ++d) h[d] = (float)(0.5 * (double)o->period[d]);
-    /* members of each group, counting sort by group id */
-    int *start = calloc((size_t)nGroup + 2, sizeof(int));
-    int *order = malloc((size_t)(s->n > 0 ? s->n : 1) * sizeof(int));
-    for (int i = 0; i < s->n; ++i) start[grp[i] + 1]++;
-    for (int g = 0; g <= nGroup; ++g) start[g + 1] += start[g];
-    int *fill = malloc(((size_t)nGroup + 1) * sizeof(int));
-    memcpy(fill, start, ((size_t)nGroup + 1) * sizeof(int));
-    for (int i = 0; i < s->n; ++i) order[fill[grp[i]]++] = i;
-    stat_item *q = malloc((size_t)(s->n > 0 ? s->n : 1) * sizeof(stat_item));
-    for (int g = 1; g <= nGroup; ++g) {
-        int n = start[g + 1] - start[g];
-        if (n <= 0) continue;
-        const skid_group *G = &gr[g];
-        for (int j = 0; j < n; ++j) {
-            int io = order[start[g] + j];
-            float r2 = 0.0f;
-            for (int d = 0; d < 3; ++d) {
-                float dx = s->pos[3 * (size_t)io + d] - G->rCenter[d];
-                if (dx > h[d]) dx -= 2 * h[d];
-                if (dx <= -h[d]) dx += 2 * h[d];
-                q[j].r[d] = dx;
-                r2 += dx * dx;
-            }
-            q[j].r2 = r2;
-            q[j].io = io;
-        }
-        qsort(q, (size_t)n, sizeof(stat_item), cmp_stat);
-        float fHalf = 0.0f;
-        for (int j = 0; j < n; ++j) fHalf += (float)(0.5 * s->mass[q[j].io]);
-        float fTot = 0, fGas = 0, fStar = 0, fVc = 0, fmVc = 0, fVdisp = 0, fRVmax = 0, fRh = 0;
-        for (int j = 0; j < n; ++j) {
-            int io = q[j].io;
-            float m = s->mass[io], soft = s->soft[io];
-            fTot += m;
-            if (q[j].r2 > 4.0 * soft * soft && o->G * fTot / sqrt(q[j].r2) > fVc) {
-                fRVmax = (float)sqrt(q[j].r2);
-                fVc = o->G * fTot / fRVmax;
-            }
-            int t = particle_type(s, io);
-            float r = rho ? rho[io] : 0.0f;
-            if (t == T_GAS && r >= o->fDensMin && s->temp[io] <= o->fTempMax) fGas += m;
-            if (t == T_STAR) fStar += m;
-            if (fTot > fHalf && fmVc == 0.0f) {
-                fRh = (float)sqrt(q[j].r2);
-                fmVc = o->G * fTot / fRh;
-            }
-            for (int d = 0; d < 3; ++d) {
-                float dv = fExp * (s->vel[3 * (size_t)io + d] - G->vcm[d]) + fExpHub * q[j].r[d];
-                fVdisp += dv * dv;
-            }
-        }
-        float rout2 = q[n - 1].r2;
-        float flVc = (float)(o->G * fTot / sqrt(rout2));
-        if (fVc == 0.0f) {
-            fVc = flVc;
-            fRVmax = (float)sqrt(rout2);
-        }
-        fVdisp = (float)sqrt(fVdisp / (3.0 * n));
-        fprintf(fp, "%d %d %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g\n", g, n,
-                fTot, fGas, fStar, sqrt(fVc), sqrt(fmVc), sqrt(flVc), fRVmax, fRh, sqrt(rout2),
-                fVdisp, G->rCenter[0], G->rCenter[1], G->rCenter[2], G->vcm[0], G->vcm[1],
-                G->vcm[2], G->rBound[0], G->rBound[1], G->rBound[2]);
+    skid_stat *st = malloc(((size_t)nGroup + 1) * sizeof(skid_stat));
+    if (!st) return -1;
+    die_on(skid_group_stats(ctx, o->G, fExp, fExpHub, o->fDensMin, o->fTempMax, st),
+           "skid_group_stats");
+    FILE *fp = fopen(path, "w");
+    if (!fp) {
+        free(st);
+        return -1;
     }
-    free(q);
-    free(fill);
-    free(order);
-    free(start);
+    for (int g = 1; g <= nGroup; ++g) {
+        const skid_stat *q = &st[g];
+        const skid_group *G = &gr[g];
+        if (q->nMembers <= 0) continue;
+        fprintf(fp, "%d %d %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g %g\n", g,
+                q->nMembers, q->fTotMass, q->fGasMass, q->fStarMass, sqrt(q->fVcirc2Max),
+                sqrt(q->fVcirc2Half), sqrt(q->fVcirc2Outer), q->fRVmax, q->fRHalf,
+                sqrt(q->fROuter2), q->fVdisp, G->rCenter[0], G->rCenter[1], G->rCenter[2],
+                G->vcm[0], G->vcm[1], G->vcm[2], G->rBound[0], G->rBound[1], G->rBound[2]);
+    }
+    free(st);
     return fclose(fp) ? -1 : 0;
 }
 
@@ -321,12 +256,21 @@ int main(int argc, char **argv)
     options o;
     parse(argc, argv, &o);
     printf("SKID v1.4.1 (GB300)\n");
-    snapshot s;
+    /* the particle records as they lie in the file, in page-locked memory;
+     * they are unpacked on the device (skid_set_tipsy) */
+    tipsy_raw raw;
     char err[512];
-    if (tipsy_read(stdin, o.bStandard, &s, err, sizeof(err))) {
+    if (tipsy_read_raw(stdin, o.bStandard, &raw, err, sizeof(err))) {
         fprintf(stderr, "skid: %s\n", err);
         return 2;
     }
+    snapshot s;
+    memset(&s, 0, sizeof(s));
+    s.time = raw.time;
+    s.nGas = raw.nGas;
+    s.nDark = raw.nDark;
+    s.nStar = raw.nStar;
+    s.n = raw.n;
     printf("nDark:%d nGas:%d nStar:%d\n", s.nDark, s.nGas, s.nStar);
     fflush(stdout);
 
@@ -341,9 +285,14 @@ int main(int argc, char **argv)
     par.device = 0;
     die_on(skid_create(&g_ctx, &par), "skid_create");
     skid_ctx *ctx = g_ctx;
-    die_on(skid_set_particles(ctx, s.nGas, s.nDark, s.nStar, s.time, s.pos, s.vel, s.mass, s.soft,
-                              s.temp),
-           "skid_set_particles");
+    die_on(skid_set_tipsy(ctx, raw.nGas, raw.nDark, raw.nStar, raw.time, o.bStandard, raw.records,
+                          raw.bytes),
+           "skid_set_tipsy");
+    if (o.bOutRay) {   /* the initial positions, for the displacements */
+        s.pos = malloc(3 * (size_t)(s.n > 0 ? s.n : 1) * sizeof(float));
+        tipsy_raw_positions(&raw, o.bStandard, s.pos);
+    }
+    tipsy_raw_free(&raw);
 
     int nFoF = 0;
     int inType = (s.nDark ? T_DARK : 0) | (s.nGas ? T_GAS : 0) | (s.nStar ? T_STAR : 0);
@@ -448,15 +397,8 @@ int main(int argc, char **argv)
         free(flag);
     }
     if (o.bOutStats) {
-        float *rho = NULL;
-        if (!o.bUnbindOnly) {
-            rho = malloc((size_t)(s.n > 0 ? s.n : 1) * sizeof(float));
-            die_on(skid_get_final_density(ctx, rho), "skid_get_final_density");
-        }
         snprintf(path, sizeof(path), "%s.stat", o.achName);
-        if (write_stats(path, &o, &s, grp, gr, nGroup, rho))
-            fprintf(stderr, "skid: cannot write %s\n", path);
-        free(rho);
+        if (write_stats(path, &o, ctx, gr, nGroup)) fprintf(stderr, "skid: cannot write %s\n", path);
     }
     skid_timings t;
     die_on(skid_get_timings(ctx, &t), "skid_get_timings");

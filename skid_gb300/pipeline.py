@@ -30,7 +30,7 @@ class Result:
     groups: np.ndarray           # gpu.GROUP_DTYPE records, index 0 = ungrouped
     n_group: int
     rho: np.ndarray | None       # initial densities (for .den)
-    rho_final: np.ndarray | None # densities after the first-step cut (for .stat)
+    stats: np.ndarray | None     # gpu.STAT_DTYPE per-group .stat columns (device)
     moved: np.ndarray | None     # moved positions (for .ray)
     counts: dict
     timings: dict
@@ -116,10 +116,13 @@ def run(snap: tipsy.Snapshot, opts: Options, ctx: gpu.Context | None = None, log
         counts["nGroup"] = ng
         grp, rec = ctx.get_groups(ng)
         say(f"Number of Groups:{ng}")
-        rho_final = ctx.get_final_density() if (opts.bOutStats and not opts.bUnbindOnly) else None
+        stats = None
+        if opts.bOutStats:
+            stats = ctx.group_stats(ng, opts.G, opts.a_shift, opts.a_hubble, opts.fDensMin,
+                                    opts.fTempMax)
         tm = ctx.timings()
         tm["wall_s"] = time.perf_counter() - t0
-        return Result(grp, rec, ng, rho, rho_final, moved, counts, tm, lines)
+        return Result(grp, rec, ng, rho, stats, moved, counts, tm, lines)
     finally:
         if own:
             ctx.close()
@@ -150,9 +153,9 @@ def read_unbind_inputs(opts: Options, snap: tipsy.Snapshot):
 # ---------------------------------------------------------------------------
 # output files
 
-def _g(x) -> str:
-    """printf %g."""
-    return "%g" % x
+def _fmt_lines(fmt: str, values) -> str:
+    """One printf-formatted value per line (numpy's vectorised formatting)."""
+    return "".join(np.char.add(np.char.mod(fmt, np.asarray(values, np.float64)), "\n"))
 
 
 def write_outputs(res: Result, snap: tipsy.Snapshot, opts: Options, outdir: str = ".") -> list:
@@ -172,13 +175,13 @@ def write_outputs(res: Result, snap: tipsy.Snapshot, opts: Options, outdir: str 
     if opts.bOutDens and res.rho is not None:
         with open(base + ".den", "w") as f:
             f.write(f"{snap.n}\n")
-            f.write("".join("%.10g\n" % float(r) for r in res.rho))
+            f.write(_fmt_lines("%.10g", res.rho))
         written.append(base + ".den")
     if opts.bOutRay and res.moved is not None:
         write_ray(base + ".ray", res.moved, snap, opts)
         written.append(base + ".ray")
-    if opts.bOutStats:
-        write_stats(base + ".stat", res, snap, opts)
+    if opts.bOutStats and res.stats is not None:
+        write_stats(base + ".stat", res)
         written.append(base + ".stat")
     return written
 
@@ -192,73 +195,32 @@ def write_ray(path, moved, snap, opts):
             dx = (moved[:, d] - snap.pos[:, d]).astype(np.float32)
             dx = np.where(dx > h, dx - np.float32(2) * h, dx).astype(np.float32)
             dx = np.where(dx <= -h, dx + np.float32(2) * h, dx).astype(np.float32)
-            f.write("".join(_g(float(x)) + "\n" for x in dx))
+            f.write(_fmt_lines("%g", dx))
 
 
-def group_stats(res: Result, snap: tipsy.Snapshot, opts: Options):
-    """kdOutStats (kd.c:1703-1839): 21 columns per group."""
-    G = np.float32(opts.G)
-    fexp = np.float32(opts.a_shift)
-    fexphub = np.float32(opts.a_hubble)
-    h = [np.float32(0.5 * opts.period[d]) for d in range(3)]
-    rho = res.rho_final if res.rho_final is not None else np.zeros(snap.n, np.float32)
-    order = np.argsort(res.grp, kind="stable")
-    bounds = np.searchsorted(res.grp[order], np.arange(res.n_group + 2))
-    n_gas, n_dark = snap.n_gas, snap.n_dark
+def stat_rows(res: Result) -> np.ndarray:
+    """The .stat table (kdOutStats, kd.c:1819-1833) as float64 rows: the
+    device's per-group columns, sqrt of the squared ones taken in double as
+    the reference's printf arguments are, and the records' centre, vcm and
+    most bound particle."""
     rows = []
     for g in range(1, res.n_group + 1):
-        idx = order[bounds[g]:bounds[g + 1]]
-        n = len(idx)
-        rec = res.groups[g]
-        q = np.empty((n, 3), np.float32)
-        for d in range(3):
-            dx = (snap.pos[idx, d] - rec["rCenter"][d]).astype(np.float32)
-            dx = np.where(dx > h[d], dx - np.float32(2) * h[d], dx).astype(np.float32)
-            dx = np.where(dx <= -h[d], dx + np.float32(2) * h[d], dx).astype(np.float32)
-            q[:, d] = dx
-        r2 = ((q[:, 0] * q[:, 0] + q[:, 1] * q[:, 1]).astype(np.float32) + q[:, 2] * q[:, 2]).astype(np.float32)
-        srt = np.argsort(r2, kind="stable")
-        idx, q, r2 = idx[srt], q[srt], r2[srt]
-        m = snap.mass[idx]
-        half = np.float32(0.0)
-        for mj in m:
-            half = np.float32(half + np.float32(0.5) * mj)
-        tot = gasm = starm = vc = mvc = vdisp = np.float32(0.0)
-        rvmax = rhm = np.float32(0.0)
-        for j in range(n):
-            tot = np.float32(tot + m[j])
-            soft = snap.soft[idx[j]]
-            if r2[j] > np.float32(4.0) * soft * soft and G * tot / np.float32(math.sqrt(r2[j])) > vc:
-                rvmax = np.float32(math.sqrt(r2[j]))
-                vc = np.float32(G * tot / rvmax)
-            io = idx[j]
-            t = GAS if io < n_gas else (DARK if io < n_gas + n_dark else STAR)
-            if t == GAS and rho[io] >= opts.fDensMin and snap.temp[io] <= opts.fTempMax:
-                gasm = np.float32(gasm + m[j])
-            if t == STAR:
-                starm = np.float32(starm + m[j])
-            if tot > half and mvc == 0.0:
-                rhm = np.float32(math.sqrt(r2[j]))
-                mvc = np.float32(G * tot / rhm)
-            for d in range(3):
-                dv = np.float32(fexp * (snap.vel[io, d] - rec["vcm"][d]) + fexphub * q[j, d])
-                vdisp = np.float32(vdisp + dv * dv)
-        rout = np.float32(math.sqrt(r2[n - 1]))
-        lvc = np.float32(G * tot / rout)
-        if vc == 0.0:
-            vc = lvc
-            rvmax = rout
-        vdisp = np.float32(math.sqrt(vdisp / (3.0 * n)))
-        rows.append((g, n, tot, gasm, starm, math.sqrt(vc), math.sqrt(mvc), math.sqrt(lvc), rvmax,
-                     rhm, rout, vdisp, *rec["rCenter"], *rec["vcm"], *rec["rBound"]))
-    return rows
+        q = res.stats[g]
+        r = res.groups[g]
+        if q["nMembers"] <= 0:
+            continue
+        rows.append([g, q["nMembers"], q["fTotMass"], q["fGasMass"], q["fStarMass"],
+                     math.sqrt(q["fVcirc2Max"]), math.sqrt(q["fVcirc2Half"]),
+                     math.sqrt(q["fVcirc2Outer"]), q["fRVmax"], q["fRHalf"],
+                     math.sqrt(q["fROuter2"]), q["fVdisp"], *r["rCenter"], *r["vcm"],
+                     *r["rBound"]])
+    return np.asarray(rows, np.float64).reshape(-1, 21)
 
 
-def write_stats(path, res, snap, opts):
-    rows = group_stats(res, snap, opts)
+def write_stats(path, res):
     with open(path, "w") as f:
-        for r in rows:
-            f.write(f"{r[0]} {r[1]} " + " ".join(_g(float(x)) for x in r[2:]) + "\n")
+        for r in stat_rows(res):
+            f.write(f"{int(r[0])} {int(r[1])} " + " ".join("%g" % float(x) for x in r[2:]) + "\n")
 
 
 def main(argv=None) -> int:

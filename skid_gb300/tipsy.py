@@ -159,7 +159,9 @@ def read_grp(path) -> np.ndarray:
 def write_grp(path, grp: np.ndarray) -> None:
     with open(path, "w") as f:
         f.write(f"{len(grp)}\n")
-        f.write("".join(f"{int(g)}\n" for g in grp))
+        if len(grp):
+            f.write("\n".join(map(str, np.asarray(grp).tolist())))
+            f.write("\n")
 
 
 def read_den(path) -> np.ndarray:

@@ -19,6 +19,8 @@ pytestmark = pytest.mark.gpu
 def test_pipeline_vs_reference(gpu_ready, name):
     from skid_gb300 import pipeline
     snap, opts, ref, counts, meta = gc.load(name)
+    if "stat" in ref:
+        opts.bOutStats = True
     res = pipeline.run(snap, opts, want_density=True)
     if "nExtraScat" in counts:
         assert f"nExtraScat:{counts['nExtraScat']}" in res.lines
@@ -26,6 +28,14 @@ def test_pipeline_vs_reference(gpu_ready, name):
     assert res.counts["nGroup"] == counts["nGroup"]
     assert abs(res.counts["nUnbound"] - counts["nUnbound"]) <= max(2, 0.001 * snap.n)
     gc.check_catalogue(res.grp, res.groups, ref, opts)
+    if "stat" in ref:
+        # the device's kdOutStats: every column agrees to float rounding
+        # when the membership is the reference's
+        st = pipeline.stat_rows(res)
+        assert st.shape == ref["stat"].shape
+        if np.array_equal(res.grp, ref["grp"]):
+            np.testing.assert_allclose(st[:, :2], ref["stat"][:, :2])
+            np.testing.assert_allclose(st[:, 2:], ref["stat"][:, 2:], rtol=2e-4, atol=2e-5)
     if "den" in ref:
         rel = np.abs(res.rho - ref["den"]) / np.maximum(ref["den"], 1e-30)
         assert rel[ref["den"] > 0].max() < 1e-5
