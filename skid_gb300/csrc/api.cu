@@ -494,12 +494,13 @@ __global__ void mass_soft_total(double *out)
     out[1] = e;
 }
 
-int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double time,
-                       const float *pos, const float *vel, const float *mass, const float *soft,
-                       const float *temp)
+}  // extern "C"
+
+namespace {
+
+// Common first half of a particle upload: counts, pipeline reset, buffers.
+int load_begin(skid_ctx *ctx, int nGas, int nDark, int nStar, double time)
 {
-    if (!ctx || nGas < 0 || nDark < 0 || nStar < 0 || !pos || !vel || !mass || !soft)
-        return SKID_EINVAL;
     long long nn = (long long)nGas + nDark + nStar;
     if (nn > (1ll << 28)) return ctx->fail(SKID_EINVAL);
     int n = (int)nn;
@@ -516,22 +517,21 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
     ctx->ms_pending = false;
     ctx->soft_changed = false;
     if (ctx->alloc_particles(n)) return ctx->fail(SKID_ENOMEM);
-    if (n == 0) { ctx->stage = STAGE_LOADED; return 0; }
-    if (dalloc(ctx->ms_dev, 2 * (size_t)MS_BLOCKS + 2)) return ctx->fail(SKID_ENOMEM);
-    // staging: raw host arrays -> device, then pack to float4 records
+    if (n > 0 && dalloc(ctx->ms_dev, 2 * (size_t)MS_BLOCKS + 2)) return ctx->fail(SKID_ENOMEM);
+    return 0;
+}
+
+// Common second half: the staged SoA arrays in ctx->raw (pos 3n, vel 3n,
+// mass n, soft n, temp n) packed into the float4 records, the potential
+// scale's reductions, and the per-particle outputs cleared.
+int load_finish(skid_ctx *ctx, bool have_temp)
+{
+    const int n = ctx->n;
     float *d_raw = ctx->raw.p;
-    size_t n3 = 3 * (size_t)n;
-    CK(cudaMemcpyAsync(d_raw, pos, n3 * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemcpyAsync(d_raw + n3, vel, n3 * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemcpyAsync(d_raw + 2 * n3, mass, n * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemcpyAsync(d_raw + 2 * n3 + n, soft, n * sizeof(float), cudaMemcpyHostToDevice,
-                       ctx->st));
-    if (temp)
-        CK(cudaMemcpyAsync(d_raw + 2 * n3 + 2 * (size_t)n, temp, n * sizeof(float),
-                           cudaMemcpyHostToDevice, ctx->st));
+    const size_t n3 = 3 * (size_t)n;
     pack_particles<<<grid_for(n), 256, 0, ctx->st>>>(d_raw, d_raw + n3, d_raw + 2 * n3,
                                                      d_raw + 2 * n3 + n,
-                                                     temp ? d_raw + 2 * n3 + 2 * (size_t)n : nullptr,
+                                                     have_temp ? d_raw + 2 * n3 + 2 * (size_t)n : nullptr,
                                                      n, ctx->pos4.p, ctx->vel4.p, ctx->temp.p); skid::note_launch();
     CK(cudaGetLastError());
     // total |mass| and smallest softening for the potential scale (fixed order)
@@ -543,9 +543,117 @@ int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double tim
     fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->rho_final.p, 0.0f, n); skid::note_launch();
     fill_float<<<grid_for(n), 256, 0, ctx->st>>>(ctx->ball2.p, -1.0f, n); skid::note_launch();
     CK(cudaMemsetAsync(ctx->grp.p, 0, n * sizeof(int), ctx->st));
-
     ctx->stage = STAGE_LOADED;
     return ctx->sync_check();
+}
+
+// TIPSY particle records (kd.c:164-217; tipsydefs.h:6-37), one thread per
+// particle: gas 12 words (mass pos vel rho temp hsmooth metals phi), dark 9
+// (mass pos vel eps phi), star 11 (mass pos vel metals tform eps phi), in
+// that order; XDR words are big-endian.  Writes the staged SoA arrays.
+__global__ void unpack_tipsy(const uint32_t *__restrict__ w, int nGas, int nDark, int n, int swap,
+                             float *__restrict__ pos, float *__restrict__ vel,
+                             float *__restrict__ mass, float *__restrict__ soft,
+                             float *__restrict__ temp)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        size_t off;
+        int isoft, itemp = -1;
+        if (i < nGas) {
+            off = 12 * (size_t)i;
+            isoft = 9;
+            itemp = 8;
+        } else if (i < nGas + nDark) {
+            off = 12 * (size_t)nGas + 9 * (size_t)(i - nGas);
+            isoft = 7;
+        } else {
+            off = 12 * (size_t)nGas + 9 * (size_t)nDark + 11 * (size_t)(i - nGas - nDark);
+            isoft = 9;
+        }
+        auto word = [&](int k) {
+            uint32_t v = __ldg(w + off + k);
+            return __uint_as_float(swap ? __byte_perm(v, 0, 0x0123) : v);
+        };
+        mass[i] = word(0);
+        pos[3 * (size_t)i] = word(1);
+        pos[3 * (size_t)i + 1] = word(2);
+        pos[3 * (size_t)i + 2] = word(3);
+        vel[3 * (size_t)i] = word(4);
+        vel[3 * (size_t)i + 1] = word(5);
+        vel[3 * (size_t)i + 2] = word(6);
+        soft[i] = word(isoft);
+        temp[i] = itemp >= 0 ? word(itemp) : 0.0f;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double time,
+                       const float *pos, const float *vel, const float *mass, const float *soft,
+                       const float *temp)
+{
+    if (!ctx || nGas < 0 || nDark < 0 || nStar < 0 || !pos || !vel || !mass || !soft)
+        return SKID_EINVAL;
+    if (int rc = load_begin(ctx, nGas, nDark, nStar, time)) return rc;
+    const int n = ctx->n;
+    if (n == 0) { ctx->stage = STAGE_LOADED; return 0; }
+    // staging: raw host arrays -> device, then pack to float4 records
+    float *d_raw = ctx->raw.p;
+    size_t n3 = 3 * (size_t)n;
+    CK(cudaMemcpyAsync(d_raw, pos, n3 * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_raw + n3, vel, n3 * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_raw + 2 * n3, mass, n * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_raw + 2 * n3 + n, soft, n * sizeof(float), cudaMemcpyHostToDevice,
+                       ctx->st));
+    if (temp)
+        CK(cudaMemcpyAsync(d_raw + 2 * n3 + 2 * (size_t)n, temp, n * sizeof(float),
+                           cudaMemcpyHostToDevice, ctx->st));
+    return load_finish(ctx, temp != nullptr);
+}
+
+int skid_set_tipsy(skid_ctx *ctx, int nGas, int nDark, int nStar, double time, int bStandard,
+                   const void *records, size_t bytes)
+{
+    if (!ctx || nGas < 0 || nDark < 0 || nStar < 0) return SKID_EINVAL;
+    const size_t want = 4 * (12 * (size_t)nGas + 9 * (size_t)nDark + 11 * (size_t)nStar);
+    if (bytes != want || (want && !records)) return ctx->fail(SKID_EINVAL);
+    if (int rc = load_begin(ctx, nGas, nDark, nStar, time)) return rc;
+    const int n = ctx->n;
+    if (n == 0) { ctx->stage = STAGE_LOADED; return 0; }
+    if (dalloc(ctx->tipsy_raw, want / 4)) return ctx->fail(SKID_ENOMEM);
+    CK(cudaMemcpyAsync(ctx->tipsy_raw.p, records, want, cudaMemcpyHostToDevice, ctx->st));
+    const uint32_t one = 1;
+    const bool little = *reinterpret_cast<const unsigned char *>(&one) == 1;
+    const int swap = (bStandard != 0) == little;   // XDR is big-endian
+    float *d_raw = ctx->raw.p;
+    const size_t n3 = 3 * (size_t)n;
+    unpack_tipsy<<<grid_for(n), 256, 0, ctx->st>>>(ctx->tipsy_raw.p, nGas, nDark, n, swap, d_raw,
+                                                   d_raw + n3, d_raw + 2 * n3, d_raw + 2 * n3 + n,
+                                                   d_raw + 2 * n3 + 2 * (size_t)n); skid::note_launch();
+    return load_finish(ctx, true);
+}
+
+int skid_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr) return SKID_EINVAL;
+    *ptr = nullptr;
+    if (cudaMallocHost(ptr, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return SKID_ENOMEM;
+    }
+    return 0;
+}
+
+int skid_host_free(void *ptr)
+{
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return SKID_ECUDA;
+    }
+    return 0;
 }
 
 __global__ void restore_soft(float4 *vel4, const float *soft, int n)

@@ -3,6 +3,8 @@
  */
 #include "tipsy_io.h"
 
+#include "skid_gpu.h"
+
 #include <errno.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -88,63 +90,71 @@ static int write_header(FILE *fp, int standard, double time, int nbodies, int ns
     return fwrite(raw, 1, 32, fp) == 32 ? 0 : -1;
 }
 
-int tipsy_read(FILE *fp, int standard, snapshot *s, char *err, size_t errlen)
+int tipsy_read_raw(FILE *fp, int standard, tipsy_raw *r, char *err, size_t errlen)
 {
-    memset(s, 0, sizeof(*s));
+    memset(r, 0, sizeof(*r));
     int cnt[5];
-    if (read_header(fp, standard, &s->time, cnt)) {
+    if (read_header(fp, standard, &r->time, cnt)) {
         snprintf(err, errlen, "truncated TIPSY header");
         return -1;
     }
-    /* cnt: nbodies, ndim, nsph, ndark, nstar */
-    s->nGas = cnt[2];
-    s->nDark = cnt[3];
-    s->nStar = cnt[4];
-    if (s->nGas < 0 || s->nDark < 0 || s->nStar < 0 ||
-        (long long)s->nGas + s->nDark + s->nStar > (1ll << 28)) {
+    r->nGas = cnt[2];
+    r->nDark = cnt[3];
+    r->nStar = cnt[4];
+    if (r->nGas < 0 || r->nDark < 0 || r->nStar < 0 ||
+        (long long)r->nGas + r->nDark + r->nStar > (1ll << 28)) {
         snprintf(err, errlen, "bad particle counts in TIPSY header (%d gas, %d dark, %d star)",
-                 s->nGas, s->nDark, s->nStar);
+                 r->nGas, r->nDark, r->nStar);
         return -1;
     }
-    int n = s->n = s->nGas + s->nDark + s->nStar;
-    size_t m = n > 0 ? (size_t)n : 1;
-    s->pos = malloc(3 * m * sizeof(float));
-    s->vel = malloc(3 * m * sizeof(float));
-    s->mass = malloc(m * sizeof(float));
-    s->soft = malloc(m * sizeof(float));
-    s->temp = calloc(m, sizeof(float));
-    if (!s->pos || !s->vel || !s->mass || !s->soft || !s->temp) {
-        tipsy_free(s);
+    r->n = r->nGas + r->nDark + r->nStar;
+    r->bytes = 4 * ((size_t)GAS_FLOATS * r->nGas + (size_t)DARK_FLOATS * r->nDark +
+                    (size_t)STAR_FLOATS * r->nStar);
+    size_t m = r->bytes ? r->bytes : 4;
+    if (skid_host_alloc(m, &r->records) == SKID_OK) {
+        r->pinned = 1;
+    } else {
+        r->records = malloc(m);
+        r->pinned = 0;
+    }
+    if (!r->records) {
         snprintf(err, errlen, "out of host memory");
         return -1;
     }
-    float rec[GAS_FLOATS];
-    for (int i = 0; i < n; ++i) {
-        int type = i < s->nGas ? 0 : (i < s->nGas + s->nDark ? 1 : 2);
-        int nf = type == 0 ? GAS_FLOATS : (type == 1 ? DARK_FLOATS : STAR_FLOATS);
-        if (read_words(fp, rec, (size_t)nf, standard)) {
-            snprintf(err, errlen, "truncated TIPSY particle records (particle %d of %d)", i, n);
-            tipsy_free(s);
-            return -1;
-        }
-        /* gas: mass pos[3] vel[3] rho temp hsmooth metals phi
-         * dark: mass pos[3] vel[3] eps phi
-         * star: mass pos[3] vel[3] metals tform eps phi */
-        s->mass[i] = rec[0];
-        for (int d = 0; d < 3; ++d) {
-            s->pos[3 * (size_t)i + d] = rec[1 + d];
-            s->vel[3 * (size_t)i + d] = rec[4 + d];
-        }
-        if (type == 0) {
-            s->temp[i] = rec[8];
-            s->soft[i] = rec[9];
-        } else if (type == 1) {
-            s->soft[i] = rec[7];
-        } else {
-            s->soft[i] = rec[9];
-        }
+    if (fread(r->records, 1, r->bytes, fp) != r->bytes) {
+        snprintf(err, errlen, "truncated TIPSY particle records");
+        tipsy_raw_free(r);
+        return -1;
     }
     return 0;
+}
+
+void tipsy_raw_free(tipsy_raw *r)
+{
+    if (r->pinned)
+        skid_host_free(r->records);
+    else
+        free(r->records);
+    memset(r, 0, sizeof(*r));
+}
+
+void tipsy_raw_positions(const tipsy_raw *r, int standard, float *pos)
+{
+    const unsigned char *b = r->records;
+    const int swap = standard == host_is_little();
+    for (int i = 0; i < r->n; ++i) {
+        size_t off = i < r->nGas ? 4 * (size_t)GAS_FLOATS * i
+                     : i < r->nGas + r->nDark
+                         ? 4 * ((size_t)GAS_FLOATS * r->nGas + (size_t)DARK_FLOATS * (i - r->nGas))
+                         : 4 * ((size_t)GAS_FLOATS * r->nGas + (size_t)DARK_FLOATS * r->nDark +
+                                (size_t)STAR_FLOATS * (i - r->nGas - r->nDark));
+        for (int d = 0; d < 3; ++d) {
+            uint32_t w;
+            memcpy(&w, b + off + 4 * (1 + d), 4);
+            if (swap) w = bswap32(w);
+            memcpy(&pos[3 * (size_t)i + d], &w, 4);
+        }
+    }
 }
 
 void tipsy_free(snapshot *s)

@@ -18,10 +18,24 @@ typedef struct snapshot {
     float *mass, *soft, *temp;
 } snapshot;
 
-/* Read a whole snapshot from fp (XDR big-endian when standard != 0).
- * Returns 0, or -1 with a message in err (size errlen). */
-int tipsy_read(FILE *fp, int standard, snapshot *s, char *err, size_t errlen);
+/* Frees the arrays a snapshot holds (NULL ones included). */
 void tipsy_free(snapshot *s);
+
+/* The header and the particle records as they lie in the file (XDR
+ * big-endian when standard != 0), for skid_set_tipsy: one fread of the
+ * whole record block into page-locked memory (skid_host_alloc; plain malloc
+ * where that is unavailable).  Returns 0, or -1 with a message in err. */
+typedef struct tipsy_raw {
+    double time;
+    int nGas, nDark, nStar, n;
+    void *records;
+    size_t bytes;
+    int pinned;
+} tipsy_raw;
+int tipsy_read_raw(FILE *fp, int standard, tipsy_raw *r, char *err, size_t errlen);
+void tipsy_raw_free(tipsy_raw *r);
+/* Decode the positions (3n floats, iOrder) of the raw records on the host. */
+void tipsy_raw_positions(const tipsy_raw *r, int standard, float *pos);
 
 /* .gtp: nGroup star records (mass, pos, vel, eps=radius, tform=time). */
 int tipsy_write_gtp(const char *path, int standard, double time, int nGroup,
