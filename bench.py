@@ -287,6 +287,43 @@ def cpu_baseline(steps=1):
             "catalogue": counts}
 
 
+def cli_process_wall(snap, repeats=3):
+    """The skid command-line tool as a user runs it: one process per run,
+    reading the TIPSY snapshot on stdin (the file read once beforehand, so it
+    is in the page cache) and writing .grp and .gtp.  Returns particles per
+    second of process wall time (best of `repeats`) and the stage split the
+    tool prints."""
+    import tempfile
+    from skid_gb300 import build, synth
+    exe = build.build_cli()
+    with tempfile.TemporaryDirectory() as tmp:
+        inp = os.path.join(tmp, "input.bin")
+        synth.write_snapshot(inp, snap)
+        with open(inp, "rb") as f:
+            f.read()
+        cmd = [exe, *flags(), "-o", "out"]
+        walls, out = [], ""
+        for _ in range(repeats):
+            t = time.perf_counter()
+            with open(inp, "rb") as f:
+                r = subprocess.run(cmd, stdin=f, cwd=tmp, capture_output=True, text=True)
+            walls.append(time.perf_counter() - t)
+            if r.returncode:
+                raise RuntimeError(f"skid CLI failed: {r.stderr[-400:]}")
+            out = r.stdout
+        files = sorted(f for f in os.listdir(tmp) if f.startswith("out."))
+    device = {}
+    for line in out.splitlines():
+        for key in ("Initial Density", "Moving Particles", "Friends of Friends", "Microstepping",
+                    "Unbinding"):
+            if line.strip().startswith(key + ":"):
+                device[key] = float(line.split(":")[1])
+    best = min(walls)
+    return {"value": snap.n / best, "unit": UNIT, "wall_s": best, "walls_s": walls,
+            "n_particles": snap.n, "files": files, "device_stage_ms": device,
+            "command": "skid_gb300/bin/skid " + " ".join(flags()) + " -o out < input.bin"}
+
+
 def reduce_max(x: float, world: int, device="cpu") -> float:
     """Max of x over ranks (the slowest replica sets the job's time)."""
     if world <= 1:
@@ -499,6 +536,7 @@ def run_gpu(args):
         ctx.close()
         return 0
     cpu = None if args.no_cpu_baseline else cpu_baseline()
+    cli = None if args.no_cli else cli_process_wall(snap)
     tm = res.timings
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -536,6 +574,8 @@ def run_gpu(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if cli:
+        line["cli_process"] = cli
     print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
@@ -675,6 +715,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT, help="particles (default 2^21)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cli", action="store_true",
+                    help="skip the skid command-line process wall-time runs")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain-form and -nsp comparison runs")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "mixed", "adjoint"],
