@@ -426,6 +426,7 @@ int skid_create(skid_ctx **pctx, const skid_params *par)
     cudaMemsetAsync(ctx->d_fbytes, 0, 2 * sizeof(double), ctx->st);
     cudaStreamSynchronize(ctx->st);
     ctx->d_status = (unsigned *)(ctx->d_scal + SC_STATUS);
+    ctx->ss.d_err = ctx->d_status;
     ctx->C.d_n = ctx->d_scal + SC_NC;
     ctx->C.d_n2 = ctx->d_scal + SC_NC2;
     ctx->C.d_floor = (unsigned *)(ctx->d_scal + SC_FLOOR);

@@ -375,7 +375,7 @@ struct skid_ctx {
         dfree(unfused_acc);
         dfree(U.usoft); dfree(U.pot_save); dfree(U.grp_save); dfree(U.order); dfree(U.rec_save);
         dfree(fof_minio); dfree(fof_flag); dfree(moved4);
-        dfree(ss.k0); dfree(ss.k1); dfree(ss.v0); dfree(ss.v1); dfree(ss.hist); dfree(ss.blk);
+        dfree(ss.k0); dfree(ss.k1); dfree(ss.v0); dfree(ss.v1); dfree(ss.hist); dfree(ss.glob); dfree(ss.blk);
         dfree(ss.box);
         dfree(probe_f); dfree(probe_acc); dfree(probe_p4); dfree(probe_i); dfree(probe_i2);
         dfree(probe_t); dfree(stat_start); dfree(stat_out); dfree(tipsy_raw); dfree(knn_heap); dfree(split_acc); dfree(split_cnt); dfree(ms_dev);

@@ -53,13 +53,18 @@ void dfree(DBuf<T> &b)
     b.n = 0;
 }
 
+// Words of SortScratch::glob: eight passes' digit offsets and tile counters.
+constexpr size_t SORT_GLOB_WORDS = 8 * 256 + 8;
+
 // Scratch for sorting and scans, sized for the largest point set.
 struct SortScratch {
     DBuf<uint64_t> k0, k1;
     DBuf<uint32_t> v0, v1;
-    DBuf<uint32_t> hist;   // per-block digit counts
+    DBuf<uint32_t> hist;   // per-tile look-back status of a sort pass (256 per tile)
+    DBuf<uint32_t> glob;   // SORT_GLOB_WORDS: digit offsets of every pass, tile counters
     DBuf<int> blk;         // per-block sums for scans
     DBuf<unsigned> box;    // bounding box (ordered uints)
+    unsigned *d_err = nullptr;   // status word a timed-out wait sets (may be null)
 };
 
 // A tree over a point set (kNN, gather, FoF, scoop).

@@ -55,7 +55,8 @@ constexpr size_t OFF_HI = align256(OFF_LO + sizeof(float4) * NA_NODES);
 constexpr size_t OFF_FLAG = align256(OFF_HI + sizeof(float4) * NA_NODES);
 constexpr size_t OFF_B2 = align256(OFF_FLAG + sizeof(int) * NA_NODES);
 constexpr size_t OFF_WORK = align256(OFF_B2 + sizeof(float) * NA_MAXN);
-constexpr size_t NA_BYTES = align256(OFF_WORK + sizeof(int) * 64);
+constexpr size_t OFF_GLOB = align256(OFF_WORK + sizeof(int) * 64);
+constexpr size_t NA_BYTES = align256(OFF_GLOB + sizeof(uint32_t) * SORT_GLOB_WORDS);
 
 static_assert((NA_LEAFBASE & (NA_LEAFBASE - 1)) == 0, "leaf count must be a power of two");
 static_assert(NA_BYTES < (8u << 20), "scratch must stay modest");
@@ -142,6 +143,7 @@ extern "C" int skid_knn_ball2_noalloc(const float *d_pos, int n, int k, const fl
     ss.v0 = view<uint32_t>(base, OFF_V0, NA_MAXN);
     ss.v1 = view<uint32_t>(base, OFF_V1, NA_MAXN);
     ss.hist = view<uint32_t>(base, OFF_HIST, 256 * (size_t)NA_TILES);
+    ss.glob = view<uint32_t>(base, OFF_GLOB, SORT_GLOB_WORDS);
     ss.blk = view<int>(base, OFF_BLK, 64);
     ss.box = view<unsigned>(base, OFF_BOX, 8);
     Tree t;

@@ -1,9 +1,17 @@
-// Stable LSD radix sort (8-bit digits) and device-wide exclusive scan.
+// Stable LSD radix sort (8-bit digits, one sweep per digit) and device-wide
+// exclusive scan.
 //
-// Each sort pass: (1) per-tile digit histograms, (2) one exclusive scan over
-// the digit-major count table, (3) a stable scatter that ranks keys inside
-// the tile with warp match + per-warp digit counts.  Tiles are 4096 keys
-// (256 threads x 16 rounds, round-major so tile order = input order).
+// The sort reads the keys once up front to count every digit position's
+// histogram (one kernel for all passes), turns them into global digit
+// offsets (one small kernel), then makes one kernel launch per 8-bit pass.
+// A pass takes tiles of 4096 keys (256 threads x 16 rounds, round-major so
+// tile order = input order) in the order blocks start (a tile counter), so
+// a tile's predecessors are always already running: it counts its digits,
+// publishes them, and finds the keys of each digit before it by decoupled
+// look-back over the predecessors' published counts (an aggregate, or an
+// inclusive prefix that ends the walk), then ranks its keys stably with warp
+// match and per-warp digit counts and scatters them.  Each look-back wait is
+// bounded; one that runs out sets the caller's status word.
 #include <atomic>
 
 #include "internal.h"
@@ -37,58 +45,141 @@ constexpr int RS_ROUNDS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
 constexpr int RS_WARPS = RS_THREADS / 32;
 
-__global__ void rs_histogram(const uint64_t *__restrict__ keys, int n, const int *d_n, int shift,
-                             int nTiles, uint32_t *__restrict__ hist)
+// ---- one-sweep passes ----
+constexpr int OS_WARPS = RS_WARPS;
+constexpr int OS_MAXPASS = 8;
+constexpr unsigned OS_AGG = 1u << 30;         // status: the tile's own digit count
+constexpr unsigned OS_PRE = 2u << 30;         // status: inclusive prefix up to the tile
+constexpr unsigned OS_VAL = (1u << 30) - 1u;
+constexpr int OS_SPIN_LIMIT = 1 << 24;
+
+// Digit histograms of every pass in one read of the keys, into glob[p*256+d].
+__global__ void os_histogram(const uint64_t *__restrict__ keys, int n, const int *d_n, int passes,
+                             uint32_t *__restrict__ glob)
 {
-    __shared__ uint32_t h[256];
-    if (d_n) n = min(n, *d_n);   // live count known only on the device
-    h[threadIdx.x] = 0;
+    __shared__ uint32_t h[OS_MAXPASS * 256];
+    if (d_n) n = min(n, *d_n);
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    int base = blockIdx.x * RS_TILE;
-    for (int r = 0; r < RS_ROUNDS; ++r) {
-        int i = base + r * RS_THREADS + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xff], 1u);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&h[p * 256 + (int)((k >> (8 * p)) & 0xff)], 1u);
     }
     __syncthreads();
-    hist[threadIdx.x * nTiles + blockIdx.x] = h[threadIdx.x];
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
+        if (h[i]) atomicAdd(&glob[i], h[i]);
 }
 
-__global__ void rs_scatter(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
-                           uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n,
-                           const int *d_n, int shift, int nTiles, const uint32_t *__restrict__ offs)
+// Histograms -> exclusive global offsets, one pass at a time (256 threads).
+__global__ void os_offsets(uint32_t *glob, int passes)
 {
+    __shared__ uint32_t ws[8];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    for (int p = 0; p < passes; ++p) {
+        const uint32_t x = glob[p * 256 + t];
+        uint32_t v = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(SKID_FULL, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane == 31) ws[w] = v;
+        __syncthreads();
+        uint32_t before = 0;
+        for (int j = 0; j < w; ++j) before += ws[j];
+        glob[p * 256 + t] = before + v - x;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(RS_THREADS)
+os_pass(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+        uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n, const int *d_n, int shift,
+        const uint32_t *__restrict__ goff, uint32_t *status, uint32_t *counter, unsigned *d_err)
+{
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t hist[256];
     __shared__ uint32_t run[256];
-    __shared__ uint32_t wcnt[RS_WARPS][256];
+    __shared__ uint32_t wcnt[OS_WARPS][256];
     if (d_n) n = min(n, *d_n);
-    if ((int)blockIdx.x * RS_TILE >= n) return;   // tile beyond the live keys
-    int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    run[tid] = offs[tid * nTiles + blockIdx.x];
-    for (int j = 0; j < RS_WARPS; ++j) wcnt[j][tid] = 0;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(counter, 1u);
+    hist[tid] = 0;
+#pragma unroll
+    for (int j = 0; j < OS_WARPS; ++j) wcnt[j][tid] = 0;
     __syncthreads();
-    int base = blockIdx.x * RS_TILE;
-    unsigned lt = (1u << lane) - 1u;
+    const int tile = (int)s_tile;
+    const int base = tile * RS_TILE;
+    if (base >= n) return;   // beyond the live keys (block-uniform)
+    uint64_t k[RS_ROUNDS];
+    uint32_t v[RS_ROUNDS];
+#pragma unroll
     for (int r = 0; r < RS_ROUNDS; ++r) {
-        int i = base + r * RS_THREADS + tid;
-        bool valid = i < n;
-        uint64_t k = valid ? kin[i] : 0;
-        uint32_t v = valid ? vin[i] : 0;
-        unsigned d = valid ? (unsigned)((k >> shift) & 0xff) : 256u + lane;  // unique for invalid
-        unsigned peers = __match_any_sync(SKID_FULL, d);
-        unsigned rank = __popc(peers & lt);
-        bool leader = (peers & lt) == 0;
-        if (valid && leader) wcnt[w][d] = __popc(peers);
+        const int i = base + r * RS_THREADS + tid;
+        k[r] = 0;
+        v[r] = 0;
+        if (i < n) {
+            k[r] = kin[i];
+            v[r] = vin[i];
+            atomicAdd(&hist[(k[r] >> shift) & 0xff], 1u);
+        }
+    }
+    __syncthreads();
+    {
+        // thread tid owns digit tid: publish, then look back
+        const uint32_t c = hist[tid];
+        uint32_t *mine = status + (size_t)tile * 256 + tid;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            atomicExch(mine, OS_PRE | c);
+        } else {
+            atomicExch(mine, OS_AGG | c);
+            int t = tile - 1, spins = 0;
+            for (;;) {
+                const uint32_t sv = *(volatile const uint32_t *)(status + (size_t)t * 256 + tid);
+                const uint32_t f = sv & ~OS_VAL;
+                if (f == 0u) {
+                    if (++spins > OS_SPIN_LIMIT) {
+                        if (d_err) atomicOr(d_err, ST_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                excl += sv & OS_VAL;
+                if (f == OS_PRE || t == 0) break;
+                --t;
+            }
+            atomicExch(mine, OS_PRE | (excl + c));
+        }
+        run[tid] = goff[tid] + excl;
+    }
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        const int i = base + r * RS_THREADS + tid;
+        const bool valid = i < n;
+        const unsigned d = valid ? (unsigned)((k[r] >> shift) & 0xff) : 256u + lane;
+        const unsigned peers = __match_any_sync(SKID_FULL, d);
+        const unsigned rank = __popc(peers & lt);
+        if (valid && (peers & lt) == 0) wcnt[w][d] = __popc(peers);
         __syncthreads();
         if (valid) {
             unsigned off = run[d] + rank;
             for (int j = 0; j < w; ++j) off += wcnt[j][d];
-            kout[off] = k;
-            vout[off] = v;
+            kout[off] = k[r];
+            vout[off] = v[r];
         }
         __syncthreads();
         {
-            unsigned s = 0;
-            for (int j = 0; j < RS_WARPS; ++j) { s += wcnt[j][tid]; wcnt[j][tid] = 0; }
-            run[tid] += s;
+            unsigned sum = 0;
+#pragma unroll
+            for (int j = 0; j < OS_WARPS; ++j) {
+                sum += wcnt[j][tid];
+                wcnt[j][tid] = 0;
+            }
+            run[tid] += sum;
         }
         __syncthreads();
     }
@@ -198,16 +289,23 @@ int num_sms()
 
 cudaError_t radix_sort(SortScratch &s, int n, int bits, cudaStream_t st, const int *d_n)
 {
-    if (n <= 0) return cudaSuccess;
-    int nTiles = (n + RS_TILE - 1) / RS_TILE;
-    cudaError_t e = dalloc(s.hist, (size_t)256 * nTiles);
-    if (e) return e;
-    for (int shift = 0; shift < bits; shift += 8) {
-        rs_histogram<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, n, d_n, shift, nTiles, s.hist.p); skid::note_launch();
-        e = scan_exclusive((const int *)s.hist.p, (int *)s.hist.p, 256 * nTiles, nullptr, s, st);
-        if (e) return e;
-        rs_scatter<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, s.v0.p, s.k1.p, s.v1.p, n, d_n, shift, nTiles,
-                                                  s.hist.p); skid::note_launch();
+    if (n <= 0 || bits <= 0) return cudaSuccess;
+    const int passes = (bits + 7) / 8 < OS_MAXPASS ? (bits + 7) / 8 : OS_MAXPASS;
+    const int nTiles = (n + RS_TILE - 1) / RS_TILE;
+    cudaError_t e;
+    if ((e = dalloc(s.hist, (size_t)256 * nTiles)) || (e = dalloc(s.glob, SORT_GLOB_WORDS)))
+        return e;
+    // glob: [p*256 + d] digit histograms -> offsets; [OS_MAXPASS*256 + p] tile counters
+    if ((e = cudaMemsetAsync(s.glob.p, 0, SORT_GLOB_WORDS * sizeof(uint32_t), st))) return e;
+    const int hblocks = nTiles < num_sms() * 2 ? nTiles : num_sms() * 2;
+    os_histogram<<<hblocks, 512, 0, st>>>(s.k0.p, n, d_n, passes, s.glob.p); skid::note_launch();
+    os_offsets<<<1, 256, 0, st>>>(s.glob.p, passes); skid::note_launch();
+    for (int p = 0; p < passes; ++p) {
+        if ((e = cudaMemsetAsync(s.hist.p, 0, (size_t)256 * nTiles * sizeof(uint32_t), st)))
+            return e;
+        os_pass<<<nTiles, RS_THREADS, 0, st>>>(s.k0.p, s.v0.p, s.k1.p, s.v1.p, n, d_n, 8 * p,
+                                                s.glob.p + 256 * p, s.hist.p,
+                                                s.glob.p + OS_MAXPASS * 256 + p, s.d_err); skid::note_launch();
         std::swap(s.k0, s.k1);
         std::swap(s.v0, s.v1);
     }
