@@ -284,8 +284,12 @@ field_kernel(FieldArgs a)
                     // gives NaN and is rejected, as the exact test would)
                     float r = c4.w * rsqrtf(c4.w) * (1.0f + 4e-6f) +
                               1e-6f * (fabsf(c4.x) + fabsf(c4.y) + fabsf(c4.z)) + 1e-30f;
-                    rel = c4.x + r >= wlo.x && c4.x - r <= whi.x && c4.y + r >= wlo.y &&
-                          c4.y - r <= whi.y && c4.z + r >= wlo.z && c4.z - r <= whi.z;
+                    // the ball itself against the box: squared distance from
+                    // the copy to the movers' box (per-axis gaps, zero inside)
+                    const float gx = fmaxf(fmaxf(wlo.x - c4.x, c4.x - whi.x), 0.0f);
+                    const float gy = fmaxf(fmaxf(wlo.y - c4.y, c4.y - whi.y), 0.0f);
+                    const float gz = fmaxf(fmaxf(wlo.z - c4.z, c4.z - whi.z), 0.0f);
+                    rel = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, gx * gx)) <= r * r;
                 }
                 // the survivors, compacted in candidate order
                 const unsigned R = __ballot_sync(SKID_FULL, rel);
