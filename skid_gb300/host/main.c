@@ -285,6 +285,17 @@ int main(int argc, char **argv)
     par.device = 0;
     die_on(skid_create(&g_ctx, &par), "skid_create");
     skid_ctx *ctx = g_ctx;
+    /* One run per process: timing the 18 candidate removal schedules would
+     * cost more than it saves, so the tool takes the schedule the tuner
+     * picks on clustered snapshots (a warp per group of up to 1024 members,
+     * 512-thread blocks above); SKID_UNBIND_TUNE=1 tunes instead. */
+    {
+        const char *tune = getenv("SKID_UNBIND_TUNE");
+        if (!tune || strcmp(tune, "1") != 0) {
+            die_on(skid_set_option(ctx, "unbind_warp_max", 1024), "skid_set_option");
+            die_on(skid_set_option(ctx, "unbind_block", 512), "skid_set_option");
+        }
+    }
     die_on(skid_set_tipsy(ctx, raw.nGas, raw.nDark, raw.nStar, raw.time, o.bStandard, raw.records,
                           raw.bytes),
            "skid_set_tipsy");
