@@ -4,14 +4,15 @@
 // The sort reads the keys once up front to count every digit position's
 // histogram (one kernel for all passes), turns them into global digit
 // offsets (one small kernel), then makes one kernel launch per 8-bit pass.
-// A pass takes tiles of 4096 keys (256 threads x 16 rounds, round-major so
-// tile order = input order) in the order blocks start (a tile counter), so
-// a tile's predecessors are always already running: it counts its digits,
-// publishes them, and finds the keys of each digit before it by decoupled
-// look-back over the predecessors' published counts (an aggregate, or an
-// inclusive prefix that ends the walk), then ranks its keys stably with warp
-// match and per-warp digit counts and scatters them.  Each look-back wait is
-// bounded; one that runs out sets the caller's status word.
+// A pass takes tiles of 4096 keys (each of 8 warps ranks 512 contiguous
+// keys with warp match, so tile order = input order) in the order blocks
+// start (a tile counter), so a tile's predecessors are always already
+// running: it counts its digits, publishes them, and finds the keys of each
+// digit before it by decoupled look-back over the predecessors' published
+// counts (an aggregate, or an inclusive prefix that ends the walk), then
+// scatters its keys stably.  Each look-back wait is bounded; one that runs
+// out sets the caller's status word.
+
 #include <atomic>
 
 #include "internal.h"
@@ -97,37 +98,51 @@ os_pass(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
         uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, int n, const int *d_n, int shift,
         const uint32_t *__restrict__ goff, uint32_t *status, uint32_t *counter, unsigned *d_err)
 {
+    constexpr int WKEYS = RS_ROUNDS * 32;          // keys per warp, contiguous
     __shared__ uint32_t s_tile;
-    __shared__ uint32_t hist[256];
-    __shared__ uint32_t run[256];
-    __shared__ uint32_t wcnt[OS_WARPS][256];
+    __shared__ uint32_t wcnt[OS_WARPS][256];       // per-warp digit counts, then offsets
+    __shared__ uint32_t run[256];                  // the tile's first output slot per digit
     if (d_n) n = min(n, *d_n);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(counter, 1u);
-    hist[tid] = 0;
 #pragma unroll
     for (int j = 0; j < OS_WARPS; ++j) wcnt[j][tid] = 0;
     __syncthreads();
     const int tile = (int)s_tile;
     const int base = tile * RS_TILE;
     if (base >= n) return;   // beyond the live keys (block-uniform)
+    // warp w ranks keys [base + w WKEYS, base + (w+1) WKEYS) in 16 rounds of
+    // 32: a key's place among its warp's keys of the same digit is the
+    // count from earlier rounds plus its rank among equal digits this round
+    const int wbase = base + w * WKEYS;
+    const unsigned lt = (1u << lane) - 1u;
     uint64_t k[RS_ROUNDS];
-    uint32_t v[RS_ROUNDS];
+    uint32_t v[RS_ROUNDS], loc[RS_ROUNDS];
 #pragma unroll
     for (int r = 0; r < RS_ROUNDS; ++r) {
-        const int i = base + r * RS_THREADS + tid;
-        k[r] = 0;
-        v[r] = 0;
-        if (i < n) {
-            k[r] = kin[i];
-            v[r] = vin[i];
-            atomicAdd(&hist[(k[r] >> shift) & 0xff], 1u);
-        }
+        const int i = wbase + r * 32 + lane;
+        const bool valid = i < n;
+        k[r] = valid ? kin[i] : 0;
+        v[r] = valid ? vin[i] : 0;
+        const unsigned d = valid ? (unsigned)((k[r] >> shift) & 0xff) : 256u + lane;
+        const unsigned peers = __match_any_sync(SKID_FULL, d);
+        const unsigned before = valid ? wcnt[w][d] : 0u;
+        __syncwarp();
+        if (valid && (peers & lt) == 0) wcnt[w][d] = before + __popc(peers);
+        __syncwarp();
+        loc[r] = before + __popc(peers & lt);
     }
     __syncthreads();
     {
-        // thread tid owns digit tid: publish, then look back
-        const uint32_t c = hist[tid];
+        // thread tid owns digit tid: the warps' exclusive offsets, the tile's
+        // count, then publish and look back over the predecessors
+        uint32_t c = 0;
+#pragma unroll
+        for (int j = 0; j < OS_WARPS; ++j) {
+            const uint32_t x = wcnt[j][tid];
+            wcnt[j][tid] = c;
+            c += x;
+        }
         uint32_t *mine = status + (size_t)tile * 256 + tid;
         uint32_t excl = 0;
         if (tile == 0) {
@@ -155,33 +170,15 @@ os_pass(const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin,
         run[tid] = goff[tid] + excl;
     }
     __syncthreads();
-    const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int r = 0; r < RS_ROUNDS; ++r) {
-        const int i = base + r * RS_THREADS + tid;
-        const bool valid = i < n;
-        const unsigned d = valid ? (unsigned)((k[r] >> shift) & 0xff) : 256u + lane;
-        const unsigned peers = __match_any_sync(SKID_FULL, d);
-        const unsigned rank = __popc(peers & lt);
-        if (valid && (peers & lt) == 0) wcnt[w][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            unsigned off = run[d] + rank;
-            for (int j = 0; j < w; ++j) off += wcnt[j][d];
+        const int i = wbase + r * 32 + lane;
+        if (i < n) {
+            const unsigned d = (unsigned)((k[r] >> shift) & 0xff);
+            const unsigned off = run[d] + wcnt[w][d] + loc[r];
             kout[off] = k[r];
             vout[off] = v[r];
         }
-        __syncthreads();
-        {
-            unsigned sum = 0;
-#pragma unroll
-            for (int j = 0; j < OS_WARPS; ++j) {
-                sum += wcnt[j][tid];
-                wcnt[j][tid] = 0;
-            }
-            run[tid] += sum;
-        }
-        __syncthreads();
     }
 }
 
