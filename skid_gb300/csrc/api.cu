@@ -1048,11 +1048,14 @@ int skid_set_option(skid_ctx *ctx, const char *name, double value)
         ctx->opt_unbind_bs = v;
     } else if (!strcmp(name, "unbind_per_group")) {
         ctx->opt_unbind_per_group = v != 0;
+    } else if (!strcmp(name, "unbind_cluster_min")) {
+        if (v != 0 && v < 1024) return SKID_EINVAL;
+        ctx->opt_unbind_clu_min = v;
     } else if (!strcmp(name, "field_unfused")) {
         ctx->opt_field_unfused = v != 0;
         ctx->drop_graphs();
     } else if (!strcmp(name, "unbind_retune")) {
-        ctx->U.tuned_tw = ctx->U.tuned_bs = -1;
+        ctx->U.tuned_tw = ctx->U.tuned_bs = ctx->U.tuned_cs = -1;
         ctx->U.ntune = 0;
     } else {
         return SKID_EINVAL;
@@ -1071,6 +1074,9 @@ int skid_get_option(skid_ctx *ctx, const char *name, double *value)
     else if (!strcmp(name, "unbind_warp_max")) *value = ctx->U.used_tw;
     else if (!strcmp(name, "unbind_block")) *value = ctx->U.used_bs;
     else if (!strcmp(name, "unbind_per_group")) *value = ctx->opt_unbind_per_group;
+    else if (!strcmp(name, "unbind_cluster_min")) *value = ctx->opt_unbind_clu_min;
+    else if (!strcmp(name, "unbind_cluster_size")) *value = ctx->U.used_cs;
+    else if (!strcmp(name, "unbind_cluster_groups")) *value = ctx->U.used_nclu;
     else if (!strcmp(name, "unbind_tune_candidates")) *value = ctx->U.ntune;
     else if (!strcmp(name, "unbind_pot_ms")) *value = ctx->U.pot_ms;
     else if (!strcmp(name, "unbind_remove_ms")) *value = ctx->U.remove_ms;

@@ -77,6 +77,7 @@ struct UnbindParams {
     int n;             // particles (size of grp)
     int tw, bs;        // removal schedule: warp-per-group up to tw members, blocks of bs
                        // threads above; -1 = autotuned
+    int clu_min;       // the largest groups above this many members may take a block cluster (0: none)
     bool per_group;    // one potential and one removal launch per group
 };
 
@@ -90,7 +91,9 @@ struct UnbindScratch {
     DBuf<float> ssoft, usoft;
     DBuf<skid_group> rec_save;
     int tuned_tw = -1, tuned_bs = -1;   // autotuned removal schedule (kept per context)
+    int tuned_cs = -1;                  // autotuned: the largest groups on block clusters (1) or not (0)
     int used_tw = -1, used_bs = -1;     // schedule of the last run
+    int used_cs = 1, used_nclu = 0;     // cluster size and clustered groups of the last run
     float tune_ms[32] = {};
     int ntune = 0, ntune_now = 0;
     float pot_ms = 0.0f, remove_ms = 0.0f;   // last run (CUDA events)
@@ -262,6 +265,7 @@ struct skid_ctx {
     // movers, 16 down to ~400k, 8 down to ~50k, 4 down to ~25k, one below.
     int opt_G = 0, opt_g32_min = 600000, opt_g16_min = 400000, opt_g8_min = 100000, opt_g4_min = 30000;
     int opt_unbind_tw = -1, opt_unbind_bs = -1;   // -1: autotuned on the first skid_unbind
+    int opt_unbind_clu_min = 2048;                // the largest groups above it may take a block cluster; 0 = never
     bool opt_unbind_per_group = false;
     bool opt_field_unfused = false;                // field pass and move pass as separate kernels
     skid::DBuf<float> unfused_acc;

@@ -36,7 +36,11 @@
 #include <cfloat>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "ctx.h"
+
+namespace cg = cooperative_groups;
 
 namespace skid {
 
@@ -312,6 +316,20 @@ __global__ void sched_counts(const int *__restrict__ gcount, int ng, int nmax, i
 
 // ---- potentials ----
 
+// out[0]: groups taken by clusters, the largest ones above `floor` members
+// but at most kmax of them; out[2]: the largest valid group's size (order is
+// largest first)
+__global__ void cluster_groups(const uint32_t *__restrict__ order, const int *d_nvalid,
+                               const int *__restrict__ gcount, int floor, int kmax, int *out)
+{
+    if (threadIdx.x != 0) return;
+    const int nv = *d_nvalid;
+    int k = 0;
+    while (k < nv && k < kmax && gcount[order[k]] > floor) ++k;
+    out[0] = k;
+    out[2] = nv > 0 ? gcount[order[0]] : 0;
+}
+
 __global__ void pot_nitems(const uint32_t *__restrict__ order, const int *d_nvalid,
                            const int *__restrict__ gcount, int ng, int *__restrict__ ni)
 {
@@ -561,6 +579,9 @@ struct RemoveArgs {
     const uint32_t *order;          // valid groups, largest first
     const int *d_cnt;               // [valid groups, groups above tw]
     int *d_queue;
+    const int *d_ccnt;              // groups taken by clusters (the largest, a prefix of order)
+    int *d_cqueue;
+    int qcap;                       // members per block slice a cluster can hold
     int single;                     // > 0: process only this group (per-group mode)
 };
 
@@ -723,11 +744,11 @@ __device__ void warp_group(const RemoveArgs &A, int g)
             const ArgRed t1 = mx, b1 = mn;
             mx = ArgRed{-FLT_MAX, 0x7fffffff};
             mn = ArgRed{FLT_MAX, 0x7fffffff};
-            if (t1.v >= hi && mx2.v < hi) {
+            if (t1.i < n && t1.v >= hi && mx2.v < hi) {
                 mx.v = member_energy(true, A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, scm, inv_d, opz_d);
                 mx.i = t1.i;
             }
-            if (b1.v <= lo && mn2.v > lo) {
+            if (b1.i < n && b1.v <= lo && mn2.v > lo) {
                 mn.v = member_energy(true, A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, scm, inv_d, opz_d);
                 mn.i = b1.i;
             }
@@ -791,13 +812,15 @@ struct BlockShared {
     float4 s_r;
     float s_eps;
     float s_cm[6];
-    int s_n, s_go, s_have, s_imin;
+    int s_n, s_go, s_have, s_imin, s_item;
     double d_cm[6], d_mass;
     double part[BS / 32][7];
     float ext[BS / 32][4];      // per-warp FP32 energy max, min, error-bound terms
     float s_w[3];               // a vcm + aH rcm (large groups' FP32 energies)
     float s_mW;                 // max_j |a vcm_j| + |aH rcm_j|
     float s_mg;                 // max over members and axes of |a v_j| + |aH r_j|
+    float gpart[8][4];          // a cluster's blocks' partials, gathered (rank order)
+    ArgRed gmx[8], gmn[8];
 };
 
 // max_j |a c_j| + |aH c_{j-3}| of a centre (rcm, vcm)
@@ -990,11 +1013,11 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 // usually only the thread's own extreme is a candidate: that
                 // one member exactly (when both its first and second are
                 // candidates on a side, the rescan below takes that side)
-                if (tmax >= hi && mx2.v < hi) {
+                if (t1.i < n && tmax >= hi && mx2.v < hi) {
                     mx.v = exact_energy(A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, inv_d, opz_d);
                     mx.i = t1.i;
                 }
-                if (tmin <= lo && mn2.v > lo) {
+                if (b1.i < n && tmin <= lo && mn2.v > lo) {
                     mn.v = exact_energy(A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, inv_d, opz_d);
                     mn.i = b1.i;
                 }
@@ -1044,11 +1067,11 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
             const ArgRed t1 = mx, b1 = mn;
             mx = ArgRed{-FLT_MAX, 0x7fffffff};
             mn = ArgRed{FLT_MAX, 0x7fffffff};
-            if (t1.v >= hi && ex2.v < hi) {
+            if (t1.i < n && t1.v >= hi && ex2.v < hi) {
                 mx.v = member_energy(true, A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, scm, inv_d, opz_d);
                 mx.i = t1.i;
             }
-            if (b1.v <= lo && en2.v > lo) {
+            if (b1.i < n && b1.v <= lo && en2.v > lo) {
                 mn.v = member_energy(true, A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, scm, inv_d, opz_d);
                 mn.i = b1.i;
             }
@@ -1131,10 +1154,319 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
     __syncthreads();
 }
 
+// ---- the largest groups: one thread-block cluster each ----
+//
+// One of the largest groups can be shared by the CS blocks of one cluster.
+// Block c holds slots [c Q, (c+1) Q) of the members (Q = ceil(n0 / CS)) in
+// shared memory: relative position and mass, the staged w = a v + aH r with
+// the softening, and the fixed-point potential, so every pass reads on-chip
+// memory instead of L2.  A removal takes three cluster barriers:
+//   1. each block's FP32 extremes and error-bound terms are gathered from
+//      all blocks' shared memory (distributed shared memory) and combined in
+//      rank order, so every block holds the same candidate thresholds;
+//   2. likewise the blocks' exact arg-max and arg-min (first index on ties)
+//      give every block the same decision; each reads the removed member from
+//      its owner block and updates its FP64 centre;
+//   3. once all have read it, the owner of the freed slot copies the last
+//      member into it (swap with the last, kd.c:1435-1440).
+// Velocities, positions and ids in global memory are swapped the same way:
+// velocities are read only for the exact energies of the few candidates and
+// for the removed member.
+struct ClusterShared {
+    float part[4];          // block FP32 max, min, max dd, max |pe|
+    ArgRed pmax, pmin;      // block exact arg-max, arg-min
+    double psum[7];         // block FP64 sums: mass, m r, m v
+    float pmg;              // block max |a v_j| + |aH r_j|
+    int item;
+};
+
+template <int BS, int CS>
+__device__ void cluster_group(const RemoveArgs &A, int g, BlockShared<BS> &S, ClusterShared &C,
+                              float4 *dyn, cg::cluster_group &cl)
+{
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int rank = (int)cl.block_rank();
+    const int s = A.gstart[g], n0 = A.gcount[g];
+    const int Q = (n0 + CS - 1) / CS;
+    const int lo = rank * Q, hi = min(lo + Q, n0);
+    float4 *s_r = dyn, *s_w = dyn + A.qcap;
+    long long *s_p = reinterpret_cast<long long *>(dyn + 2 * A.qcap);
+    float4 *qr = A.qr + s, *qv = A.qv + s;
+    int *qid = A.qid + s;
+    const long long *pot = A.pot + s;
+    // the slice into shared memory, its FP64 sums and member magnitudes
+    double m = 0.0, c[6] = {0, 0, 0, 0, 0, 0};
+    float mg = 0.0f;
+    for (int i = lo + tid; i < hi; i += BS) {
+        const float4 r = qr[i], v = qv[i];
+        s_r[i - lo] = r;
+        s_w[i - lo] = make_float4(__fmaf_rn(A.fShift, v.x, A.fCosmo * r.x),
+                                  __fmaf_rn(A.fShift, v.y, A.fCosmo * r.y),
+                                  __fmaf_rn(A.fShift, v.z, A.fCosmo * r.z), v.w);
+        s_p[i - lo] = pot[i];
+        m += r.w;
+        c[0] += fmul(r.w, r.x); c[1] += fmul(r.w, r.y); c[2] += fmul(r.w, r.z);
+        c[3] += fmul(r.w, v.x); c[4] += fmul(r.w, v.y); c[5] += fmul(r.w, v.z);
+        mg = fmaxf(mg, fabsf(A.fShift * v.x) + fabsf(A.fCosmo * r.x));
+        mg = fmaxf(mg, fabsf(A.fShift * v.y) + fabsf(A.fCosmo * r.y));
+        mg = fmaxf(mg, fabsf(A.fShift * v.z) + fabsf(A.fCosmo * r.z));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        m += __shfl_xor_sync(SKID_FULL, m, o);
+        for (int d = 0; d < 6; ++d) c[d] += __shfl_xor_sync(SKID_FULL, c[d], o);
+    }
+    mg = __uint_as_float(__reduce_max_sync(SKID_FULL, __float_as_uint(mg)));
+    if (lane == 0) {
+        S.part[w][0] = m;
+        for (int d = 0; d < 6; ++d) S.part[w][1 + d] = c[d];
+        S.ext[w][0] = mg;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double t[7] = {0, 0, 0, 0, 0, 0, 0};
+        float tm = 0.0f;
+        for (int k = 0; k < BS / 32; ++k) {
+            for (int d = 0; d < 7; ++d) t[d] += S.part[k][d];
+            tm = fmaxf(tm, S.ext[k][0]);
+        }
+        for (int d = 0; d < 7; ++d) C.psum[d] = t[d];
+        C.pmg = tm;
+    }
+    cl.sync();
+    if (tid == 0) {
+        // every block combines the partials in rank order: the same values
+        double t[7] = {0, 0, 0, 0, 0, 0, 0};
+        float tm = 0.0f;
+        for (int b = 0; b < CS; ++b) {
+            const ClusterShared *rc = cl.map_shared_rank(&C, b);
+            for (int d = 0; d < 7; ++d) t[d] += rc->psum[d];
+            tm = fmaxf(tm, rc->pmg);
+        }
+        S.d_mass = t[0];
+        for (int d = 0; d < 6; ++d) {
+            S.d_cm[d] = t[1 + d] / t[0];
+            S.s_cm[d] = (float)S.d_cm[d];
+        }
+        for (int d = 0; d < 3; ++d)
+            S.s_w[d] = (float)((double)A.fShift * S.d_cm[3 + d] + (double)A.fCosmo * S.d_cm[d]);
+        S.s_mg = tm * 1.0000002f;
+        S.s_mW = centre_mag(A, S.d_cm);
+        S.s_n = n0;
+        S.s_have = 0;
+        S.s_go = 1;
+    }
+    cl.sync();   // every block has read the sums before any overwrites them
+    int nrem = 0;
+    const double opz_d = 1.0 + (double)A.z, inv_d = 1.0 / (double)A.scale;
+    const float epot = A.inv_scale * A.opz;
+    for (;;) {
+        const int n = S.s_n;
+        const bool sub = S.s_have != 0 && A.subpot;
+        const float4 rs = S.s_r;
+        const float es = S.s_eps;
+        double dcm[6];
+        for (int d = 0; d < 6; ++d) dcm[d] = S.d_cm[d];
+        const float wx = S.s_w[0], wy = S.s_w[1], wz = S.s_w[2];
+        const float gms = fmul(A.G, rs.w) * A.scale;
+        ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
+        ArgRed mx2 = mx, mn2 = mn;
+        float ddmx = 0.0f, pemx = 0.0f;
+        const int e = min(hi, n);
+        for (int i = lo + tid; i < e; i += BS) {
+            const float4 r = s_r[i - lo], wv = s_w[i - lo];
+            long long p = s_p[i - lo];
+            if (sub) {
+                // kdSubPot (grav.c:44-59): the term the potentials added
+                const float d2 = d2of(fsub(rs.x, r.x), fsub(rs.y, r.y), fsub(rs.z, r.z));
+                p -= fx(fmul(gms, pair_dir(d2, fadd(es, wv.w), A.plummer)), 1.0f);
+                s_p[i - lo] = p;
+            }
+            const float dx = wv.x - wx, dy = wv.y - wy, dz = wv.z - wz;
+            const float dd = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+            const float pe = ll2f_fast(p) * epot;
+            const float E = 0.5f * dd - pe;
+            keep_top2(mx, mx2, E, i);
+            keep_bot2(mn, mn2, E, i);
+            ddmx = fmaxf(ddmx, dd);
+            pemx = fmaxf(pemx, fabsf(pe));
+        }
+        // 1. the FP32 extremes and bound terms over the whole group
+        {
+            float a0 = mx.v, a1 = mn.v, a2 = ddmx, a3 = pemx;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                a0 = fmaxf(a0, __shfl_xor_sync(SKID_FULL, a0, o));
+                a1 = fminf(a1, __shfl_xor_sync(SKID_FULL, a1, o));
+                a2 = fmaxf(a2, __shfl_xor_sync(SKID_FULL, a2, o));
+                a3 = fmaxf(a3, __shfl_xor_sync(SKID_FULL, a3, o));
+            }
+            if (lane == 0) {
+                S.ext[w][0] = a0;
+                S.ext[w][1] = a1;
+                S.ext[w][2] = a2;
+                S.ext[w][3] = a3;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                float b0 = -FLT_MAX, b1 = FLT_MAX, b2 = 0.0f, b3 = 0.0f;
+                for (int k = 0; k < BS / 32; ++k) {
+                    b0 = fmaxf(b0, S.ext[k][0]);
+                    b1 = fminf(b1, S.ext[k][1]);
+                    b2 = fmaxf(b2, S.ext[k][2]);
+                    b3 = fmaxf(b3, S.ext[k][3]);
+                }
+                C.part[0] = b0;
+                C.part[1] = b1;
+                C.part[2] = b2;
+                C.part[3] = b3;
+            }
+        }
+        cl.sync();
+        if (tid < CS) {
+            // thread b fetches block b's partials from its shared memory
+            const ClusterShared *rc = cl.map_shared_rank(&C, tid);
+            for (int d = 0; d < 4; ++d) S.gpart[tid][d] = rc->part[d];
+        }
+        __syncthreads();
+        float gmax = -FLT_MAX, gmin = FLT_MAX, gdd = 0.0f, gpe = 0.0f;
+        for (int b = 0; b < CS; ++b) {
+            gmax = fmaxf(gmax, S.gpart[b][0]);
+            gmin = fminf(gmin, S.gpart[b][1]);
+            gdd = fmaxf(gdd, S.gpart[b][2]);
+            gpe = fmaxf(gpe, S.gpart[b][3]);
+        }
+        // the staged path's bound (block_group, groups above 1024 members)
+        const float Cm = S.s_mg + S.s_mW;
+        const float bound =
+            1.9073486e-06f * (Cm * (1.7320509f * sqrtf(gdd) + 3.0f * Cm) + 1.5f * gdd + 2.0f * gpe) +
+            1e-30f;
+        const float hiE = gmax - 2.0f * bound, loE = gmin + 2.0f * bound;
+        const ArgRed t1 = mx, b1 = mn;
+        mx = ArgRed{-FLT_MAX, 0x7fffffff};
+        mn = ArgRed{FLT_MAX, 0x7fffffff};
+        if (t1.i < e && t1.v >= hiE && mx2.v < hiE) {
+            mx.v = exact_energy(A, s_r[t1.i - lo], qv[t1.i], s_p[t1.i - lo], dcm, inv_d, opz_d);
+            mx.i = t1.i;
+        }
+        if (b1.i < e && b1.v <= loE && mn2.v > loE) {
+            mn.v = exact_energy(A, s_r[b1.i - lo], qv[b1.i], s_p[b1.i - lo], dcm, inv_d, opz_d);
+            mn.i = b1.i;
+        }
+        const bool scan_hi = mx2.v >= hiE, scan_lo = mn2.v <= loE;
+        if (scan_hi || scan_lo) {
+            for (int i = lo + tid; i < e; i += BS) {
+                const float4 wv = s_w[i - lo];
+                const long long p = s_p[i - lo];
+                const float dx = wv.x - wx, dy = wv.y - wy, dz = wv.z - wz;
+                const float E =
+                    0.5f * __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) - ll2f_fast(p) * epot;
+                const bool ch = scan_hi && E >= hiE, clo = scan_lo && E <= loE;
+                if (ch || clo) {
+                    const float X = exact_energy(A, s_r[i - lo], qv[i], p, dcm, inv_d, opz_d);
+                    if (ch && X > mx.v) { mx.v = X; mx.i = i; }
+                    if (clo && X < mn.v) { mn.v = X; mn.i = i; }
+                }
+            }
+        }
+        // 2. the exact arg-max and arg-min over the whole group
+        mx = warp_argmax(mx);
+        mn = warp_argmin(mn);
+        if (lane == 0) { S.smax[w] = mx; S.smin[w] = mn; }
+        __syncthreads();
+        if (tid == 0) {
+            ArgRed a = S.smax[0], b = S.smin[0];
+            for (int k = 1; k < BS / 32; ++k) {
+                const ArgRed x = S.smax[k], y = S.smin[k];
+                if (x.v > a.v || (x.v == a.v && x.i < a.i)) a = x;
+                if (y.v < b.v || (y.v == b.v && y.i < b.i)) b = y;
+            }
+            C.pmax = a;
+            C.pmin = b;
+        }
+        cl.sync();
+        if (tid < CS) {
+            const ClusterShared *rc = cl.map_shared_rank(&C, tid);
+            S.gmx[tid] = rc->pmax;
+            S.gmn[tid] = rc->pmin;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            ArgRed a = S.gmx[0], b = S.gmn[0];
+            for (int k = 1; k < CS; ++k) {
+                const ArgRed x = S.gmx[k], y = S.gmn[k];
+                if (x.v > a.v || (x.v == a.v && x.i < a.i)) a = x;
+                if (y.v < b.v || (y.v == b.v && y.i < b.i)) b = y;
+            }
+            // kd.c:1389-1409: fTotBig starts at -1, fTotMin at 1
+            S.s_imin = b.v < 1.0f ? b.i : 0;
+            if (!(a.v >= 0.0f) || A.nounbind || n == 0) {
+                S.s_go = 0;
+            } else {
+                const int ib = a.i;
+                const int ob = ib / Q;
+                const float4 r = cl.map_shared_rank(s_r, ob)[ib - ob * Q];
+                const float4 wv = cl.map_shared_rank(s_w, ob)[ib - ob * Q];
+                const float4 v = qv[ib];
+                if (rank == 0) A.grp[qid[ib]] = 0;
+                ++nrem;
+                const int nn = n - 1;
+                if (nn == 0) {
+                    S.d_mass = 0.0;
+                    for (int d = 3; d < 6; ++d) S.d_cm[d] = 0.0;
+                    S.s_go = 0;
+                } else {
+                    double mm = S.d_mass;
+                    for (int d = 0; d < 6; ++d) dcm[d] = S.d_cm[d];
+                    rcm_update(mm, dcm, r, v);
+                    S.d_mass = mm;
+                    for (int d = 0; d < 6; ++d) {
+                        S.d_cm[d] = dcm[d];
+                        S.s_cm[d] = (float)dcm[d];
+                    }
+                    for (int d = 0; d < 3; ++d)
+                        S.s_w[d] = (float)((double)A.fShift * dcm[3 + d] + (double)A.fCosmo * dcm[d]);
+                    S.s_mW = centre_mag(A, dcm);
+                    S.s_r = r;
+                    S.s_eps = wv.w;
+                    S.s_have = 1;
+                }
+                S.s_n = nn;
+                S.s_item = ib;
+            }
+        }
+        // 3. every block has read the removed member (and rank 0 its id)
+        // before its slot is overwritten
+        cl.sync();
+        if (tid == 0 && S.s_go) {
+            const int ib = S.s_item;
+            const int nn = S.s_n;
+            if (ib / Q == rank && ib != nn) {
+                const int on = nn / Q;
+                s_r[ib - lo] = cl.map_shared_rank(s_r, on)[nn - on * Q];
+                s_w[ib - lo] = cl.map_shared_rank(s_w, on)[nn - on * Q];
+                s_p[ib - lo] = cl.map_shared_rank(s_p, on)[nn - on * Q];
+                const float4 rl = qr[nn], vl = qv[nn], rb = qr[ib], vb = qv[ib];
+                const int il = qid[nn], ir = qid[ib];
+                qr[ib] = rl; qv[ib] = vl; qid[ib] = il;
+                qr[nn] = rb; qv[nn] = vb; qid[nn] = ir;
+            }
+        }
+        __syncthreads();
+        if (!S.s_go) break;
+    }
+    if (rank == 0 && tid == 0) {
+        double dcm[6];
+        for (int d = 0; d < 6; ++d) dcm[d] = S.d_cm[d];
+        write_record(A, g, S.s_n, S.d_mass, dcm, qr[S.s_imin], nrem);
+    }
+    cl.sync();   // no block leaves while another may still read its shared memory
+}
+
 // Persistent removal: queue items [0, nbig) are large groups (one block
 // each), then chunks of BS/32 small groups (one warp each), all largest
 // first.  With A.single > 0 one block processes just that group.
-template <int BS>
+template <int BS, int CS>
 __global__ void __launch_bounds__(BS) remove_kernel(RemoveArgs A)
 {
     __shared__ BlockShared<BS> S;
@@ -1144,18 +1476,37 @@ __global__ void __launch_bounds__(BS) remove_kernel(RemoveArgs A)
         block_group<BS>(A, A.single, S);
         return;
     }
-    const int nvalid = A.d_cnt[0], nbig = A.d_cnt[1];
-    const int nitems = nbig + (nvalid - nbig + W - 1) / W;
+    int first = 0;
+    if constexpr (CS > 1) {
+        // launched as clusters of CS blocks: the largest groups first, one
+        // cluster each, then every block goes on alone
+        __shared__ ClusterShared C;
+        extern __shared__ float4 dyn[];
+        cg::cluster_group cl = cg::this_cluster();
+        const int nclu = *A.d_ccnt;
+        for (;;) {
+            if (cl.block_rank() == 0 && threadIdx.x == 0) C.item = atomicAdd(A.d_cqueue, 1);
+            cl.sync();
+            const int item = cl.map_shared_rank(&C, 0)->item;
+            cl.sync();
+            if (item >= nclu) break;
+            cluster_group<BS, CS>(A, (int)A.order[item], S, C, dyn, cl);
+        }
+        first = nclu;
+    }
+    const int nvalid = A.d_cnt[0], nbig = A.d_cnt[1] > first ? A.d_cnt[1] : first;
+    const int nb = nbig - first;
+    const int nitems = nb + (nvalid - nbig + W - 1) / W;
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(A.d_queue, 1);
         __syncthreads();
         const int item = s_item;
         __syncthreads();
         if (item >= nitems) break;
-        if (item < nbig) {
-            block_group<BS>(A, (int)A.order[item], S);
+        if (item < nb) {
+            block_group<BS>(A, (int)A.order[first + item], S);
         } else {
-            int k = nbig + (item - nbig) * W + (threadIdx.x >> 5);
+            int k = nbig + (item - nb) * W + (threadIdx.x >> 5);
             if (k < nvalid) warp_group(A, (int)A.order[k]);
         }
     }
@@ -1164,12 +1515,50 @@ __global__ void __launch_bounds__(BS) remove_kernel(RemoveArgs A)
 template <int BS>
 cudaError_t launch_remove(const RemoveArgs &A, int blocks, cudaStream_t st)
 {
-    remove_kernel<BS><<<blocks, BS, 0, st>>>(A); note_launch();
+    remove_kernel<BS, 1><<<blocks, BS, 0, st>>>(A); note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t remove_launch(const RemoveArgs &A, int bs, int blocks, cudaStream_t st)
+// Cluster launch: as many clusters of CS blocks as fit at once, each block
+// with A.qcap members' worth of dynamic shared memory.
+template <int BS, int CS>
+cudaError_t launch_remove_clusters(const RemoveArgs &A, cudaStream_t st)
 {
+    const size_t smem = (size_t)A.qcap * (2 * sizeof(float4) + sizeof(long long));
+    cudaError_t e = cudaFuncSetAttribute(remove_kernel<BS, CS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(BS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(CS, 1, 1);
+    int nclusters = 0;
+    if ((e = cudaOccupancyMaxActiveClusters(&nclusters, remove_kernel<BS, CS>, &cfg))) return e;
+    if (nclusters < 1) return cudaErrorInvalidConfiguration;
+    cfg.gridDim = dim3(CS * nclusters, 1, 1);
+    e = cudaLaunchKernelEx(&cfg, remove_kernel<BS, CS>, A);
+    note_launch();
+    return e ? e : cudaGetLastError();
+}
+
+// cs: 1 (no clusters), 4 or 8
+cudaError_t remove_launch(const RemoveArgs &A, int bs, int cs, int blocks, cudaStream_t st)
+{
+    if (cs == 4 || cs == 8) {
+        switch (bs) {
+        case 512: return cs == 4 ? launch_remove_clusters<512, 4>(A, st) : launch_remove_clusters<512, 8>(A, st);
+        case 1024: return cs == 4 ? launch_remove_clusters<1024, 4>(A, st) : launch_remove_clusters<1024, 8>(A, st);
+        default: return cs == 4 ? launch_remove_clusters<256, 4>(A, st) : launch_remove_clusters<256, 8>(A, st);
+        }
+    }
     switch (bs) {
     case 128: return launch_remove<128>(A, blocks, st);
     case 512: return launch_remove<512>(A, blocks, st);
@@ -1182,10 +1571,10 @@ int remove_blocks(int bs)
 {
     int perSM = 0;
     switch (bs) {
-    case 128: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<128>, 128, 0); break;
-    case 512: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<512>, 512, 0); break;
-    case 1024: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<1024>, 1024, 0); break;
-    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<256>, 256, 0); break;
+    case 128: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<128, 1>, 128, 0); break;
+    case 512: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<512, 1>, 512, 0); break;
+    case 1024: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<1024, 1>, 1024, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, remove_kernel<256, 1>, 256, 0); break;
     }
     return num_sms() * (perSM > 0 ? perSM : 1);
 }
@@ -1205,7 +1594,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     if ((e = dalloc(U.qr, nslots)) || (e = dalloc(U.qv, nslots)) || (e = dalloc(U.qw, nslots)) ||
         (e = dalloc(U.qid, nslots)) ||
         (e = dalloc(U.pot, nslots)) || (e = dalloc(U.scnt, ng)) || (e = dalloc(U.soff, ng + 1)) ||
-        (e = dalloc(U.nt, ng)) || (e = dalloc(U.toff, ng + 1)) || (e = dalloc(U.cnt, 8)) ||
+        (e = dalloc(U.nt, ng)) || (e = dalloc(U.toff, ng + 1)) || (e = dalloc(U.cnt, 16)) ||
         (e = dalloc(U.order, ng)))
         return e;
     float3 hP = make_float3((float)(0.5 * (double)P.period.x), (float)(0.5 * (double)P.period.y),
@@ -1245,10 +1634,29 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     // potential items, largest groups first
     pot_nitems<<<grid_for(ng), 256, 0, st>>>(U.order.p, U.cnt.p + 2, G.count.p, ng, U.nt.p); note_launch();
     if ((e = scan_exclusive(U.nt.p, U.toff.p, ng, U.cnt.p + 1, ss, st))) return e;
-    int hc[3] = {0, 0, 0};
-    if ((e = cudaMemcpyAsync(hc, U.cnt.p + 1, 2 * sizeof(int), cudaMemcpyDeviceToHost, st))) return e;
+    // clustered groups: the largest ones above clu_min members, at most as
+    // many as keep half the SMs busy with clusters of 4 blocks; and the
+    // largest group's size, which sizes the blocks' shared-memory slices
+    const int clu_min = P.clu_min > P.tw && P.clu_min > 1024 ? P.clu_min : 0;
+    const int clu_kmax = num_sms() / 8 > 1 ? num_sms() / 8 : 1;
+    if ((e = cudaMemsetAsync(U.cnt.p + 8, 0, 4 * sizeof(int), st))) return e;
+    if (clu_min > 0) {
+        cluster_groups<<<1, 32, 0, st>>>(U.order.p, U.cnt.p + 2, G.count.p, clu_min, clu_kmax,
+                                         U.cnt.p + 9); note_launch();
+    }
+    int hc[11] = {0};
+    if ((e = cudaMemcpyAsync(hc, U.cnt.p + 1, 11 * sizeof(int), cudaMemcpyDeviceToHost, st))) return e;
     if ((e = cudaStreamSynchronize(st))) return e;
-    const int nitems = hc[0], nvalid = hc[1];
+    const int nitems = hc[0], nvalid = hc[1], nclu = hc[8], nlargest = hc[10];
+    // cluster size: 4 blocks while a quarter of the largest group fits in
+    // about 200 KB of shared memory (40 B per member), else 8, else none
+    int cs = 1, qcap = 0;
+    if (clu_min > 0 && nclu > 0) {
+        const int per = (int)(2 * sizeof(float4) + sizeof(long long));
+        const int q4 = (nlargest + 3) / 4, q8 = (nlargest + 7) / 8;
+        if ((size_t)q4 * per <= 200u * 1024u) { cs = 4; qcap = q4; }
+        else if ((size_t)q8 * per <= 200u * 1024u) { cs = 8; qcap = q8; }
+    }
     if ((e = dalloc(U.items, nitems > 0 ? nitems : 1))) return e;
     if (nitems > 0)
         pot_fill<<<grid_for(nvalid), 256, 0, st>>>(U.order.p, U.cnt.p + 2, G.count.p, U.toff.p,
@@ -1281,6 +1689,9 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
     A.order = U.order.p;
     A.d_cnt = U.cnt.p + 4;
     A.d_queue = U.cnt.p + 6;
+    A.d_ccnt = U.cnt.p + 9;
+    A.d_cqueue = U.cnt.p + 10;
+    A.qcap = qcap;
     A.single = 0;
 
     const int potBlocks = nitems < num_sms() * 32 ? (nitems > 0 ? nitems : 1) : num_sms() * 32;
@@ -1292,13 +1703,14 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
                                                        U.ssoft.p, P.G, P.plummer, P.scale, U.pot.p); note_launch();
         return cudaGetLastError();
     };
-    auto removal = [&](int tw, int bs) -> cudaError_t {
+    auto removal = [&](int tw, int bs, int ucs) -> cudaError_t {
         cudaError_t e2;
         if ((e2 = cudaMemsetAsync(U.cnt.p + 4, 0, 3 * sizeof(int), st))) return e2;
+        if ((e2 = cudaMemsetAsync(U.cnt.p + 10, 0, sizeof(int), st))) return e2;
         sched_counts<<<grid_for(ng), 256, 0, st>>>(G.count.p, ng, P.nmax, tw, U.cnt.p + 4); note_launch();
         if ((e2 = cudaMemsetAsync(d_unbound, 0, sizeof(int), st))) return e2;
         if (nvalid <= 0) return cudaSuccess;
-        return remove_launch(A, bs, remove_blocks(bs), st);
+        return remove_launch(A, bs, bs >= 256 ? ucs : 1, remove_blocks(bs), st);
     };
 
     if (P.per_group) {
@@ -1319,7 +1731,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
                 U.scnt.p, U.slist.p, U.ssoft.p, P.G, P.plummer, P.scale, U.pot.p); note_launch();
             RemoveArgs A1 = A;
             A1.single = (int)order[k];
-            if ((e = remove_launch(A1, 256, 1, st))) return e;
+            if ((e = remove_launch(A1, 256, 1, 1, st))) return e;
         }
         return cudaGetLastError();
     }
@@ -1361,7 +1773,7 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
                     (e = prep()))
                     break;
                 cudaEventRecord(e0, st);
-                if ((e = removal(a, b))) break;
+                if ((e = removal(a, b, 1))) break;
                 cudaEventRecord(e1, st);
                 if ((e = cudaEventSynchronize(e1))) break;
                 float ms = 0.0f;
@@ -1373,11 +1785,31 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
             }
             if (e) break;
         }
+        // then the best schedule with the largest groups on thread-block
+        // clusters, kept only if it is faster
+        int bcs = 1;
+        if (!e && cs > 1 && bbs >= 256) {
+            if (!(e = cudaMemcpyAsync(U.pot.p, U.pot_save.p, nslots * sizeof(long long), cudaMemcpyDeviceToDevice, st)) &&
+                !(e = cudaMemcpyAsync(G.rec.p, U.rec_save.p, ng * sizeof(skid_group), cudaMemcpyDeviceToDevice, st)) &&
+                !(e = cudaMemcpyAsync(grp, U.grp_save.p, P.n * sizeof(int), cudaMemcpyDeviceToDevice, st)) &&
+                !(e = prep())) {
+                cudaEventRecord(e0, st);
+                e = removal(btw, bbs, cs);
+                cudaEventRecord(e1, st);
+                if (!e) e = cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                if (!e) cudaEventElapsedTime(&ms, e0, e1);
+                U.tune_ms[U.ntune < 32 ? U.ntune : 31] = ms;
+                ++U.ntune;
+                if (!e && ms < best) bcs = cs;
+            }
+        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (e) return e;
         U.tuned_tw = btw;
         U.tuned_bs = bbs;
+        U.tuned_cs = bcs > 1 ? 1 : 0;
         tw = btw;
         bs = bbs;
         if ((e = cudaMemcpyAsync(U.pot.p, U.pot_save.p, nslots * sizeof(long long), cudaMemcpyDeviceToDevice, st)) ||
@@ -1386,10 +1818,16 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
             (e = prep()))
             return e;
     }
+    // clusters: as the tuner chose for a tuned schedule; with a fixed one,
+    // whenever there are groups for them
+    const bool tuned_sched = P.tw < 0 || P.bs < 0;
+    const int ucs = cs > 1 && (!tuned_sched || U.tuned_cs == 1) ? cs : 1;
     U.used_tw = tw;
     U.used_bs = bs;
+    U.used_cs = ucs;
+    U.used_nclu = ucs > 1 ? nclu : 0;
     if (U.ntune) cudaEventRecord(t1, st);   // tuning ran in between: time the final removal only
-    e = removal(tw, bs);
+    e = removal(tw, bs, ucs);
     cudaEventRecord(t2, st);
     if (!e) e = cudaEventSynchronize(t2);
     float a = 0.0f, b = 0.0f;

@@ -115,11 +115,12 @@ def test_schedules_and_unfused_forms_agree(gpu_ready, name):
 
 
 def test_unbind_large_groups_fp32_path(gpu_ready):
-    """Groups above 1024 members take the FP32-energy removal path (staged
-    a v + aH r per member, member loads batched per thread): unbind-only mode
-    on three groups of 1790-4075 members, with a twelfth of their members
-    sped up fourfold so that each loses 89-203 of them one by one, must
-    unbind exactly the particles the oracle's FP64 loop unbinds."""
+    """Groups above 1024 members take the staged-energy removal paths (one
+    block per group, or one thread-block cluster per group with the members
+    in the blocks' shared memory): unbind-only mode on three groups of
+    1790-4075 members, with a twelfth of their members sped up fourfold so
+    that each loses 89-203 of them one by one, must unbind exactly the
+    particles the oracle's FP64 loop unbinds, for every block size."""
     from skid_gb300 import gpu, tipsy
     from skid_gb300.options import Options
     from tests.helpers import small_snapshot
@@ -145,17 +146,23 @@ def test_unbind_large_groups_fp32_path(gpu_ready):
     cen["vcm"] = r1["groups"]["vcm"]
     removed = cnt[big] - np.bincount(r2["grp"], minlength=len(cnt))[big]
     assert removed.min() >= 50
-    for bs in (256, 512, 1024):
+    # block sizes, and the thread-block-cluster path (groups above 1025
+    # members shared by a cluster of blocks holding them in shared memory)
+    for bs, tw, cmin in ((256, 1024, 0), (512, 1024, 0), (1024, 1024, 0), (256, 512, 1025),
+                         (512, 512, 1025), (1024, 256, 1025)):
         with _ctx(opts) as ctx:
-            ctx.set_option("unbind_warp_max", 1024)
+            ctx.set_option("unbind_warp_max", tw)
             ctx.set_option("unbind_block", bs)
+            ctx.set_option("unbind_cluster_min", cmin)
             ctx.set_particles(snap)
             ctx.set_groups(r1["grp"], cen)
             nu = ctx.unbind(opts.iSoftType, opts.fScoop, opts.bGasAndDark, opts.bNoUnbind,
                             opts.nMaxMembers, opts.G, opts.z, opts.a_shift, opts.a_hubble)
             grp, rec = ctx.get_groups(ng)
-        assert nu == r2["nUnbound"], bs
-        assert np.array_equal(grp, r2["grp"]), bs
+            nclu = ctx.get_option("unbind_cluster_groups")
+        assert (nclu >= len(big)) if cmin else (nclu == 0), (bs, cmin, nclu)
+        assert nu == r2["nUnbound"], (bs, cmin)
+        assert np.array_equal(grp, r2["grp"]), (bs, cmin)
         og = r2["groups"]
         np.testing.assert_allclose(rec["fMass"][big], og["fMass"][big], rtol=1e-6)
         np.testing.assert_allclose(rec["vcm"][big], og["vcm"][big], rtol=1e-4, atol=1e-6)
@@ -194,18 +201,25 @@ def test_unbind_isolated_config1_2e21(gpu_ready):
     cen = np.zeros(ng + 1, gpu.GROUP_DTYPE)
     cen["rCenter"] = rec0["rCenter"]
     cen["vcm"] = rec0["vcm"]
-    with _ctx(opts) as ctx:
-        ctx.set_particles(snap)
-        ctx.set_groups(grp0, cen)
-        nu = ctx.unbind(opts.iSoftType, opts.fScoop, opts.bGasAndDark, opts.bNoUnbind,
-                        opts.nMaxMembers, opts.G, opts.z, opts.a_shift, opts.a_hubble)
-        grp, rec = ctx.get_groups(ng)
     big = np.nonzero(sizes > 1024)[0] + 1
     lost_big = int(np.sum(sizes[big - 1] - np.bincount(r2["grp"], minlength=ng + 1)[big]))
     assert lost_big > 10000
-    assert nu == r2["nUnbound"]
-    assert np.array_equal(grp, r2["grp"])
     og = r2["groups"]
     keep = og["nMembers"][1:] > 0
-    np.testing.assert_allclose(rec["fMass"][1:][keep], og["fMass"][1:][keep], rtol=1e-6)
-    assert np.abs(rec["rBound"][1:][keep] - og["rBound"][1:][keep]).max() < 1e-5
+    # the tuned schedule, then a fixed one with the largest groups on
+    # thread-block clusters (their members in the blocks' shared memory)
+    for setting in ({}, {"unbind_warp_max": 1024, "unbind_block": 512, "unbind_cluster_min": 2048}):
+        with _ctx(opts) as ctx:
+            for k, v in setting.items():
+                ctx.set_option(k, v)
+            ctx.set_particles(snap)
+            ctx.set_groups(grp0, cen)
+            nu = ctx.unbind(opts.iSoftType, opts.fScoop, opts.bGasAndDark, opts.bNoUnbind,
+                            opts.nMaxMembers, opts.G, opts.z, opts.a_shift, opts.a_hubble)
+            grp, rec = ctx.get_groups(ng)
+            if setting:
+                assert ctx.get_option("unbind_cluster_groups") > 0
+        assert nu == r2["nUnbound"], setting
+        assert np.array_equal(grp, r2["grp"]), setting
+        np.testing.assert_allclose(rec["fMass"][1:][keep], og["fMass"][1:][keep], rtol=1e-6)
+        assert np.abs(rec["rBound"][1:][keep] - og["rBound"][1:][keep]).max() < 1e-5
