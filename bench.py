@@ -520,8 +520,9 @@ def run_gpu(args):
                  "moving_ms": round(float(pres.timings["moving_ms"]), 3)}
         opts_nsp = Options.parse(flags() + ["-nsp"])
         pipeline.run(snap, opts_nsp, ctx=ctx, upload=False)   # warm-up (graphs for -nsp)
-        n_ms, nres = timed_runs(ctx, opts_nsp, 1)
-        nsp = {"value": world * n / (n_ms[0] / 1000.0), "ms_per_step": n_ms[0],
+        n_ms, nres = timed_runs(ctx, opts_nsp, min(args.steps, 5))
+        nsp = {"value": world * n * len(n_ms) / (sum(n_ms) / 1000.0),
+               "ms_per_step": sum(n_ms) / len(n_ms), "steps": len(n_ms),
                "groups": nres.n_group, "iterations": nres.counts.get("nIter"),
                "stage_ms": {k: round(float(nres.timings[k]), 3) for k in
                             ("density_ms", "moving_ms", "unbind_ms")}}
@@ -537,6 +538,9 @@ def run_gpu(args):
         return 0
     cpu = None if args.no_cpu_baseline else cpu_baseline()
     cli = None if args.no_cli else cli_process_wall(snap)
+    extra = None
+    if not args.no_extra and world == 1 and CONFIG == 1:
+        extra = {"adjoint_2e20": adjoint_workload(3), "mixed_2e24": mixed_workload(2)}
     tm = res.timings
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -564,11 +568,14 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "kernel": "field_kernel (move-field gather + move)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": field_traffic(),
+                     "traffic_source": "static: mean DRAM read+write bytes per launch from the "
+                                       "committed ncu capture "
+                                       "(profiles/field_kernel_skid_config1_2e21.md)",
                      "launches": f_launch, "avg_launch_ms": f_ms / max(f_launch, 1),
                      "algorithmic_bytes_per_launch": f_bytes / max(f_launch, 1),
                      "issue": {"frac": field_issue(), "unit": "fraction of peak issue slots",
-                               "source": "ncu issue active, one launch at full activity "
-                                         "(profiles/field_kernel_skid_config1_2e21.md)"}},
+                               "source": "static: ncu issue active of one launch at full "
+                                         "activity (profiles/field_kernel_skid_config1_2e21.md)"}},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
@@ -576,6 +583,8 @@ def run_gpu(args):
         line["cpu_baseline"] = cpu
     if cli:
         line["cli_process"] = cli
+    if extra:
+        line["configs"] = extra
     print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
@@ -590,9 +599,15 @@ def synth_n(config):
 
 
 def run_adjoint(args):
+    """Config 3 alone: prints adjoint_workload's line."""
+    print(json.dumps(adjoint_workload(args.steps, args.check)), flush=True)
+    return 0
+
+
+def adjoint_workload(steps, check_fd=False):
     """Config 3: N = 2^20.  Times the density adjoint (dL/dx of sum w_i rho_i,
     both neighbour modes) and the potential-energy adjoint of the 200 largest
-    groups, after the ordinary pipeline up to the group centres; with --check,
+    groups, after the ordinary pipeline up to the group centres; with check_fd,
     compares 1024 random particles with FP64 central differences (h = 1e-6)."""
     import torch
     from skid_gb300 import build, gpu, synth
@@ -622,8 +637,8 @@ def run_adjoint(args):
     ctx.scatter_active(False, False)
     ctx.density()
     dens_ms, _ = timed(lambda: (ctx.restart(), ctx.scatter_active(False, False), ctx.density()), 3)
-    walk_ms, g_walk = timed(lambda: ctx.density_adjoint(w, gpu.ADJ_RECOMPUTE), max(2, args.steps))
-    list_ms, g_list = timed(lambda: ctx.density_adjoint(w, gpu.ADJ_STORED), max(2, args.steps))
+    walk_ms, g_walk = timed(lambda: ctx.density_adjoint(w, gpu.ADJ_RECOMPUTE), max(2, steps))
+    list_ms, g_list = timed(lambda: ctx.density_adjoint(w, gpu.ADJ_STORED), max(2, steps))
     ctx.init_move(opts.fDensMin, opts.fTempMax, opts.fMassMax, False, False)
     ctx.move_step(opts.fStep, True, False)
     na = 1
@@ -635,10 +650,10 @@ def run_adjoint(args):
     sizes = np.bincount(grp, minlength=ng + 1)[1:]
     sel = (np.argsort(-sizes, kind="stable")[:200] + 1).astype(np.int32)
     v = rng.standard_normal(len(sel)).astype(np.float32)
-    pot_ms, (E, gpot) = timed(lambda: ctx.potential_adjoint(sel, v, G=opts.G), max(2, args.steps))
+    pot_ms, (E, gpot) = timed(lambda: ctx.potential_adjoint(sel, v, G=opts.G), max(2, steps))
     ctx.close()
     check = None
-    if args.check:
+    if check_fd:
         from oracle import oracle
         pick = rng.choice(snap.n, 1024, replace=False)
         an, fd, ab = oracle.density_adjoint_check(snap.pos, snap.mass, w, opts.nSmooth, 1.0, pick)
@@ -659,8 +674,59 @@ def run_adjoint(args):
                        "density_adjoint_stored_ms": list_ms,
                        "potential_adjoint_ms": pot_ms, "potential_groups": len(sel),
                        "potential_pairs": pairs, "check": check}}
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
+
+
+def mixed_workload(steps=2):
+    """Config 4 at full size: 2^24 gas + dark particles (-gd, z = 0.5,
+    Zel'dovich k^-2 background), resident and end-to-end particles/s over
+    `steps` runs after one warm-up (whose first unbinding tunes the schedule).
+    Its parity case is the 32768-particle slice of the same generator run by
+    reference skid (tests/golden/config4_slice_32k)."""
+    import torch
+    from skid_gb300 import gpu, pipeline, synth, tipsy
+    from skid_gb300.options import Options
+    t = time.perf_counter()
+    snap = synth.make_snapshot(synth.CONFIGS[4])
+    gen_s = time.perf_counter() - t
+
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a, np.float32)).pin_memory().numpy()
+    snap = tipsy.Snapshot(snap.time, snap.n_gas, snap.n_dark, snap.n_star, pinned(snap.pos),
+                          pinned(snap.vel), pinned(snap.mass), pinned(snap.soft),
+                          pinned(snap.temp))
+    opts = Options.parse(synth.WORKLOAD_FLAGS[4])
+    ctx = gpu.Context(period=1.0, nSmooth=opts.nSmooth)
+    strm = torch.cuda.ExternalStream(ctx.stream_ptr())
+    res = pipeline.run(snap, opts, ctx=ctx)
+
+    def timed(upload):
+        ms = []
+        out = None
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(strm)
+            out = pipeline.run(snap, opts, ctx=ctx, upload=upload)
+            e1.record(strm)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return sum(ms) / len(ms), out
+    r_ms, res = timed(False)
+    e_ms, _ = timed(True)
+    ctx.close()
+    tm = res.timings
+    return {"workload": "config 4: N=2^24 (50% gas of mass 0.2, 50% dark), 6000 NFW halos "
+                        "(3.5 dex, c 4-20, 50%) + Zel'dovich-displaced k^-2 Gaussian random "
+                        "field background, z = 0.5, -gd",
+            "flags": " ".join(synth.WORKLOAD_FLAGS[4]), "n_particles": snap.n,
+            "value": snap.n / (r_ms / 1000.0), "ms_per_step": r_ms,
+            "e2e_value": snap.n / (e_ms / 1000.0), "e2e_ms_per_step": e_ms, "steps": steps,
+            "groups": res.n_group, "groups_before_unbind": res.counts.get("nGroupFoF"),
+            "unbound": res.counts.get("nUnbound"), "iterations": res.counts.get("nIter"),
+            "stage_ms": {k: round(float(tm[k]), 3) for k in
+                         ("density_ms", "moving_ms", "fof_ms", "micro_ms", "unbind_ms")},
+            "generation_s": round(gen_s, 1)}
 
 
 def run_batch(args):
@@ -717,6 +783,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cli", action="store_true",
                     help="skip the skid command-line process wall-time runs")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the adjoint (2^20) and mixed-species (2^24) workload runs")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain-form and -nsp comparison runs")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "mixed", "adjoint"],
