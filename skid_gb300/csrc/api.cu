@@ -880,7 +880,10 @@ int skid_prune_inactive(skid_ctx *ctx, float fCvg, int *nActive)
     return 0;
 }
 
-static int graph_slot(int G) { return G == 32 ? 0 : G == 16 ? 1 : G == 8 ? 2 : G == 4 ? 3 : 4; }
+static int graph_slot(int G)
+{
+    return G == 32 ? 0 : G == 16 ? 1 : G == 8 ? 2 : G == 4 ? 3 : G == 64 ? 5 : 4;
+}
 
 int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *nActive,
                       int *nScatter)
@@ -1025,8 +1028,11 @@ int skid_set_option(skid_ctx *ctx, const char *name, double value)
     if (!ctx || !name) return SKID_EINVAL;
     int v = (int)value;
     if (!strcmp(name, "field_movers_per_warp")) {
-        if (v != 0 && v != 1 && v != 4 && v != 8 && v != 16 && v != 32) return SKID_EINVAL;
+        if (v != 0 && v != 1 && v != 4 && v != 8 && v != 16 && v != 32 && v != 64) return SKID_EINVAL;
         ctx->opt_G = v;
+    } else if (!strcmp(name, "field_g64_min")) {
+        if (v < 0) return SKID_EINVAL;
+        ctx->opt_g64_min = v;
     } else if (!strcmp(name, "field_g32_min")) {
         if (v < 0) return SKID_EINVAL;
         ctx->opt_g32_min = v;
@@ -1068,6 +1074,7 @@ int skid_get_option(skid_ctx *ctx, const char *name, double *value)
     if (!ctx || !name || !value) return SKID_EINVAL;
     if (!strcmp(name, "field_movers_per_warp")) *value = ctx->opt_G;
     else if (!strcmp(name, "field_g32_min")) *value = ctx->opt_g32_min;
+    else if (!strcmp(name, "field_g64_min")) *value = ctx->opt_g64_min;
     else if (!strcmp(name, "field_g16_min")) *value = ctx->opt_g16_min;
     else if (!strcmp(name, "field_g8_min")) *value = ctx->opt_g8_min;
     else if (!strcmp(name, "field_g4_min")) *value = ctx->opt_g4_min;

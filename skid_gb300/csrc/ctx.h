@@ -191,7 +191,7 @@ struct skid_ctx {
     skid::AdjointState adj;         // density / potential adjoints
 
     // outer-iteration CUDA graphs, one per movers-per-warp setting
-    static constexpr int NSLOT = 5;          // movers per warp 32, 16, 8, 4, 1
+    static constexpr int NSLOT = 6;          // movers per warp 32, 16, 8, 4, 1, 64
     cudaGraphExec_t iter_graph[NSLOT] = {};
     long long iter_graph_kernels[NSLOT] = {};
     float g_fStep[NSLOT] = {}, g_fCvg[NSLOT] = {};
@@ -264,6 +264,7 @@ struct skid_ctx {
     // move-field time is lowest with 32 movers per warp above ~600k active
     // movers, 16 down to ~400k, 8 down to ~50k, 4 down to ~25k, one below.
     int opt_G = 0, opt_g32_min = 600000, opt_g16_min = 400000, opt_g8_min = 100000, opt_g4_min = 30000;
+    int opt_g64_min = 0;                          // 64 movers per warp at or above (0: never)
     int opt_unbind_tw = -1, opt_unbind_bs = -1;   // -1: autotuned on the first skid_unbind
     int opt_unbind_clu_min = 2048;                // the largest groups above it may take a block cluster; 0 = never
     bool opt_unbind_per_group = false;
@@ -273,7 +274,8 @@ struct skid_ctx {
     // for G is sized for it; the count only falls within a run).
     int slot_bound(int G) const
     {
-        int b = opt_G || G == 32 ? M.cap
+        int b = opt_G || G == 64 || (G == 32 && !opt_g64_min) ? M.cap
+                : G == 32        ? opt_g64_min
                 : G == 16        ? opt_g32_min
                 : G == 8         ? opt_g16_min
                 : G == 4         ? opt_g8_min
@@ -284,7 +286,8 @@ struct skid_ctx {
     int movers_per_warp() const
     {
         if (opt_G) return opt_G;
-        return nActive >= opt_g32_min   ? 32
+        return opt_g64_min && nActive >= opt_g64_min ? 64
+               : nActive >= opt_g32_min ? 32
                : nActive >= opt_g16_min ? 16
                : nActive >= opt_g8_min  ? 8
                : nActive >= opt_g4_min  ? 4

@@ -170,18 +170,21 @@ density_kernel(TreeView t, const float *__restrict__ ball2, float3 L, float3 hL,
     }
 }
 
-// Movers per warp G: 32, 16, 8, 4 or 1, with 32/G lanes per mover.  Fewer
-// movers per warp keep the union of their neighbourhoods small when the
-// active movers are sparse.  At a visited leaf the candidates whose ball
-// reaches the movers' box are compacted in order; a mover's lanes test every
-// (32/G)-th of them (one cheap pass that sets a hit mask), then run the field
-// terms for their hits only, and are combined with a fixed xor-butterfly, so
-// sums are deterministic for a given G.
+// Movers per warp G: 64, 32, 16, 8, 4 or 1; with G <= 32, 32/G lanes per
+// mover, and with G = 64 two movers per lane.  More movers per warp share
+// the tree walk and the leaf staging among more of them while the active
+// movers are dense; fewer keep the union of their neighbourhoods small when
+// they are sparse.  At a visited leaf the candidates whose ball reaches the
+// movers' box are compacted in order; a mover's lanes test every (32/G)-th
+// of them (one cheap pass that sets a hit mask), then run the field terms for
+// their hits only, and are combined with a fixed xor-butterfly, so sums are
+// deterministic for a given G.
 template <int G, bool STATS>
-__global__ void __launch_bounds__(G_WARPS * 32, SKID_FIELD_MINB)
+__global__ void __launch_bounds__(G_WARPS * 32, G > 32 ? 10 : SKID_FIELD_MINB)
 field_kernel(FieldArgs a)
 {
-    constexpr int L = 32 / G;   // lanes per mover
+    constexpr int MPL = G > 32 ? G / 32 : 1;   // movers per lane
+    constexpr int L = G >= 32 ? 1 : 32 / G;    // lanes per mover
     __shared__ float4 cpos_s[G_WARPS][SKID_LEAF];
     __shared__ float2 ccoef_s[G_WARPS][SKID_LEAF];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -208,14 +211,25 @@ field_kernel(FieldArgs a)
             part = item % S;
             item /= S;
         }
-        int slot = item * G + lane / L;
-        bool valid = slot < nA;
-        int mi = a.act[valid ? slot : item * G];
-        float4 yp = a.mpos[mi];
-        float3 y = make_float3(yp.x, yp.y, yp.z);
+        int slot[MPL], mi[MPL];
+        bool valid[MPL];
+        float4 yp[MPL];
+        float3 y[MPL];
         // bounding box of the warp's movers, for the per-leaf candidate prefilter
-        float3 wlo = valid ? y : make_float3(FLT_MAX, FLT_MAX, FLT_MAX);
-        float3 whi = valid ? y : make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+        float3 wlo = make_float3(FLT_MAX, FLT_MAX, FLT_MAX);
+        float3 whi = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+#pragma unroll
+        for (int k = 0; k < MPL; ++k) {
+            slot[k] = item * G + k * 32 + lane / L;
+            valid[k] = slot[k] < nA;
+            mi[k] = a.act[valid[k] ? slot[k] : item * G];
+            yp[k] = a.mpos[mi[k]];
+            y[k] = make_float3(yp[k].x, yp[k].y, yp[k].z);
+            if (valid[k]) {
+                wlo = make_float3(fminf(wlo.x, y[k].x), fminf(wlo.y, y[k].y), fminf(wlo.z, y[k].z));
+                whi = make_float3(fmaxf(whi.x, y[k].x), fmaxf(whi.y, y[k].y), fmaxf(whi.z, y[k].z));
+            }
+        }
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             wlo.x = fminf(wlo.x, __shfl_xor_sync(SKID_FULL, wlo.x, o));
@@ -225,7 +239,9 @@ field_kernel(FieldArgs a)
             whi.y = fmaxf(whi.y, __shfl_xor_sync(SKID_FULL, whi.y, o));
             whi.z = fmaxf(whi.z, __shfl_xor_sync(SKID_FULL, whi.z, o));
         }
-        float ax = 0.0f, ay = 0.0f, az = 0.0f;
+        float ax[MPL], ay[MPL], az[MPL];
+#pragma unroll
+        for (int k = 0; k < MPL; ++k) ax[k] = ay[k] = az[k] = 0.0f;
         // Depth-first walk by ball boxes in strides of five levels, aligned
         // so the last stride ends at the leaves: a visited node has each lane
         // test one of its 32 descendants five levels down against the movers'
@@ -254,8 +270,12 @@ field_kernel(FieldArgs a)
             if (STATS) ++st_nodes;
             {
                 float4 blo = a.blo[node], bhi = a.bhi[node];
-                bool want = valid && y.x >= blo.x && y.x <= bhi.x && y.y >= blo.y &&
-                            y.y <= bhi.y && y.z >= blo.z && y.z <= bhi.z;
+                bool want = false;
+#pragma unroll
+                for (int k = 0; k < MPL; ++k)
+                    want = want || (valid[k] && y[k].x >= blo.x && y[k].x <= bhi.x &&
+                                    y[k].y >= blo.y && y[k].y <= bhi.y && y[k].z >= blo.z &&
+                                    y[k].z <= bhi.z);
                 if (!__any_sync(SKID_FULL, want)) continue;
                 if (node < a.leafBase) {
                     const int cf = node << 5;
@@ -303,87 +323,103 @@ field_kernel(FieldArgs a)
                 }
                 __syncwarp();
                 // a mover's L lanes take every L-th survivor
-                unsigned mask = 0;
+                unsigned mask[MPL];
+#pragma unroll
+                for (int k = 0; k < MPL; ++k) mask[k] = 0;
                 if (want) {
 #pragma unroll FIELD_UNROLL
                     for (int t = sub; t < nR; t += L) {
                         float4 c = cpos_s[w][t];
-                        // smBallGather's test (smooth1.c:365-369), from the copy
-                        float d2 = d2of(fsub(c.x, y.x), fsub(c.y, y.y), fsub(c.z, y.z));
-                        mask |= (unsigned)(d2 < c.w) << t;
+#pragma unroll
+                        for (int k = 0; k < MPL; ++k) {
+                            // smBallGather's test (smooth1.c:365-369), from the copy
+                            float d2 = d2of(fsub(c.x, y[k].x), fsub(c.y, y[k].y), fsub(c.z, y[k].z));
+                            mask[k] |= (unsigned)(d2 < c.w) << t;
+                        }
                     }
-                    if (STATS) st_tests += (nR - sub + L - 1) / L;
+                    if (STATS) st_tests += MPL * ((nR - sub + L - 1) / L);
                 }
-                if (STATS) st_hits += __popc(mask);
-                for (unsigned m = mask; m; m &= m - 1) {
-                    int j = __ffs(m) - 1;
-                    float4 c = cpos_s[w][j];
-                    float2 k = ccoef_s[w][j];
-                    // the field value (smooth1.c:450-458) only has to be
-                    // accurate, not bit-exact: FMA and the approximate
-                    // reciprocal square root (q = r2 / sqrt(r2), 1/q)
-                    float dx = c.x - y.x, dy = c.y - y.y, dz = c.z - y.z;
-                    float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) * k.x;
-                    float iq = rsqrtf(r2);
-                    float q = r2 > 0.0f ? r2 * iq : 0.0f;
-                    float F = r2 < 1.0f ? __fmaf_rn(2.25f, q, -3.0f)
-                                        : __fmaf_rn(-0.75f, q, 3.0f) - 3.0f * iq;
-                    F *= k.y;
-                    ax = __fmaf_rn(dx, F, ax);
-                    ay = __fmaf_rn(dy, F, ay);
-                    az = __fmaf_rn(dz, F, az);
+                unsigned hitany = 0;
+#pragma unroll
+                for (int k = 0; k < MPL; ++k) {
+                    hitany |= mask[k];
+                    if (STATS) st_hits += __popc(mask[k]);
+                    for (unsigned m = mask[k]; m; m &= m - 1) {
+                        int j = __ffs(m) - 1;
+                        float4 c = cpos_s[w][j];
+                        float2 cf = ccoef_s[w][j];
+                        // the field value (smooth1.c:450-458) only has to be
+                        // accurate, not bit-exact: FMA and the approximate
+                        // reciprocal square root (q = r2 / sqrt(r2), 1/q)
+                        float dx = c.x - y[k].x, dy = c.y - y[k].y, dz = c.z - y[k].z;
+                        float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) * cf.x;
+                        float iq = rsqrtf(r2);
+                        float q = r2 > 0.0f ? r2 * iq : 0.0f;
+                        float F = r2 < 1.0f ? __fmaf_rn(2.25f, q, -3.0f)
+                                            : __fmaf_rn(-0.75f, q, 3.0f) - 3.0f * iq;
+                        F *= cf.y;
+                        ax[k] = __fmaf_rn(dx, F, ax[k]);
+                        ay[k] = __fmaf_rn(dy, F, ay[k]);
+                        az[k] = __fmaf_rn(dz, F, az[k]);
+                    }
                 }
                 // copies that reached a mover: touched, and their density
                 // enters the floor of the cut (smooth1.c:460-461)
-                unsigned any = __reduce_or_sync(SKID_FULL, mask);
+                unsigned any = __reduce_or_sync(SKID_FULL, hitany);
                 if (rel && ((any >> slotR) & 1u)) a.touched[cb + lane] = 1;
             }
         }
 #pragma unroll
         for (int o = L / 2; o > 0; o >>= 1) {
-            ax = fadd(ax, __shfl_xor_sync(SKID_FULL, ax, o));
-            ay = fadd(ay, __shfl_xor_sync(SKID_FULL, ay, o));
-            az = fadd(az, __shfl_xor_sync(SKID_FULL, az, o));
+            ax[0] = fadd(ax[0], __shfl_xor_sync(SKID_FULL, ax[0], o));
+            ay[0] = fadd(ay[0], __shfl_xor_sync(SKID_FULL, ay[0], o));
+            az[0] = fadd(az[0], __shfl_xor_sync(SKID_FULL, az[0], o));
         }
-        if (!valid || sub != 0) continue;
-        if (G == 1 && S > 1) {
-            // the last of the mover's S parts sums them in part order
-            float *pa = a.part_acc + 3 * ((size_t)slot * S + part);
-            pa[0] = ax;
-            pa[1] = ay;
-            pa[2] = az;
-            __threadfence();
-            if (atomicAdd(&a.part_cnt[slot], 1) != S - 1) continue;
-            __threadfence();
-            ax = ay = az = 0.0f;
-            for (int p = 0; p < S; ++p) {
-                const float *q = a.part_acc + 3 * ((size_t)slot * S + p);
-                ax = fadd(ax, __ldcg(q));
-                ay = fadd(ay, __ldcg(q + 1));
-                az = fadd(az, __ldcg(q + 2));
+        if (sub != 0) continue;
+#pragma unroll
+        for (int k = 0; k < MPL; ++k) {
+            if (!valid[k]) continue;
+            float fx = ax[k], fy = ay[k], fz = az[k];
+            if (G == 1 && S > 1) {
+                // the last of the mover's S parts sums them in part order
+                float *pa = a.part_acc + 3 * ((size_t)slot[k] * S + part);
+                pa[0] = fx;
+                pa[1] = fy;
+                pa[2] = fz;
+                __threadfence();
+                if (atomicAdd(&a.part_cnt[slot[k]], 1) != S - 1) continue;
+                __threadfence();
+                fx = fy = fz = 0.0f;
+                for (int p = 0; p < S; ++p) {
+                    const float *q = a.part_acc + 3 * ((size_t)slot[k] * S + p);
+                    fx = fadd(fx, __ldcg(q));
+                    fy = fadd(fy, __ldcg(q + 1));
+                    fz = fadd(fz, __ldcg(q + 2));
+                }
+                a.part_cnt[slot[k]] = 0;
             }
-            a.part_cnt[slot] = 0;
-        }
-        if (a.acc_out) {
-            a.acc_out[3 * (size_t)slot + 0] = ax;
-            a.acc_out[3 * (size_t)slot + 1] = ay;
-            a.acc_out[3 * (size_t)slot + 2] = az;
-        }
-        if (a.fStep > 0.0f) {
-            // kdMoveParticles (kd.c:711-728)
-            float s = d2of(ax, ay, az);
-            float ai = sqrtf(s);
-            ai = ai > 0.0f ? __fdiv_rn(a.fStep, ai) : 0.0f;
-            y.x = fsub(y.x, fmul(ai, ax));
-            y.y = fsub(y.y, fmul(ai, ay));
-            y.z = fsub(y.z, fmul(ai, az));
-            if (y.x > a.wrapHi.x) y.x = fsub(y.x, a.period.x);
-            if (y.x <= a.wrapLo.x) y.x = fadd(y.x, a.period.x);
-            if (y.y > a.wrapHi.y) y.y = fsub(y.y, a.period.y);
-            if (y.y <= a.wrapLo.y) y.y = fadd(y.y, a.period.y);
-            if (y.z > a.wrapHi.z) y.z = fsub(y.z, a.period.z);
-            if (y.z <= a.wrapLo.z) y.z = fadd(y.z, a.period.z);
-            a.mpos[mi] = make_float4(y.x, y.y, y.z, yp.w);
+            if (a.acc_out) {
+                a.acc_out[3 * (size_t)slot[k] + 0] = fx;
+                a.acc_out[3 * (size_t)slot[k] + 1] = fy;
+                a.acc_out[3 * (size_t)slot[k] + 2] = fz;
+            }
+            if (a.fStep > 0.0f) {
+                // kdMoveParticles (kd.c:711-728)
+                float3 yk = y[k];
+                float s2 = d2of(fx, fy, fz);
+                float ai = sqrtf(s2);
+                ai = ai > 0.0f ? __fdiv_rn(a.fStep, ai) : 0.0f;
+                yk.x = fsub(yk.x, fmul(ai, fx));
+                yk.y = fsub(yk.y, fmul(ai, fy));
+                yk.z = fsub(yk.z, fmul(ai, fz));
+                if (yk.x > a.wrapHi.x) yk.x = fsub(yk.x, a.period.x);
+                if (yk.x <= a.wrapLo.x) yk.x = fadd(yk.x, a.period.x);
+                if (yk.y > a.wrapHi.y) yk.y = fsub(yk.y, a.period.y);
+                if (yk.y <= a.wrapLo.y) yk.y = fadd(yk.y, a.period.y);
+                if (yk.z > a.wrapHi.z) yk.z = fsub(yk.z, a.period.z);
+                if (yk.z <= a.wrapLo.z) yk.z = fadd(yk.z, a.period.z);
+                a.mpos[mi[k]] = make_float4(yk.x, yk.y, yk.z, yp[k].w);
+            }
         }
     }
     if (STATS && a.stats) {
@@ -489,6 +525,7 @@ cudaError_t field_move(const FieldArgs &a, int max_movers, cudaStream_t st)
     cudaError_t e = cudaMemsetAsync(a.d_work, 0, sizeof(int), st);
     if (e) return e;
     switch (a.G) {
+    case 64: return launch_field<64>(a, max_movers, st);
     case 1: return launch_field<1>(a, max_movers, st);
     case 4: return launch_field<4>(a, max_movers, st);
     case 8: return launch_field<8>(a, max_movers, st);

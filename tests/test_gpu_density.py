@@ -52,8 +52,8 @@ def test_knn_probe_brute(gpu_ready):
             assert np.array_equal(b, oracle.knn_ball2(pos, k, 1.0, brute=True))
 
 
-@pytest.mark.parametrize("period,G", [(1.0, 32), (None, 32), (1.0, 16), (1.0, 8), (None, 4),
-                                      (1.0, 1)])
+@pytest.mark.parametrize("period,G", [(1.0, 64), (None, 64), (1.0, 32), (None, 32), (1.0, 16),
+                                      (1.0, 8), (None, 4), (1.0, 1)])
 def test_move_field(gpu_ready, period, G):
     """The move field (minus grad rho, smooth1.c:447-459) at every particle,
     for each number of movers per warp the move step uses."""
@@ -75,3 +75,22 @@ def test_move_field(gpu_ready, period, G):
     acc_or, absacc, _ = oracle.field(snap.pos, snap.mass, b, mask, probe, period)
     err = np.linalg.norm(acc - acc_or, axis=1) / np.maximum(absacc, 1e-30)
     assert err.max() < 1e-5, f"field norm-wise err {err.max():.3g}"
+
+
+@pytest.mark.parametrize("period", [1.0, None])
+def test_move_field_two_movers_per_lane_is_one(gpu_ready, period):
+    """With 64 movers per warp each lane holds two movers, and with 32 one;
+    either way a mover's hits are summed by one lane in the same order (leaves
+    depth first, candidates in leaf order), so the fields are bit-identical."""
+    from skid_gb300 import gpu
+    snap = small_snapshot(n=8192, seed=22)
+    out = []
+    for G in (32, 64):
+        with gpu.Context(period=period, nSmooth=64) as ctx:
+            ctx.set_option("field_movers_per_warp", G)
+            ctx.set_particles(snap)
+            ctx.scatter_active()
+            ctx.density()
+            ctx.init_move()
+            out.append(ctx.field(snap.pos))
+    assert np.array_equal(out[0], out[1])
