@@ -6,8 +6,8 @@
 // runs the pipelines of several volumes at once: each host worker owns a
 // context (its own stream and device memory) and takes volumes from a shared
 // queue, largest first, so the long volumes start early and the short ones
-// fill the gaps.  Contexts keep their buffers, captured move-iteration graphs
-// and autotuned unbinding schedule from one volume to the next.  The calls
+// fill the gaps.  Contexts keep their buffers from one volume to the next,
+// and use the usual removal schedule rather than tuning their own.  The calls
 // per volume are exactly the single-volume sequence of the reference driver
 // (main.c:374-485), so every volume's result equals a run of its own.
 #include <algorithm>
@@ -134,6 +134,12 @@ extern "C" int skid_batch_run(skid_volume *vols, int nVol, const skid_batch_flag
             // no context: the volumes this worker would have taken are left to the others
             return;
         }
+        // Each worker's context would otherwise time the 18 candidate removal
+        // schedules on its first volume, every batch: the volumes take the
+        // schedule the tuner picks on clustered snapshots instead (a warp per
+        // group of up to 1024 members, 512-thread blocks above).
+        skid_set_option(ctx, "unbind_warp_max", 1024);
+        skid_set_option(ctx, "unbind_block", 512);
         for (;;) {
             int k = next.fetch_add(1);
             if (k >= nVol) break;
