@@ -896,7 +896,7 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
     int gs = graph_slot(G);
     bool same = ctx->iter_graph[gs] && ctx->g_fStep[gs] == fStep && ctx->g_fCvg[gs] == fCvg &&
                 ctx->g_nocut[gs] == (bNoCut != 0) && ctx->g_stats[gs] == ctx->field_stats_on &&
-                ctx->g_bound[gs] >= ctx->nActive;
+                ctx->g_bound[gs] >= ctx->nActive && ctx->g_key[gs] == ctx->graph_key();
     bool ran = false;
     if (!same) {
         if (ctx->iter_graph[gs]) {
@@ -948,6 +948,7 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
             ctx->g_nocut[gs] = bNoCut != 0;
             ctx->g_stats[gs] = ctx->field_stats_on;
             ctx->g_bound[gs] = bound;
+            ctx->g_key[gs] = ctx->graph_key();
         }
     }
     if (!ran) {

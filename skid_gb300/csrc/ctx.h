@@ -198,6 +198,38 @@ struct skid_ctx {
     bool g_nocut[NSLOT] = {};
     bool g_stats[NSLOT] = {};
     int g_bound[NSLOT] = {};                 // active movers the graph's prune is sized for
+    // What else a captured iteration bakes in: the buffers (allocation
+    // epoch), the copy tree's shape, the mover and copy counts and the
+    // movers' Morton key frame.  A graph whose key still matches is replayed
+    // in later runs instead of being captured again.
+    struct GraphKey {
+        unsigned long long epoch = 0;
+        int leafBase = 0, nMove = 0, nScat = 0, nExtra = 0, n = 0;
+        float klo[3] = {}, kinv[3] = {};
+        bool unfused = false;
+        bool operator==(const GraphKey &o) const
+        {
+            return epoch == o.epoch && leafBase == o.leafBase && nMove == o.nMove &&
+                   nScat == o.nScat && nExtra == o.nExtra && n == o.n && klo[0] == o.klo[0] &&
+                   klo[1] == o.klo[1] && klo[2] == o.klo[2] && kinv[0] == o.kinv[0] &&
+                   kinv[1] == o.kinv[1] && kinv[2] == o.kinv[2] && unfused == o.unfused;
+        }
+    };
+    GraphKey g_key[NSLOT];
+    GraphKey graph_key() const
+    {
+        GraphKey k;
+        k.epoch = skid::alloc_epoch();
+        k.leafBase = ctree.leafBase;
+        k.nMove = nMove;
+        k.nScat = nScatInit;
+        k.nExtra = nExtraScat;
+        k.n = n;
+        k.klo[0] = mkey_lo.x; k.klo[1] = mkey_lo.y; k.klo[2] = mkey_lo.z;
+        k.kinv[0] = mkey_inv.x; k.kinv[1] = mkey_inv.y; k.kinv[2] = mkey_inv.z;
+        k.unfused = opt_field_unfused;
+        return k;
+    }
     float3 mkey_lo{}, mkey_inv{};   // Morton frame of mover positions
     // move-field kernel timing: an event pair per step slot of an iteration
     cudaEvent_t fev[2 * skid::PRUNE_STEPS] = {};
@@ -310,7 +342,8 @@ struct skid_ctx {
 
     void reset_pipeline()
     {
-        drop_graphs();
+        // the move-iteration graphs stay: skid_move_iterate replays one only
+        // while its key (graph_key) still matches
         iter_eager_done = false;
         stage = skid::STAGE_NONE;
         nScatInit = nExtraScat = nMove = nActive = 0;

@@ -24,6 +24,11 @@ constexpr int SKID_MAX_DEVICES = 64;
 // reach a dalloc that finds its buffer already large enough.
 std::recursive_mutex &device_mutex();
 
+// Counts every device (re)allocation made through dalloc, process-wide: a
+// captured graph whose count is unchanged still points at live buffers.
+unsigned long long alloc_epoch();
+void bump_alloc_epoch();
+
 template <typename T>
 struct DBuf {
     T *p = nullptr;
@@ -38,6 +43,7 @@ cudaError_t dalloc(DBuf<T> &b, size_t n)
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.n = 0;
+    bump_alloc_epoch();
     cudaError_t e = cudaMalloc((void **)&b.p, (n ? n : 1) * sizeof(T));
     if (e == cudaSuccess) b.n = n;
     return e;

@@ -40,6 +40,13 @@ std::recursive_mutex &device_mutex()
 }
 
 namespace {
+std::atomic<unsigned long long> g_alloc_epoch{0};
+}  // namespace
+
+unsigned long long alloc_epoch() { return g_alloc_epoch.load(); }
+void bump_alloc_epoch() { ++g_alloc_epoch; }
+
+namespace {
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_ROUNDS = 16;

@@ -59,3 +59,27 @@ def test_pipeline_vs_oracle(gpu_ready, seed, n, flags):
     assert res.counts["nGroupFoF"] == r["nGroupFoF"]
     assert res.counts["nGroup"] == r["nGroup"]
     assert res.counts["nIter"] == r["nIter"]
+
+
+def test_reused_context_gives_fresh_results(gpu_ready):
+    """A context replays its captured move-iteration graphs in later runs
+    while everything they depend on is unchanged, and captures new ones
+    otherwise: runs on one context of A, then B (other particles, same size),
+    then A again (uploaded, and restarted in place) must each equal a run on
+    a fresh context."""
+    from skid_gb300 import gpu, pipeline
+    from skid_gb300.options import Options
+    from tests.helpers import small_snapshot
+    opts = Options.parse(["-tau", "0.012", "-s", "32", "-m", "8", "-p", "1", "-H", "2.89441"])
+    a = small_snapshot(n=12000, n_halo=10, seed=51, r200=0.06)
+    b = small_snapshot(n=12000, n_halo=10, seed=52, r200=0.06)
+    fresh = [pipeline.run(s, opts).grp for s in (a, b)]
+    with gpu.Context(period=1.0, nSmooth=opts.nSmooth) as ctx:
+        runs = [pipeline.run(a, opts, ctx=ctx).grp, pipeline.run(b, opts, ctx=ctx).grp,
+                pipeline.run(a, opts, ctx=ctx).grp,
+                pipeline.run(a, opts, ctx=ctx, upload=False).grp,
+                pipeline.run(a, opts, ctx=ctx, upload=False).grp]
+    assert np.array_equal(runs[0], fresh[0])
+    assert np.array_equal(runs[1], fresh[1])
+    for r in runs[2:]:
+        assert np.array_equal(r, fresh[0])
