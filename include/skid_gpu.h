@@ -222,7 +222,10 @@ int skid_get_timings(skid_ctx *ctx, skid_timings *t);
 int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
 
 /* Tuning knobs (no reference counterpart).  Names:
- *   "field_movers_per_warp"  0 = by active count (default), or 32, 16, 8, 4, 1
+ *   "field_movers_per_warp"  0 = by active count (default), or 64 (two per
+ *                            lane), 32, 16, 8, 4, 1
+ *   "field_g64_min"          active movers at or above which 64 per warp
+ *                            (default 0: never)
  *   "field_g32_min"          active movers at or above which 32 per warp
  *   "field_g16_min"          ... 16 per warp
  *   "field_g8_min"           ... 8 per warp
@@ -234,6 +237,11 @@ int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
  *                            skid_unbind of the context, the fastest is kept)
  *   "unbind_block"           threads per block for larger groups: 128, 256,
  *                            512, 1024, or -1 = autotuned
+ *   "unbind_cluster_min"     groups above this size (at least 1024) may be
+ *                            removed by a cluster of blocks that hold their
+ *                            members in shared memory; 0 = never; -1 (the
+ *                            default) = above 2048, and only when the
+ *                            autotuner measured that faster
  *   "unbind_per_group"       1: one potential and one removal launch per group
  *                            (the reference's serial loop, for comparison)
  *   "unbind_retune"          forget the autotuned schedule
@@ -246,7 +254,9 @@ int skid_field_stats(skid_ctx *ctx, int enable, unsigned long long *out4);
 int skid_set_option(skid_ctx *ctx, const char *name, double value);
 
 /* Current value of a knob; for "unbind_warp_max" and "unbind_block" the
- * schedule the last skid_unbind used, "unbind_tune_candidates" the number of
+ * schedule the last skid_unbind used, "unbind_cluster_size" and
+ * "unbind_cluster_groups" its cluster size (1: none) and the number of groups
+ * it removed on clusters, "unbind_tune_candidates" the number of
  * schedules the autotuner timed, "unbind_tune_ms<k>" the removal time of
  * candidate k (warp sizes outer, block sizes inner), "unbind_pot_ms" and
  * "unbind_remove_ms" the potential and removal times of the last

@@ -1056,7 +1056,7 @@ int skid_set_option(skid_ctx *ctx, const char *name, double value)
     } else if (!strcmp(name, "unbind_per_group")) {
         ctx->opt_unbind_per_group = v != 0;
     } else if (!strcmp(name, "unbind_cluster_min")) {
-        if (v != 0 && v < 1024) return SKID_EINVAL;
+        if (v != -1 && v != 0 && v < 1024) return SKID_EINVAL;
         ctx->opt_unbind_clu_min = v;
     } else if (!strcmp(name, "field_unfused")) {
         ctx->opt_field_unfused = v != 0;

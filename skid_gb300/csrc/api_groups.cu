@@ -241,7 +241,8 @@ int skid_unbind(skid_ctx *ctx, int iSoftType, float fScoop, int bGasAndDark, int
     P.n = ctx->n;
     P.tw = ctx->opt_unbind_tw;
     P.bs = ctx->opt_unbind_bs;
-    P.clu_min = ctx->opt_unbind_clu_min;
+    P.clu_auto = ctx->opt_unbind_clu_min < 0;
+    P.clu_min = P.clu_auto ? 2048 : ctx->opt_unbind_clu_min;
     P.per_group = ctx->opt_unbind_per_group;
     CK(unbind_run(ctx->G, ctx->G.gof.p, ctx->n, ctx->pos4.p, ctx->vel4.p, ctx->utree, P, ctx->grp.p,
                   ctx->d_scal + SC_NUNB, ctx->ss, ctx->U, st));

@@ -78,6 +78,7 @@ struct UnbindParams {
     int tw, bs;        // removal schedule: warp-per-group up to tw members, blocks of bs
                        // threads above; -1 = autotuned
     int clu_min;       // the largest groups above this many members may take a block cluster (0: none)
+    bool clu_auto;     // clu_min is the default: only a tuned schedule that measured them faster uses clusters
     bool per_group;    // one potential and one removal launch per group
 };
 
@@ -298,7 +299,8 @@ struct skid_ctx {
     int opt_G = 0, opt_g32_min = 600000, opt_g16_min = 400000, opt_g8_min = 100000, opt_g4_min = 30000;
     int opt_g64_min = 0;                          // 64 movers per warp at or above (0: never)
     int opt_unbind_tw = -1, opt_unbind_bs = -1;   // -1: autotuned on the first skid_unbind
-    int opt_unbind_clu_min = 2048;                // the largest groups above it may take a block cluster; 0 = never
+    int opt_unbind_clu_min = -1;                  // the largest groups above it may take a block cluster; 0 = never;
+                                                  // -1 = 2048, and only where the tuner measured clusters faster
     bool opt_unbind_per_group = false;
     bool opt_field_unfused = false;                // field pass and move pass as separate kernels
     skid::DBuf<float> unfused_acc;

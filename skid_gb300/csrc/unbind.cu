@@ -1819,9 +1819,9 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
             return e;
     }
     // clusters: as the tuner chose for a tuned schedule; with a fixed one,
-    // whenever there are groups for them
+    // whenever there are groups for them and the caller set the threshold
     const bool tuned_sched = P.tw < 0 || P.bs < 0;
-    const int ucs = cs > 1 && (!tuned_sched || U.tuned_cs == 1) ? cs : 1;
+    const int ucs = cs > 1 && (tuned_sched ? U.tuned_cs == 1 : !P.clu_auto) ? cs : 1;
     U.used_tw = tw;
     U.used_bs = bs;
     U.used_cs = ucs;

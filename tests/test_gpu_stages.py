@@ -206,9 +206,11 @@ def test_unbind_isolated_config1_2e21(gpu_ready):
     assert lost_big > 10000
     og = r2["groups"]
     keep = og["nMembers"][1:] > 0
-    # the tuned schedule, then a fixed one with the largest groups on
+    # the tuned schedule; the fixed one the skid tool uses (no clusters
+    # unless asked for); and that one with the largest groups on
     # thread-block clusters (their members in the blocks' shared memory)
-    for setting in ({}, {"unbind_warp_max": 1024, "unbind_block": 512, "unbind_cluster_min": 2048}):
+    fixed = {"unbind_warp_max": 1024, "unbind_block": 512}
+    for setting in ({}, fixed, dict(fixed, unbind_cluster_min=2048)):
         with _ctx(opts) as ctx:
             for k, v in setting.items():
                 ctx.set_option(k, v)
@@ -217,8 +219,10 @@ def test_unbind_isolated_config1_2e21(gpu_ready):
             nu = ctx.unbind(opts.iSoftType, opts.fScoop, opts.bGasAndDark, opts.bNoUnbind,
                             opts.nMaxMembers, opts.G, opts.z, opts.a_shift, opts.a_hubble)
             grp, rec = ctx.get_groups(ng)
-            if setting:
+            if "unbind_cluster_min" in setting:
                 assert ctx.get_option("unbind_cluster_groups") > 0
+            elif setting:
+                assert ctx.get_option("unbind_cluster_groups") == 0
         assert nu == r2["nUnbound"], setting
         assert np.array_equal(grp, r2["grp"]), setting
         np.testing.assert_allclose(rec["fMass"][1:][keep], og["fMass"][1:][keep], rtol=1e-6)
