@@ -559,6 +559,8 @@ def run_gpu(args):
                    "stage_ms": {k: round(float(tm[k]), 3) for k in
                                 ("density_ms", "moving_ms", "fof_ms", "micro_ms", "groups_ms",
                                  "unbind_ms", "toosmall_ms")},
+                   "step_ms": [round(x, 3) for x in step_ms],
+                   "e2e_step_ms": [round(x, 3) for x in e2e_ms],
                    "form": "fused density-field adjoint + move kernel; every unbinding group "
                            "in one autotuned launch",
                    "unbind_schedule": sched, "plain": plain, "nsp": nsp},

@@ -307,7 +307,7 @@ int skid_ctx::enqueue_step(float fStep, bool initial, bool nocut, int slot, int 
     CK(tree_refit(ctree, C.cpos.p, nullptr, C.d_n, st, true, C.d_dirty));
     // between prunes, re-sort the active movers while they are many (16 or
     // more per warp): the warps' boxes stay tight as the movers drift
-    if (!compact && G >= 16) CK(mover_resort(M, mkey_lo, mkey_inv, ss, st, slot_bound(G)));
+    if (!compact && G >= 16) CK(mover_resort(M, mkey_lo, mkey_inv, ss, st, slot_bound(G), opt_curve & 1));
     return 0;
 }
 
@@ -734,7 +734,7 @@ int skid_density(skid_ctx *ctx, int *nExtraScat)
     Ranges r = ctx->ranges;
     gather_ranges<<<grid_for(ns), 256, 0, st>>>(r, ctx->pos4.p, ctx->spos0.p, ctx->sidx0.p); skid::note_launch();
     CK(cudaGetLastError());
-    CK(tree_build(ctx->stree, ctx->spos0.p, ns, true, ctx->ss, st));
+    CK(tree_build(ctx->stree, ctx->spos0.p, ns, true, ctx->ss, st, ctx->opt_curve & 4));
     CK(knn_ball2(ctx->stree, ctx->par.nSmooth, ctx->L, ctx->per, ctx->sb2.p,
                  ctx->d_scal + SC_WORK, ctx->knn_heap, st));
     // node max fBall2 for the density gather
@@ -754,7 +754,7 @@ int skid_density(skid_ctx *ctx, int *nExtraScat)
                              (float)((double)ctx->par.center[2] + 0.5 * (double)ctx->par.period[2]));
     int nc = 0;
     CK(build_copies(ctx->stree.pos.p, ctx->sb2.p, ctx->srho.p, ctx->sidx.p, ns, ctx->L, blo, bhi,
-                    ctx->par.periodic != 0, ctx->C, ctx->ss, &nc, st));
+                    ctx->par.periodic != 0, ctx->C, ctx->ss, &nc, st, ctx->opt_curve & 2));
     CK(tree_shape(ctx->ctree, nc, true));
     CK(tree_refit(ctx->ctree, ctx->C.cpos.p, nullptr, ctx->C.d_n, st, true));
     ctx->nCopies = nc;
@@ -804,10 +804,10 @@ int skid_init_move(skid_ctx *ctx, float fDensMin, float fTempMax, float fMassMax
     if (int rc = ctx->read_int(ctx->M.d_nA, &nm)) return rc;
     ctx->nMove = nm;
     ctx->M.cap = nm > 0 ? nm : 1;   // prune passes and sorts run over this capacity
-    // Morton order of the movers' starting positions keeps warps coherent.
+    // Hilbert order of the movers' starting positions keeps warps coherent.
     if (nm > 0) {
         gather_by_index<<<grid_for(nm), 256, 0, st>>>(ctx->M.act2.p, ctx->pos4.p, nm, ctx->M.mold.p); skid::note_launch();
-        CK(morton_order(ctx->M.mold.p, nm, ctx->ss, st));
+        CK(curve_order(ctx->M.mold.p, nm, ctx->ss, st, ctx->opt_curve & 1));
         // key frame for the re-sorts at every prune: the periodic box, or the
         // movers' starting bounding box grown by half its size
         unsigned hb[6];
@@ -871,7 +871,7 @@ int skid_prune_inactive(skid_ctx *ctx, float fCvg, int *nActive)
     if (!ctx) return SKID_EINVAL;
     if (ctx->stage < STAGE_MOVE) return ctx->fail(SKID_ESTATE);
     ctx->timer_start();
-    CK(mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, ctx->st));
+    CK(mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, ctx->st, -1, ctx->opt_curve & 1));
     int na = 0;
     if (int rc = ctx->read_int(ctx->M.d_nA, &na)) return rc;
     ctx->tim.moving_ms += ctx->timer_stop();
@@ -908,7 +908,7 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
             for (int i = 0; i < PRUNE_STEPS; ++i)
                 if (int rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G, i == PRUNE_STEPS - 1))
                     return rc;
-            CK(mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st));
+            CK(mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st, -1, ctx->opt_curve & 1));
             ctx->iter_eager_done = true;
             ran = true;
         } else {
@@ -924,7 +924,8 @@ int skid_move_iterate(skid_ctx *ctx, float fStep, float fCvg, int bNoCut, int *n
             for (int i = 0; i < PRUNE_STEPS && !rc; ++i)
                 rc = ctx->enqueue_step(fStep, false, bNoCut != 0, i, G, i == PRUNE_STEPS - 1);
             const int bound = ctx->slot_bound(G);
-            if (!rc && mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st, bound))
+            if (!rc && mover_prune(ctx->M, ctx->L, ctx->mkey_lo, ctx->mkey_inv, fCvg, ctx->ss, st, bound,
+                                   ctx->opt_curve & 1))
                 rc = SKID_ECUDA;
             set_capturing(false);
             cudaError_t ce = cudaStreamEndCapture(st, &g);
@@ -1058,6 +1059,10 @@ int skid_set_option(skid_ctx *ctx, const char *name, double value)
     } else if (!strcmp(name, "unbind_cluster_min")) {
         if (v != -1 && v != 0 && v < 1024) return SKID_EINVAL;
         ctx->opt_unbind_clu_min = v;
+    } else if (!strcmp(name, "curve")) {
+        if (v < 0 || v > 7) return SKID_EINVAL;
+        ctx->opt_curve = v;
+        ctx->drop_graphs();   // the captured prunes and re-sorts carry the curve
     } else if (!strcmp(name, "field_unfused")) {
         ctx->opt_field_unfused = v != 0;
         ctx->drop_graphs();
@@ -1083,6 +1088,7 @@ int skid_get_option(skid_ctx *ctx, const char *name, double *value)
     else if (!strcmp(name, "unbind_block")) *value = ctx->U.used_bs;
     else if (!strcmp(name, "unbind_per_group")) *value = ctx->opt_unbind_per_group;
     else if (!strcmp(name, "unbind_cluster_min")) *value = ctx->opt_unbind_clu_min;
+    else if (!strcmp(name, "curve")) *value = ctx->opt_curve;
     else if (!strcmp(name, "unbind_cluster_size")) *value = ctx->U.used_cs;
     else if (!strcmp(name, "unbind_cluster_groups")) *value = ctx->U.used_nclu;
     else if (!strcmp(name, "unbind_tune_candidates")) *value = ctx->U.ntune;

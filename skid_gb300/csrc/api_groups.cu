@@ -93,7 +93,7 @@ int skid_fof(skid_ctx *ctx, float fTau, int *nGroup)
                ctx->parent, ctx->fof_minio, ctx->fof_flag, ctx->grp.p, ctx->d_scal + SC_NG,
                ctx->d_scal + SC_WORK, ctx->d_status, st));
     if (nm > 0) {
-        // keep movers in Morton order of their current positions (coherent
+        // keep movers in Hilbert order of their current positions (coherent
         // warps for the micro-steps)
         if (dalloc(ctx->moved4, ctx->n)) return ctx->fail(SKID_ENOMEM);
         reorder_movers<<<grid_for(nm), 256, 0, st>>>(ctx->mtree.perm.p, nm, ctx->M.mold.p,

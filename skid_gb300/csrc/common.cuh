@@ -112,12 +112,85 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v)
     return v;
 }
 
+// 3-D Hilbert index of B-bit integer coordinates (3B bits), after
+// J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707 (2004):
+// the axes are turned into the curve's transposed form (undo the excess
+// work level by level, then Gray-encode), whose bits are interleaved with x
+// highest at each level.  Consecutive indices are face-adjacent cells, so a
+// run of consecutive points stays compact (a Morton run jumps across the
+// box at every high-level boundary), and the index at B-1 bits of the
+// halved coordinates is this index's top 3(B-1) bits.
+template <int B>
+__device__ __forceinline__ uint64_t hilbert3(uint32_t x, uint32_t y, uint32_t z)
+{
+#pragma unroll
+    for (int b = B - 1; b > 0; --b) {
+        const uint32_t Q = 1u << b, P = Q - 1u;
+        x ^= (x & Q) ? P : 0u;
+        if (y & Q) {
+            x ^= P;
+        } else {
+            const uint32_t t = (x ^ y) & P;
+            x ^= t;
+            y ^= t;
+        }
+        if (z & Q) {
+            x ^= P;
+        } else {
+            const uint32_t t = (x ^ z) & P;
+            x ^= t;
+            z ^= t;
+        }
+    }
+    y ^= x;
+    z ^= y;
+    uint32_t t = 0;
+#pragma unroll
+    for (int b = B - 1; b > 0; --b) t ^= (z & (1u << b)) ? (1u << b) - 1u : 0u;
+    x ^= t;
+    y ^= t;
+    z ^= t;
+    return (spread3(x) << 2) | (spread3(y) << 1) | spread3(z);
+}
+
+// A point's cell on the 2^21 grid of the cubic frame (lo, inv).
+__device__ __forceinline__ uint3 grid21(float3 p, float3 lo, float3 inv)
+{
+    const float fx = fminf(fmaxf((p.x - lo.x) * inv.x, 0.0f), 2097151.0f);
+    const float fy = fminf(fmaxf((p.y - lo.y) * inv.y, 0.0f), 2097151.0f);
+    const float fz = fminf(fmaxf((p.z - lo.z) * inv.z, 0.0f), 2097151.0f);
+    return make_uint3((uint32_t)fx, (uint32_t)fy, (uint32_t)fz);
+}
+
+// The 63-bit Hilbert key of a point (21 levels).
+__device__ __forceinline__ uint64_t hilbert63(float3 p, float3 lo, float3 inv)
+{
+    const uint3 q = grid21(p, lo, inv);
+    return hilbert3<21>(q.x, q.y, q.z);
+}
+
+// The 63-bit Morton key of a point (bits of x, y, z interleaved).
 __device__ __forceinline__ uint64_t morton63(float3 p, float3 lo, float3 inv)
 {
-    float fx = fminf(fmaxf((p.x - lo.x) * inv.x, 0.0f), 2097151.0f);
-    float fy = fminf(fmaxf((p.y - lo.y) * inv.y, 0.0f), 2097151.0f);
-    float fz = fminf(fmaxf((p.z - lo.z) * inv.z, 0.0f), 2097151.0f);
-    return (spread3((uint64_t)fx) << 2) | (spread3((uint64_t)fy) << 1) | spread3((uint64_t)fz);
+    const uint3 q = grid21(p, lo, inv);
+    return (spread3(q.x) << 2) | (spread3(q.y) << 1) | spread3(q.z);
+}
+
+// The top 32 bits of hilbert63, from the 11 coarsest levels alone.
+__device__ __forceinline__ uint64_t hilbert_top32(float3 p, float3 lo, float3 inv)
+{
+    const uint3 q = grid21(p, lo, inv);
+    return hilbert3<11>(q.x >> 10, q.y >> 10, q.z >> 10) >> 1;
+}
+
+// Sort keys on either curve: 63 bits, or the top 32.
+__device__ __forceinline__ uint64_t curve63(float3 p, float3 lo, float3 inv, bool hil)
+{
+    return hil ? hilbert63(p, lo, inv) : morton63(p, lo, inv);
+}
+__device__ __forceinline__ uint64_t curve_top32(float3 p, float3 lo, float3 inv, bool hil)
+{
+    return hil ? hilbert_top32(p, lo, inv) : morton63(p, lo, inv) >> 31;
 }
 
 // Order-preserving float <-> uint for atomic min/max.

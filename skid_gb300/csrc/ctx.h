@@ -201,7 +201,7 @@ struct skid_ctx {
     int g_bound[NSLOT] = {};                 // active movers the graph's prune is sized for
     // What else a captured iteration bakes in: the buffers (allocation
     // epoch), the copy tree's shape, the mover and copy counts and the
-    // movers' Morton key frame.  A graph whose key still matches is replayed
+    // movers' Hilbert key frame.  A graph whose key still matches is replayed
     // in later runs instead of being captured again.
     struct GraphKey {
         unsigned long long epoch = 0;
@@ -231,7 +231,7 @@ struct skid_ctx {
         k.unfused = opt_field_unfused;
         return k;
     }
-    float3 mkey_lo{}, mkey_inv{};   // Morton frame of mover positions
+    float3 mkey_lo{}, mkey_inv{};   // Hilbert key frame of mover positions
     // move-field kernel timing: an event pair per step slot of an iteration
     cudaEvent_t fev[2 * skid::PRUNE_STEPS] = {};
     double *d_fbytes = nullptr;     // [bytes, launches] accumulated on device
@@ -298,6 +298,7 @@ struct skid_ctx {
     // movers, 16 down to ~400k, 8 down to ~50k, 4 down to ~25k, one below.
     int opt_G = 0, opt_g32_min = 600000, opt_g16_min = 400000, opt_g8_min = 100000, opt_g4_min = 30000;
     int opt_g64_min = 0;                          // 64 movers per warp at or above (0: never)
+    int opt_curve = 7;                            // Hilbert order (else Morton) of: 1 movers, 2 copies, 4 scatterer tree
     int opt_unbind_tw = -1, opt_unbind_bs = -1;   // -1: autotuned on the first skid_unbind
     int opt_unbind_clu_min = -1;                  // the largest groups above it may take a block cluster; 0 = never;
                                                   // -1 = 2048, and only where the tuner measured clusters faster

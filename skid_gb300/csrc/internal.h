@@ -112,9 +112,10 @@ int num_sms();
 // ---- tree.cu ----
 // Build a tree over n points (float4, w carried along).  perm maps sorted
 // slots to input indices.  `balls` reserves ball boxes, filled by a refit
-// that is given per-slot ball data.
+// that is given per-slot ball data.  Points are ordered by their Hilbert
+// key (hil) or Morton key; any order gives the same search results.
 cudaError_t tree_build(Tree &t, const float4 *pts, int n, bool balls, SortScratch &s,
-                       cudaStream_t st);
+                       cudaStream_t st, bool hil = true);
 // Recompute leaf and node boxes from pos (t.pos when null).  With aux, ball
 // data per slot (aux.x = ball2) also builds the ball boxes and max ball2;
 // with ballw the ball2 is pos.w instead.  d_n (device) overrides t.n; with
@@ -123,8 +124,8 @@ cudaError_t tree_refit(Tree &t, const float4 *pos, const float4 *aux, const int 
                        cudaStream_t st, bool ballw = false, int *d_dirty = nullptr);
 // Node arrays for n already-ordered points (no sort).
 cudaError_t tree_shape(Tree &t, int n, bool balls);
-// Morton order of n points: sorted permutation lands in s.v0.
-cudaError_t morton_order(const float4 *pts, int n, SortScratch &s, cudaStream_t st);
+// Hilbert (hil) or Morton order of n points: sorted permutation lands in s.v0.
+cudaError_t curve_order(const float4 *pts, int n, SortScratch &s, cudaStream_t st, bool hil = true);
 cudaError_t bbox_of(const float4 *pts, int n, unsigned *d_box6, cudaStream_t st);
 
 // ---- knn.cu ----
@@ -139,7 +140,7 @@ cudaError_t density_gather(const Tree &t, const float *ball2_sorted, float3 L, b
                            float *rho_sorted, int *d_work, cudaStream_t st);
 
 // Scatterer copies of the move phase (originals and periodic replicas), in
-// Morton order of the copy positions, compacted as ScatterCut removes them.
+// Hilbert order of the copy positions, compacted as ScatterCut removes them.
 //   cpos  = (x_c, y_c, z_c, fBall2)
 //   ccoef = (ih2, fNorm*m, rho, iOrder | 0x80000000 for the original)
 struct CopyState {
@@ -169,7 +170,7 @@ struct CopyState {
 };
 
 // Movers: positions by mover index; `act` lists the active ones, sorted by
-// the Morton key of their current positions after every prune.
+// the Hilbert key of their current positions after every prune.
 struct MoverState {
     int cap = 0;
     DBuf<float4> mpos, mold;
@@ -212,22 +213,24 @@ cudaError_t move_movers(const FieldArgs &a, const float *acc, float fStep, int m
 
 // ---- scatter.cu ----
 // Copies of the ns scatterers (sorted order) with their densities; sets
-// *nCopies and fills C (Morton-sorted).
+// *nCopies and fills C, sorted by Hilbert (hil) or Morton key.
 cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rho, const int *sidx,
                          int ns, float3 L, float3 boxlo, float3 boxhi, bool periodic,
-                         CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st);
+                         CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st,
+                         bool hil = true);
 // After a move pass: density floor, cut, stable compaction, counts.
 // compact = false defers the compaction: cut copies stay marked in their
 // slots (empty ball, density -inf) and only the live count is published.
 cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho, const int *d_nA,
                         double *d_fbytes, bool compact, cudaStream_t st);
-// Prune converged movers, then re-sort the active ones by Morton key.
-// Re-sort the active movers by the Morton key of their current positions.
+// Re-sort the active movers by the Hilbert (hil) or Morton key of their
+// current positions.
 cudaError_t mover_resort(MoverState &m, float3 keylo, float3 keyinv, SortScratch &ss,
-                         cudaStream_t st, int bound);
+                         cudaStream_t st, int bound, bool hil = true);
+// Prune converged movers, then re-sort the active ones by key as above.
 // bound: active movers at most (the sort and tiles are sized for it).
 cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,
-                        SortScratch &ss, cudaStream_t st, int bound = -1);
+                        SortScratch &ss, cudaStream_t st, int bound = -1, bool hil = true);
 
 inline int grid_for(int n, int threads = 256)
 {

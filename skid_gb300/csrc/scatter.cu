@@ -15,10 +15,10 @@
 //    mover; copies below it go.  On the first step (dark-only input or -fic)
 //    copies that reached no mover count as density 0.  A copy cut is marked
 //    dead in its slot (empty ball, density -inf); the survivors are compacted
-//    in slot order, which keeps them Morton-sorted, at the last step of each
+//    in slot order, which keeps them Hilbert-sorted, at the last step of each
 //    outer iteration (and after every single step), followed by a refit.
 //  - prune: kdPruneInactive (kd.c:735-793), stable, then the active movers
-//    are re-sorted by the Morton key of their current positions so that each
+//    are re-sorted by the Hilbert key of their current positions so that each
 //    warp's movers stay close together as the active set thins out.
 #include <cfloat>
 #include <cstring>
@@ -101,12 +101,12 @@ __global__ void copy_write_kernel(const float4 *__restrict__ spos, const float *
     }
 }
 
-__global__ void copy_keys_kernel(const float4 *__restrict__ cpos, int n, float3 lo, float3 inv,
+__global__ void copy_keys_kernel(const float4 *__restrict__ cpos, int n, float3 lo, float3 inv, int hil,
                                  uint64_t *keys, uint32_t *vals)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 q = cpos[i];
-        keys[i] = morton63(make_float3(q.x, q.y, q.z), lo, inv);
+        keys[i] = curve63(make_float3(q.x, q.y, q.z), lo, inv, hil != 0);
         vals[i] = (uint32_t)i;
     }
 }
@@ -332,7 +332,7 @@ prune_flag_kernel(const float4 *__restrict__ mpos, const float4 *__restrict__ mo
     if (threadIdx.x == 0) blk[blockIdx.x] = kept;
 }
 
-// Survivors get rOld reset (kd.c:785-789) and the Morton key of their
+// Survivors get rOld reset (kd.c:785-789) and the Hilbert key of their
 // current position at their compacted slot (tile b starts after the
 // survivors of the tiles before it; slots [0, survivors) are all written and
 // only those are sorted).  Block 0 publishes the survivor count in *d_nA2.
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(CT_THREADS)
 prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ blk, int nb,
                      const int *d_nA, int *d_nA2, const int *__restrict__ act,
                      const float4 *__restrict__ mpos, float4 *__restrict__ mold, float3 lo,
-                     float3 inv, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
+                     float3 inv, int hil, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
 {
     __shared__ int sh[32];
     const int n = *d_nA;
@@ -372,26 +372,26 @@ prune_scatter_kernel(const int *__restrict__ keep, const int *__restrict__ blk, 
             int m = act[i];
             float4 p = mpos[m];
             mold[m] = p;
-            // the top 32 bits of the Morton key (10 to 11 bits per axis) are
+            // the top 32 bits of the Hilbert key (10 to 11 levels) are
             // enough to give each warp a compact set of movers
-            keys[d] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
+            keys[d] = curve_top32(make_float3(p.x, p.y, p.z), lo, inv, hil != 0);
             vals[d] = (uint32_t)m;
         }
         o += __popc(msk[j]);
     }
 }
 
-// Keys (top 32 bits of the Morton key) of the active movers' current
-// positions, in active order.
+// Keys (top 32 bits of the Hilbert or Morton key) of the active movers'
+// current positions, in active order.
 __global__ void resort_keys_kernel(const int *__restrict__ act, const int *d_nA,
-                                   const float4 *__restrict__ mpos, float3 lo, float3 inv,
+                                   const float4 *__restrict__ mpos, float3 lo, float3 inv, int hil,
                                    uint64_t *__restrict__ keys, uint32_t *__restrict__ vals)
 {
     const int n = *d_nA;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int m = act[i];
         float4 p = mpos[m];
-        keys[i] = morton63(make_float3(p.x, p.y, p.z), lo, inv) >> 31;
+        keys[i] = curve_top32(make_float3(p.x, p.y, p.z), lo, inv, hil != 0);
         vals[i] = (uint32_t)m;
     }
 }
@@ -419,7 +419,7 @@ float ord_to_float(unsigned u)
 
 cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rho, const int *sidx,
                          int ns, float3 L, float3 boxlo, float3 boxhi, bool periodic,
-                         CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st)
+                         CopyState &C, SortScratch &ss, int *nCopies, cudaStream_t st, bool hil)
 {
     cudaError_t e;
     if ((e = dalloc(C.mask, ns)) || (e = dalloc(C.cnt, ns)) || (e = dalloc(C.off, ns)))
@@ -431,7 +431,7 @@ cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rh
     if ((e = cudaStreamSynchronize(st))) return e;
     if ((e = C.alloc(nc))) return e;
     copy_write_kernel<<<grid_for(ns), 256, 0, st>>>(spos, ball2, rho, sidx, C.mask.p, C.off.p, ns, L, C.cpos2.p, C.ccoef2.p); skid::note_launch();
-    // Morton order of the copy positions (replicas lie just outside the box)
+    // Hilbert order of the copy positions (replicas lie just outside the box)
     if ((e = dalloc(ss.k0, nc)) || (e = dalloc(ss.k1, nc)) || (e = dalloc(ss.v0, nc)) ||
         (e = dalloc(ss.v1, nc)) || (e = dalloc(ss.box, 8)))
         return e;
@@ -443,7 +443,7 @@ cudaError_t build_copies(const float4 *spos, const float *ball2, const float *rh
     float3 hi = make_float3(ord_to_float(hb[3]), ord_to_float(hb[4]), ord_to_float(hb[5]));
     float ext = fmaxf(fmaxf(hi.x - lo.x, hi.y - lo.y), fmaxf(hi.z - lo.z, 1e-30f));
     float s = 2097151.0f / ext;
-    copy_keys_kernel<<<grid_for(nc), 256, 0, st>>>(C.cpos2.p, nc, lo, make_float3(s, s, s), ss.k0.p, ss.v0.p); skid::note_launch();
+    copy_keys_kernel<<<grid_for(nc), 256, 0, st>>>(C.cpos2.p, nc, lo, make_float3(s, s, s), hil ? 1 : 0, ss.k0.p, ss.v0.p); skid::note_launch();
     if ((e = radix_sort(ss, nc, 63, st))) return e;
     copy_permute_kernel<<<grid_for(nc), 256, 0, st>>>(ss.v0.p, nc, C.cpos2.p, C.ccoef2.p, C.cpos.p, C.ccoef.p); skid::note_launch();
     if ((e = cudaMemsetAsync(C.touched.p, 0, C.cap, st))) return e;
@@ -478,13 +478,13 @@ cudaError_t scatter_cut(CopyState &C, bool initial, bool nocut, float *final_rho
     return cudaGetLastError();
 }
 
-// Global re-sort of the active movers between prunes by the Morton key of
+// Global re-sort of the active movers between prunes by the Hilbert key of
 // their current positions (the same 32-bit key as the prune's; equal keys keep
-// their order).  A mover that crosses a high-level Morton boundary has to move
+// their order).  A mover that crosses a high-level curve boundary has to move
 // far in the order, which only a global sort does: a tile-local sort, or a
 // coarser key, loses most of the gain.
 cudaError_t mover_resort(MoverState &m, float3 keylo, float3 keyinv, SortScratch &ss,
-                         cudaStream_t st, int bound)
+                         cudaStream_t st, int bound, bool hil)
 {
     cudaError_t e;
     int cap = bound > 0 && bound < m.cap ? bound : m.cap;
@@ -495,14 +495,14 @@ cudaError_t mover_resort(MoverState &m, float3 keylo, float3 keyinv, SortScratch
         (e = dalloc(ss.v1, cap)))
         return e;
     resort_keys_kernel<<<grid_for(cap), 256, 0, st>>>(m.act.p, m.d_nA, m.mpos.p, keylo, keyinv,
-                                                      ss.k0.p, ss.v0.p); skid::note_launch();
+                                                      hil ? 1 : 0, ss.k0.p, ss.v0.p); skid::note_launch();
     if ((e = radix_sort(ss, cap, 32, st, m.d_nA))) return e;
     act_from_sorted<<<grid_for(cap), 256, 0, st>>>(ss.v0.p, m.d_nA, m.act.p, m.d_nA); skid::note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyinv, float fCvg,
-                        SortScratch &ss, cudaStream_t st, int bound)
+                        SortScratch &ss, cudaStream_t st, int bound, bool hil)
 {
     cudaError_t e;
     int cap = bound > 0 && bound < m.cap ? bound : m.cap;
@@ -519,8 +519,8 @@ cudaError_t mover_prune(MoverState &m, float3 period, float3 keylo, float3 keyin
     prune_flag_kernel<<<nb, CT_THREADS, 0, st>>>(m.mpos.p, m.mold.p, m.act.p, m.d_nA, hP, fCvg2,
                                                  m.keep.p, m.blk.p); skid::note_launch();
     prune_scatter_kernel<<<nb, CT_THREADS, 0, st>>>(m.keep.p, m.blk.p, nb, m.d_nA, m.d_nA2, m.act.p,
-                                                    m.mpos.p, m.mold.p, keylo, keyinv, ss.k0.p,
-                                                    ss.v0.p); skid::note_launch();
+                                                    m.mpos.p, m.mold.p, keylo, keyinv, hil ? 1 : 0,
+                                                    ss.k0.p, ss.v0.p); skid::note_launch();
     // an even number of digit passes leaves the result in (k0, v0), so a
     // captured graph replays consistently; only the surviving movers' keys
     // (the first *d_nA2 slots) are sorted

@@ -1,4 +1,4 @@
-// Device tree build: Morton-sorted points bucketed into leaves of one warp
+// Device tree build: Hilbert- (or Morton-) sorted points bucketed into leaves of one warp
 // (32 points) under an implicit complete binary tree (heap numbering of
 // kd.h:6-15).  Replaces the reference's median-split kd build
 // (kdBuildTree/kdBuildMoveTree, kd.c:225-552): any tree gives the same search
@@ -40,8 +40,8 @@ __global__ void bbox_kernel(const float4 *__restrict__ p, int n, unsigned *box)
     }
 }
 
-__global__ void morton_kernel(const float4 *__restrict__ p, int n, const unsigned *box,
-                              uint64_t *keys, uint32_t *vals)
+__global__ void curve_kernel(const float4 *__restrict__ p, int n, const unsigned *box, int hil,
+                             uint64_t *keys, uint32_t *vals)
 {
     float3 lo = make_float3(ord2f(box[0]), ord2f(box[1]), ord2f(box[2]));
     float3 hi = make_float3(ord2f(box[3]), ord2f(box[4]), ord2f(box[5]));
@@ -50,7 +50,7 @@ __global__ void morton_kernel(const float4 *__restrict__ p, int n, const unsigne
     float3 inv = make_float3(s, s, s);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 q = p[i];
-        keys[i] = morton63(make_float3(q.x, q.y, q.z), lo, inv);
+        keys[i] = curve63(make_float3(q.x, q.y, q.z), lo, inv, hil != 0);
         vals[i] = (uint32_t)i;
     }
 }
@@ -166,7 +166,7 @@ static int leaf_base_for(int n)
 }
 
 cudaError_t tree_build(Tree &t, const float4 *pts, int n, bool balls, SortScratch &s,
-                       cudaStream_t st)
+                       cudaStream_t st, bool hil)
 {
     cudaError_t e;
     t.n = n;
@@ -182,13 +182,13 @@ cudaError_t tree_build(Tree &t, const float4 *pts, int n, bool balls, SortScratc
     }
     if (n > 0) {
         int blocks = min((n + 255) / 256, num_sms() * 8);
-        if ((e = morton_order(pts, n, s, st))) return e;
+        if ((e = curve_order(pts, n, s, st, hil))) return e;
         gather_sorted<<<blocks, 256, 0, st>>>(pts, s.v0.p, n, t.pos.p, t.perm.p); skid::note_launch();
     }
     return tree_refit(t, nullptr, nullptr, nullptr, st);
 }
 
-cudaError_t morton_order(const float4 *pts, int n, SortScratch &s, cudaStream_t st)
+cudaError_t curve_order(const float4 *pts, int n, SortScratch &s, cudaStream_t st, bool hil)
 {
     cudaError_t e;
     if (n <= 0) return cudaSuccess;
@@ -198,7 +198,7 @@ cudaError_t morton_order(const float4 *pts, int n, SortScratch &s, cudaStream_t 
     unsigned *dbox = s.box.p;
     if ((e = bbox_of(pts, n, dbox, st))) return e;
     int blocks = min((n + 255) / 256, num_sms() * 8);
-    morton_kernel<<<blocks, 256, 0, st>>>(pts, n, dbox, s.k0.p, s.v0.p); skid::note_launch();
+    curve_kernel<<<blocks, 256, 0, st>>>(pts, n, dbox, hil ? 1 : 0, s.k0.p, s.v0.p); skid::note_launch();
     return radix_sort(s, n, 63, st);
 }
 

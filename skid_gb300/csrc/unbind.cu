@@ -728,11 +728,26 @@ __device__ void warp_group(const RemoveArgs &A, int g)
             keep_bot2(mn, mn2, E, i);
             if (exact) dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
         }
+        float hi = 0.0f, lo = 0.0f;
+        const ArgRed t1 = mx, b1 = mn;
+        // members again, in the same order with the same FP32 energies: the
+        // candidates on the asked sides exactly (FP64, as the reference)
+        auto rescan = [&](bool scan_hi, bool scan_lo) {
+            for (int i = lane; i < n; i += 32) {
+                float4 r = qr[i], v = qv[i];
+                long long p = pot[i];
+                float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
+                const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
+                if (ch || cl) {
+                    float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
+                    if (ch && X > mx.v) { mx.v = X; mx.i = i; }
+                    if (cl && X < mn.v) { mn.v = X; mn.i = i; }
+                }
+            }
+        };
         if (exact) {
             // only members whose FP32 energy is within twice the error bound
-            // of the extremes can be the exact arg-max / arg-min: evaluate
-            // those exactly (FP64, as the reference does) -- usually just the
-            // lane's own extreme, else its members again
+            // of the extremes can be the exact arg-max / arg-min
             float emax = mx.v, emin = mn.v;
 #pragma unroll
             for (int o = 16; o; o >>= 1) {
@@ -740,38 +755,49 @@ __device__ void warp_group(const RemoveArgs &A, int g)
                 emin = fminf(emin, __shfl_xor_sync(SKID_FULL, emin, o));
                 dmax = fmaxf(dmax, __shfl_xor_sync(SKID_FULL, dmax, o));
             }
-            const float hi = emax - 2.0f * dmax, lo = emin + 2.0f * dmax;
-            const ArgRed t1 = mx, b1 = mn;
-            mx = ArgRed{-FLT_MAX, 0x7fffffff};
-            mn = ArgRed{FLT_MAX, 0x7fffffff};
-            if (t1.i < n && t1.v >= hi && mx2.v < hi) {
-                mx.v = member_energy(true, A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, scm, inv_d, opz_d);
-                mx.i = t1.i;
-            }
-            if (b1.i < n && b1.v <= lo && mn2.v > lo) {
-                mn.v = member_energy(true, A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, scm, inv_d, opz_d);
-                mn.i = b1.i;
-            }
-            const bool scan_hi = mx2.v >= hi, scan_lo = mn2.v <= lo;
-            if (scan_hi || scan_lo) {
-                for (int i = lane; i < n; i += 32) {
-                    float4 r = qr[i], v = qv[i];
-                    long long p = pot[i];
-                    float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-                    const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
-                    if (ch || cl) {
-                        float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
-                        if (ch && X > mx.v) { mx.v = X; mx.i = i; }
-                        if (cl && X < mn.v) { mn.v = X; mn.i = i; }
-                    }
+            hi = emax - 2.0f * dmax;
+            lo = emin + 2.0f * dmax;
+            // One candidate alone is the exact arg-max (every other member's
+            // exact energy is below emax - dmax, and its own at least that),
+            // and the sign of its exact energy is known when its FP32 energy
+            // is at least the bound, or below minus the bound: the usual pass
+            // needs no FP64 energy.  Otherwise the candidates are evaluated
+            // exactly -- usually just the lane's own extreme, else its
+            // members again.
+            const unsigned chi = __ballot_sync(SKID_FULL, t1.v >= hi);
+            const bool one = chi != 0 && (chi & (chi - 1)) == 0 && !__any_sync(SKID_FULL, mx2.v >= hi);
+            if (one && emax >= dmax) {
+                mx.v = emax;
+                mx.i = __shfl_sync(SKID_FULL, t1.i, __ffs(chi) - 1);
+            } else if (one && emax < -dmax) {
+                mx.v = emax;
+            } else {
+                mx = ArgRed{-FLT_MAX, 0x7fffffff};
+                if (t1.i < n && t1.v >= hi && mx2.v < hi) {
+                    mx.v = member_energy(true, A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, scm, inv_d, opz_d);
+                    mx.i = t1.i;
                 }
+                if (mx2.v >= hi) rescan(true, false);
+                mx = warp_argmax(mx);
             }
+        } else {
+            mx = warp_argmax(mx);
         }
-        mx = warp_argmax(mx);
-        mn = warp_argmin(mn);
-        // kd.c:1389-1409: fTotBig starts at -1, fTotMin at 1
-        imin = mn.v < 1.0f ? mn.i : 0;
-        if (!(mx.v >= 0.0f) || A.nounbind || n == 0) break;
+        if (!(mx.v >= 0.0f) || A.nounbind || n == 0) {
+            // the group's most bound member (kd.c:1389-1409: fTotMin starts
+            // at 1), needed only once the removals stop
+            if (exact) {
+                mn = ArgRed{FLT_MAX, 0x7fffffff};
+                if (b1.i < n && b1.v <= lo && mn2.v > lo) {
+                    mn.v = member_energy(true, A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, scm, inv_d, opz_d);
+                    mn.i = b1.i;
+                }
+                if (mn2.v <= lo) rescan(false, true);
+            }
+            mn = warp_argmin(mn);
+            imin = mn.v < 1.0f ? mn.i : 0;
+            break;
+        }
         const int ib = mx.i;
         __syncwarp();
         float4 r = qr[ib], v = qv[ib];
@@ -821,6 +847,8 @@ struct BlockShared {
     float s_mg;                 // max over members and axes of |a v_j| + |aH r_j|
     float gpart[8][4];          // a cluster's blocks' partials, gathered (rank order)
     ArgRed gmx[8], gmn[8];
+    int ccnt[BS / 32];          // per-warp arg-max candidate counts (two for a thread with two)
+    int cidx[BS / 32];          // the warp's first candidate
 };
 
 // max_j |a c_j| + |aH c_{j-3}| of a centre (rcm, vcm)
@@ -831,6 +859,19 @@ __device__ __forceinline__ float centre_mag(const RemoveArgs &A, const double *d
     for (int d = 0; d < 3; ++d)
         m = fmaxf(m, fabsf(A.fShift * (float)dcm[3 + d]) + fabsf(A.fCosmo * (float)dcm[d]));
     return m * 1.0000002f;
+}
+
+// FP32 filter energy of a large group's member from its staged
+// w = a v + aH r: E = 1/2 |w - W|^2 - pot (1+z) 2^-S (dd and pe returned for
+// the pass's error bound), each operation rounded as written, so every
+// evaluation of a member gives the same value.
+__device__ __forceinline__ float staged_energy(float4 w, long long p, float wx, float wy, float wz,
+                                              float epot, float &dd, float &pe)
+{
+    const float dx = __fsub_rn(w.x, wx), dy = __fsub_rn(w.y, wy), dz = __fsub_rn(w.z, wz);
+    dd = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    pe = __fmul_rn(ll2f_fast(p), epot);
+    return __fsub_rn(__fmul_rn(0.5f, dd), pe);
 }
 
 // A large group, the whole block.
@@ -874,6 +915,7 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         S.s_n = n0;
         S.s_have = 0;
         S.s_go = 1;
+        S.s_imin = 0;
         for (int d = 0; d < 3; ++d)
             S.s_w[d] = (float)((double)A.fShift * S.d_cm[3 + d] + (double)A.fCosmo * S.d_cm[d]);
     }
@@ -916,10 +958,15 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         double dcm[6];
         float scm[6];
         for (int d = 0; d < 6; ++d) { dcm[d] = S.d_cm[d]; scm[d] = S.s_cm[d]; }
+        const float wx = S.s_w[0], wy = S.s_w[1], wz = S.s_w[2];
+        // the thread's two largest and two smallest FP32 energies (first
+        // index first on ties), the block's extremes, and the pass's bound
+        // on |FP32 energy - reference energy| (bnd)
         ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
-        ArgRed ex2 = mx, en2 = mn;     // the thread's second largest / smallest (exact path)
-        float dmax = 0.0f;
+        ArgRed x2 = mx, n2 = mn;
+        float gmax = -FLT_MAX, gmin = FLT_MAX, bnd = 0.0f;
         if (exact) {
+            float dmax = 0.0f;
             for (int i = tid; i < n; i += BS) {
                 float4 r = qr[i], v = qv[i];
                 long long p = pot[i];
@@ -928,26 +975,42 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                     pot[i] = p;
                 }
                 float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-                keep_top2(mx, ex2, E, i);
-                keep_bot2(mn, en2, E, i);
+                keep_top2(mx, x2, E, i);
+                keep_bot2(mn, n2, E, i);
                 dmax = fmaxf(dmax, energy_err(A, r, v, p, scm, E));
             }
+            float a0 = mx.v, a1 = mn.v;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                a0 = fmaxf(a0, __shfl_xor_sync(SKID_FULL, a0, o));
+                a1 = fminf(a1, __shfl_xor_sync(SKID_FULL, a1, o));
+                dmax = fmaxf(dmax, __shfl_xor_sync(SKID_FULL, dmax, o));
+            }
+            if (lane == 0) {
+                S.ext[w][0] = a0;
+                S.ext[w][1] = a1;
+                S.ext[w][2] = dmax;
+            }
+            __syncthreads();
+            for (int k = 0; k < BS / 32; ++k) {
+                gmax = fmaxf(gmax, S.ext[k][0]);
+                gmin = fminf(gmin, S.ext[k][1]);
+                bnd = fmaxf(bnd, S.ext[k][2]);
+            }
         } else {
-            const float wx = S.s_w[0], wy = S.s_w[1], wz = S.s_w[2];
             const float gms = fmul(A.G, rs.w) * A.scale;   // the removed member's G m 2^S
             const bool sub = have && A.subpot;
             float ddmx = 0.0f, pemx = 0.0f;
-            ArgRed mx2{-FLT_MAX, 0x7fffffff}, mn2{FLT_MAX, 0x7fffffff};
             // RB members per thread per batch, all loaded before any is used,
             // so their memory latencies overlap
             constexpr int RB = BS >= 1024 ? 2 : 4;
             for (int i0 = tid; i0 < n; i0 += RB * BS) {
-                float4 r[RB], w[RB];
+                float4 r[RB], wv[RB];
                 long long p[RB];
 #pragma unroll
                 for (int k = 0; k < RB; ++k) {
                     const int i = i0 + k * BS;
-                    if (i < n) { r[k] = qr[i]; w[k] = qw[i]; p[k] = pot[i]; }
+                    if (i < n) { r[k] = qr[i]; wv[k] = qw[i]; p[k] = pot[i]; }
                 }
 #pragma unroll
                 for (int k = 0; k < RB; ++k) {
@@ -956,30 +1019,24 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                     if (sub) {
                         // kdSubPot (grav.c:44-59): the term the potentials added
                         float d2 = d2of(fsub(rs.x, r[k].x), fsub(rs.y, r[k].y), fsub(rs.z, r[k].z));
-                        p[k] -= fx(fmul(gms, pair_dir(d2, fadd(es, w[k].w), A.plummer)), 1.0f);
+                        p[k] -= fx(fmul(gms, pair_dir(d2, fadd(es, wv[k].w), A.plummer)), 1.0f);
                         pot[i] = p[k];
                     }
-                    const float dx = w[k].x - wx, dy = w[k].y - wy, dz = w[k].z - wz;
-                    const float dd = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
-                    const float pe = ll2f_fast(p[k]) * epot;
-                    const float E = 0.5f * dd - pe;
-                    // the thread's two largest and two smallest, first index first
-                    if (E > mx.v) { mx2 = mx; mx.v = E; mx.i = i; }
-                    else if (E > mx2.v) { mx2.v = E; mx2.i = i; }
-                    if (E < mn.v) { mn2 = mn; mn.v = E; mn.i = i; }
-                    else if (E < mn2.v) { mn2.v = E; mn2.i = i; }
+                    float dd, pe;
+                    const float E = staged_energy(wv[k], p[k], wx, wy, wz, epot, dd, pe);
+                    keep_top2(mx, x2, E, i);
+                    keep_bot2(mn, n2, E, i);
                     ddmx = fmaxf(ddmx, dd);
                     pemx = fmaxf(pemx, fabsf(pe));
                 }
             }
-            // Filtered exact decisions, as for the smaller groups.  Bound on
-            // |E_i(FP32) - E_i(reference)|: with C = max |a v| + |aH r| over
-            // members plus the same for the centre, each component of
-            // w_i - W is within 2^-21 C of the reference's dv, so
-            // 2^-19 (C (sqrt(3 dd) + 3 C) + 1.5 dd + 2 |pe|) over the pass's
-            // largest dd and |pe| covers every member, several times over.
-            float tmax = mx.v, tmin = mn.v;
-            float a0 = tmax, a1 = tmin;
+            // Bound on |E_i(FP32) - E_i(reference)|: with C = max |a v| +
+            // |aH r| over members plus the same for the centre, each
+            // component of w_i - W is within 2^-21 C of the reference's dv,
+            // so 2^-19 (C (sqrt(3 dd) + 3 C) + 1.5 dd + 2 |pe|) over the
+            // pass's largest dd and |pe| covers every member, several times
+            // over.
+            float a0 = mx.v, a1 = mn.v;
 #pragma unroll
             for (int o = 16; o; o >>= 1) {
                 a0 = fmaxf(a0, __shfl_xor_sync(SKID_FULL, a0, o));
@@ -994,7 +1051,7 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 S.ext[w][3] = pemx;
             }
             __syncthreads();
-            float gmax = -FLT_MAX, gmin = FLT_MAX, gdd = 0.0f, gpe = 0.0f;
+            float gdd = 0.0f, gpe = 0.0f;
             for (int k = 0; k < BS / 32; ++k) {
                 gmax = fmaxf(gmax, S.ext[k][0]);
                 gmin = fminf(gmin, S.ext[k][1]);
@@ -1002,149 +1059,158 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 gpe = fmaxf(gpe, S.ext[k][3]);
             }
             const float C = S.s_mg + S.s_mW;
-            const float bound =
-                1.9073486e-06f * (C * (1.7320509f * sqrtf(gdd) + 3.0f * C) + 1.5f * gdd + 2.0f * gpe) +
-                1e-30f;
-            const float hi = gmax - 2.0f * bound, lo = gmin + 2.0f * bound;
-            const ArgRed t1 = mx, b1 = mn;
-            mx = ArgRed{-FLT_MAX, 0x7fffffff};
-            mn = ArgRed{FLT_MAX, 0x7fffffff};
-            if ((tmax >= hi && mx2.v < hi) || (tmin <= lo && mn2.v > lo)) {
-                // usually only the thread's own extreme is a candidate: that
-                // one member exactly (when both its first and second are
-                // candidates on a side, the rescan below takes that side)
-                if (t1.i < n && tmax >= hi && mx2.v < hi) {
-                    mx.v = exact_energy(A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, inv_d, opz_d);
-                    mx.i = t1.i;
+            bnd = 1.9073486e-06f * (C * (1.7320509f * sqrtf(gdd) + 3.0f * C) + 1.5f * gdd + 2.0f * gpe) +
+                  1e-30f;
+        }
+        // Only members within twice the bound of the extremes can be the
+        // exact arg-max or arg-min.
+        const float hi = gmax - 2.0f * bnd, lo = gmin + 2.0f * bnd;
+        const ArgRed t1 = mx, b1 = mn;
+        // members again, in the same order with the same FP32 energies: the
+        // candidates on the asked side exactly (FP64, as the reference)
+        auto rescan = [&](bool scan_hi, bool scan_lo) {
+            for (int i = tid; i < n; i += BS) {
+                float E;
+                if (exact) {
+                    E = member_energy(false, A, qr[i], qv[i], pot[i], dcm, scm, inv_d, opz_d);
+                } else {
+                    float dd, pe;
+                    E = staged_energy(qw[i], pot[i], wx, wy, wz, epot, dd, pe);
                 }
-                if (b1.i < n && tmin <= lo && mn2.v > lo) {
-                    mn.v = exact_energy(A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, inv_d, opz_d);
-                    mn.i = b1.i;
+                const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
+                if (ch || cl) {
+                    const float X = exact_energy(A, qr[i], qv[i], pot[i], dcm, inv_d, opz_d);
+                    if (ch && X > mx.v) { mx.v = X; mx.i = i; }
+                    if (cl && X < mn.v) { mn.v = X; mn.i = i; }
                 }
             }
-            const bool scan_hi = tmax >= hi && mx2.v >= hi, scan_lo = tmin <= lo && mn2.v <= lo;
-            if (scan_hi || scan_lo) {
-                // this thread holds several candidates on a side: its members
-                // again, in the same order, with the same FP32 energies, the
-                // candidates exactly
-                for (int i = tid; i < n; i += BS) {
-                    const float4 wi = qw[i];
-                    const long long pi = pot[i];
-                    const float dx = wi.x - wx, dy = wi.y - wy, dz = wi.z - wz;
-                    const float E =
-                        0.5f * __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)) - ll2f_fast(pi) * epot;
-                    const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
-                    if (ch || cl) {
-                        const float X = exact_energy(A, qr[i], qv[i], pi, dcm, inv_d, opz_d);
-                        if (ch && X > mx.v) { mx.v = X; mx.i = i; }
-                        if (cl && X < mn.v) { mn.v = X; mn.i = i; }
-                    }
-                }
+        };
+        // The arg-max.  One candidate alone is the exact arg-max (every other
+        // member's exact energy is below gmax - bnd, its own at least that),
+        // and the sign of its exact energy is known when gmax >= bnd or
+        // gmax < -bnd: the usual pass evaluates no FP64 energy.  The warps'
+        // candidate counts ride on the barrier the block needs anyway (a
+        // thread with two candidates counts as two).
+        {
+            const unsigned bal = __ballot_sync(SKID_FULL, t1.v >= hi);
+            const int first = __shfl_sync(SKID_FULL, t1.i, bal ? __ffs(bal) - 1 : 0);
+            const bool two = __any_sync(SKID_FULL, x2.v >= hi);
+            if (lane == 0) {
+                S.ccnt[w] = __popc(bal) + (two ? 2 : 0);
+                S.cidx[w] = first;
             }
         }
-        if (exact) {
-            // filtered exact evaluation, as in warp_group
-            float emax = mx.v, emin = mn.v;
-#pragma unroll
-            for (int o = 16; o; o >>= 1) {
-                emax = fmaxf(emax, __shfl_xor_sync(SKID_FULL, emax, o));
-                emin = fminf(emin, __shfl_xor_sync(SKID_FULL, emin, o));
-                dmax = fmaxf(dmax, __shfl_xor_sync(SKID_FULL, dmax, o));
-            }
-            if (lane == 0) {
-                S.ext[w][0] = emax;
-                S.ext[w][1] = emin;
-                S.ext[w][2] = dmax;
-            }
-            __syncthreads();
-            emax = -FLT_MAX; emin = FLT_MAX; dmax = 0.0f;
-            for (int k = 0; k < BS / 32; ++k) {
-                emax = fmaxf(emax, S.ext[k][0]);
-                emin = fminf(emin, S.ext[k][1]);
-                dmax = fmaxf(dmax, S.ext[k][2]);
-            }
-            const float hi = emax - 2.0f * dmax, lo = emin + 2.0f * dmax;
-            const ArgRed t1 = mx, b1 = mn;
+        __syncthreads();
+        int ccnt = 0, cidx = 0;
+        for (int k = 0; k < BS / 32; ++k) {
+            const int c = S.ccnt[k];
+            if (c && !ccnt) cidx = S.cidx[k];
+            ccnt += c;
+        }
+        bool go;
+        int ib = cidx;
+        if (ccnt == 1 && gmax >= bnd) {
+            go = true;
+        } else if (ccnt == 1 && gmax < -bnd) {
+            go = false;
+        } else {
             mx = ArgRed{-FLT_MAX, 0x7fffffff};
-            mn = ArgRed{FLT_MAX, 0x7fffffff};
-            if (t1.i < n && t1.v >= hi && ex2.v < hi) {
-                mx.v = member_energy(true, A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, scm, inv_d, opz_d);
+            if (t1.i < n && t1.v >= hi && x2.v < hi) {
+                mx.v = exact_energy(A, qr[t1.i], qv[t1.i], pot[t1.i], dcm, inv_d, opz_d);
                 mx.i = t1.i;
             }
-            if (b1.i < n && b1.v <= lo && en2.v > lo) {
-                mn.v = member_energy(true, A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, scm, inv_d, opz_d);
+            if (x2.v >= hi) rescan(true, false);
+            mx = warp_argmax(mx);
+            if (lane == 0) S.smax[w] = mx;
+            __syncthreads();
+            ArgRed a = S.smax[0];
+            for (int k = 1; k < BS / 32; ++k) {
+                const ArgRed x = S.smax[k];
+                if (x.v > a.v || (x.v == a.v && x.i < a.i)) a = x;
+            }
+            go = a.v >= 0.0f;   // kd.c:1389-1409: fTotBig starts at -1
+            ib = a.i;
+        }
+        if (A.nounbind || n == 0) go = false;
+        if (!go) {
+            // the group's most bound member (fTotMin starts at 1), needed
+            // only once the removals stop
+            mn = ArgRed{FLT_MAX, 0x7fffffff};
+            if (b1.i < n && b1.v <= lo && n2.v > lo) {
+                mn.v = exact_energy(A, qr[b1.i], qv[b1.i], pot[b1.i], dcm, inv_d, opz_d);
                 mn.i = b1.i;
             }
-            const bool scan_hi = ex2.v >= hi, scan_lo = en2.v <= lo;
-            if (scan_hi || scan_lo) {
-                for (int i = tid; i < n; i += BS) {
-                    float4 r = qr[i], v = qv[i];
-                    long long p = pot[i];
-                    float E = member_energy(false, A, r, v, p, dcm, scm, inv_d, opz_d);
-                    const bool ch = scan_hi && E >= hi, cl = scan_lo && E <= lo;
-                    if (ch || cl) {
-                        float X = member_energy(true, A, r, v, p, dcm, scm, inv_d, opz_d);
-                        if (ch && X > mx.v) { mx.v = X; mx.i = i; }
-                        if (cl && X < mn.v) { mn.v = X; mn.i = i; }
-                    }
+            if (n2.v <= lo) rescan(false, true);
+            mn = warp_argmin(mn);
+            if (lane == 0) S.smin[w] = mn;
+            __syncthreads();
+            if (tid == 0) {
+                ArgRed b = S.smin[0];
+                for (int k = 1; k < BS / 32; ++k) {
+                    const ArgRed y = S.smin[k];
+                    if (y.v < b.v || (y.v == b.v && y.i < b.i)) b = y;
                 }
+                S.s_imin = b.v < 1.0f ? b.i : 0;
             }
+            break;
         }
-        mx = warp_argmax(mx);
-        mn = warp_argmin(mn);
-        if (lane == 0) { S.smax[w] = mx; S.smin[w] = mn; }
-        __syncthreads();
+        // Remove member ib, swapping the last member into its slot
+        // (kd.c:1424-1440).  Warp 0 updates the FP64 centre while warp 1
+        // moves the records; the two-warp barrier orders warp 0's reads of
+        // slot ib before warp 1's writes to it.
+        const int nn = n - 1;
+        float4 r_ib = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v_ib = r_ib;
+        int id_ib = 0;
+        float4 rl = r_ib, vl = r_ib, wl = r_ib, wb = r_ib, rb = r_ib, vb = r_ib;
+        int il = 0, ir = 0;
+        long long pl = 0, pb = 0;
         if (tid == 0) {
-            ArgRed a = S.smax[0], b = S.smin[0];
-            for (int k = 1; k < BS / 32; ++k) {
-                ArgRed x = S.smax[k], y = S.smin[k];
-                if (x.v > a.v || (x.v == a.v && x.i < a.i)) a = x;
-                if (y.v < b.v || (y.v == b.v && y.i < b.i)) b = y;
-            }
-            S.s_imin = b.v < 1.0f ? b.i : 0;
-            if (!(a.v >= 0.0f) || A.nounbind || n == 0) {
-                S.s_go = 0;
+            r_ib = qr[ib];
+            v_ib = qv[ib];
+            id_ib = qid[ib];
+        } else if (tid == 32 && nn > 0) {
+            rl = qr[nn]; vl = qv[nn]; il = qid[nn]; pl = pot[nn];
+            rb = qr[ib]; vb = qv[ib]; ir = qid[ib]; pb = pot[ib];
+            if (!exact) { wl = qw[nn]; wb = qw[ib]; }
+        }
+        if (w < 2) {
+            __syncwarp();
+            asm volatile("barrier.sync 1, 64;" ::: "memory");
+        }
+        if (tid == 0) {
+            A.grp[id_ib] = 0;
+            ++nrem;
+            if (nn == 0) {
+                S.d_mass = 0.0;
+                for (int d = 3; d < 6; ++d) S.d_cm[d] = 0.0;
             } else {
-                int ib = a.i;
-                float4 r = qr[ib], v = qv[ib];
-                A.grp[qid[ib]] = 0;
-                ++nrem;
-                int nn = n - 1;
-                if (nn == 0) {
-                    S.d_mass = 0.0;
-                    for (int d = 3; d < 6; ++d) S.d_cm[d] = 0.0;
-                    S.s_go = 0;
-                } else {
-                    double mm = S.d_mass;
-                    for (int d = 0; d < 6; ++d) dcm[d] = S.d_cm[d];
-                    rcm_update(mm, dcm, r, v);
-                    S.d_mass = mm;
-                    for (int d = 0; d < 6; ++d) {
-                        S.d_cm[d] = dcm[d];
-                        S.s_cm[d] = (float)dcm[d];
-                    }
+                double mm = S.d_mass;
+                rcm_update(mm, dcm, r_ib, v_ib);
+                S.d_mass = mm;
+                for (int d = 0; d < 6; ++d) {
+                    S.d_cm[d] = dcm[d];
+                    S.s_cm[d] = (float)dcm[d];
+                }
+                if (!exact) {
                     for (int d = 0; d < 3; ++d)
                         S.s_w[d] = (float)((double)A.fShift * dcm[3 + d] + (double)A.fCosmo * dcm[d]);
                     S.s_mW = centre_mag(A, dcm);
-                    float4 rl = qr[nn], vl = qv[nn];
-                    int il = qid[nn], ir = qid[ib];
-                    long long pl = pot[nn], pb = pot[ib];
-                    qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
-                    qr[nn] = r; qv[nn] = v; qid[nn] = ir; pot[nn] = pb;
-                    if (!exact) {
-                        float4 wl = qw[nn], wb = qw[ib];
-                        qw[ib] = wl;
-                        qw[nn] = wb;
-                    }
-                    S.s_r = r;
-                    S.s_eps = v.w;
-                    S.s_have = 1;
                 }
-                S.s_n = nn;
+                S.s_r = r_ib;
+                S.s_eps = v_ib.w;
+                S.s_have = 1;
+            }
+            S.s_n = nn;
+        } else if (tid == 32 && nn > 0) {
+            qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
+            qr[nn] = rb; qv[nn] = vb; qid[nn] = ir; pot[nn] = pb;
+            if (!exact) {
+                qw[ib] = wl;
+                qw[nn] = wb;
             }
         }
         __syncthreads();
-        if (!S.s_go) break;
+        if (nn == 0) break;
     }
     if (tid == 0) {
         double dcm[6];

@@ -24,7 +24,12 @@ def test_pipeline_vs_reference(gpu_ready, name):
     res = pipeline.run(snap, opts, want_density=True)
     if "nExtraScat" in counts:
         assert f"nExtraScat:{counts['nExtraScat']}" in res.lines
-    assert res.counts["nGroupFoF"] == counts["nGroupFoF"]
+    # Groups before unbinding: within 1e-4 of the reference's count (exact
+    # below 10^4 groups).  The move field sums in another order than the
+    # reference's, so trajectories differ in the last bits, and tau-linking
+    # of a boundary particle can flip; the final catalogue is held to the
+    # same groups and >= 99.9 % agreement below.
+    assert abs(res.counts["nGroupFoF"] - counts["nGroupFoF"]) <= int(1e-4 * counts["nGroupFoF"])
     assert res.counts["nGroup"] == counts["nGroup"]
     assert abs(res.counts["nUnbound"] - counts["nUnbound"]) <= max(2, 0.001 * snap.n)
     gc.check_catalogue(res.grp, res.groups, ref, opts)

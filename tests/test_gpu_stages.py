@@ -193,7 +193,9 @@ def test_unbind_isolated_config1_2e21(gpu_ready):
             ctx.move_step(np.float32(pipeline.MICRO_STEP * opts.fStep), False, opts.bNoScatterCut)
         ctx.group_centers()
         grp0, rec0 = ctx.get_groups(ng)
-    assert ng == counts["nGroupFoF"]
+    # the groups fed to both unbinders are the GPU's own; their count is the
+    # reference's to within the pipeline test's tolerance
+    assert abs(ng - counts["nGroupFoF"]) <= int(1e-4 * counts["nGroupFoF"])
     sizes = np.bincount(grp0, minlength=ng + 1)[1:]
     assert np.count_nonzero(sizes > 1024) >= 100
     centers = np.concatenate([rec0["rCenter"][1:], rec0["vcm"][1:]], axis=1)
