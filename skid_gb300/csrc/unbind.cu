@@ -849,6 +849,11 @@ struct BlockShared {
     ArgRed gmx[8], gmn[8];
     int ccnt[BS / 32];          // per-warp arg-max candidate counts (two for a thread with two)
     int cidx[BS / 32];          // the warp's first candidate
+    // records of each warp's first candidate (slot BS/32: the removed member
+    // when the decision needed the exact energies)
+    float4 cr[BS / 32 + 1], cv[BS / 32 + 1], cw[BS / 32 + 1];
+    long long cp[BS / 32 + 1];
+    int cid[BS / 32 + 1];
 };
 
 // max_j |a c_j| + |aH c_{j-3}| of a centre (rcm, vcm)
@@ -965,6 +970,19 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         ArgRed mx{-FLT_MAX, 0x7fffffff}, mn{FLT_MAX, 0x7fffffff};
         ArgRed x2 = mx, n2 = mn;
         float gmax = -FLT_MAX, gmin = FLT_MAX, bnd = 0.0f;
+        // The lane holding its warp's largest FP32 energy (the only lane of
+        // the warp that can hold the member removed in the usual pass)
+        // prefetches that member's records into L1 while the block meets at
+        // the barrier.
+        auto prefetch_top = [&](float wmax) {
+            if (mx.v == wmax && mx.i < n) {
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(qr + mx.i));
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(qv + mx.i));
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(pot + mx.i));
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(qid + mx.i));
+                if (!exact) asm volatile("prefetch.global.L1 [%0];" ::"l"(qw + mx.i));
+            }
+        };
         if (exact) {
             float dmax = 0.0f;
             for (int i = tid; i < n; i += BS) {
@@ -986,6 +1004,7 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 a1 = fminf(a1, __shfl_xor_sync(SKID_FULL, a1, o));
                 dmax = fmaxf(dmax, __shfl_xor_sync(SKID_FULL, dmax, o));
             }
+            prefetch_top(a0);
             if (lane == 0) {
                 S.ext[w][0] = a0;
                 S.ext[w][1] = a1;
@@ -1044,6 +1063,7 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 ddmx = fmaxf(ddmx, __shfl_xor_sync(SKID_FULL, ddmx, o));
                 pemx = fmaxf(pemx, __shfl_xor_sync(SKID_FULL, pemx, o));
             }
+            prefetch_top(a0);
             if (lane == 0) {
                 S.ext[w][0] = a0;
                 S.ext[w][1] = a1;
@@ -1066,6 +1086,18 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
         // exact arg-max or arg-min.
         const float hi = gmax - 2.0f * bnd, lo = gmin + 2.0f * bnd;
         const ArgRed t1 = mx, b1 = mn;
+        // the last member's records, final for this pass now (their owners
+        // wrote the potentials before the barrier), for the swap
+        float4 lr = make_float4(0.0f, 0.0f, 0.0f, 0.0f), lv = lr, lw = lr;
+        long long lp = 0;
+        int lq = 0;
+        if (tid == 32 && n > 1) {
+            lr = qr[n - 1];
+            lv = qv[n - 1];
+            lp = pot[n - 1];
+            lq = qid[n - 1];
+            if (!exact) lw = qw[n - 1];
+        }
         // members again, in the same order with the same FP32 energies: the
         // candidates on the asked side exactly (FP64, as the reference)
         auto rescan = [&](bool scan_hi, bool scan_lo) {
@@ -1099,12 +1131,22 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
                 S.ccnt[w] = __popc(bal) + (two ? 2 : 0);
                 S.cidx[w] = first;
             }
+            if (bal && lane == __ffs(bal) - 1) {
+                S.cr[w] = qr[t1.i];
+                S.cv[w] = qv[t1.i];
+                S.cw[w] = exact ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : qw[t1.i];
+                S.cp[w] = pot[t1.i];
+                S.cid[w] = qid[t1.i];
+            }
         }
         __syncthreads();
-        int ccnt = 0, cidx = 0;
+        int ccnt = 0, cidx = 0, kw = 0;
         for (int k = 0; k < BS / 32; ++k) {
             const int c = S.ccnt[k];
-            if (c && !ccnt) cidx = S.cidx[k];
+            if (c && !ccnt) {
+                cidx = S.cidx[k];
+                kw = k;
+            }
             ccnt += c;
         }
         bool go;
@@ -1130,6 +1172,15 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
             }
             go = a.v >= 0.0f;   // kd.c:1389-1409: fTotBig starts at -1
             ib = a.i;
+            kw = BS / 32;
+            if (go && tid == 0) {
+                S.cr[kw] = qr[ib];
+                S.cv[kw] = qv[ib];
+                S.cw[kw] = exact ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : qw[ib];
+                S.cp[kw] = pot[ib];
+                S.cid[kw] = qid[ib];
+            }
+            __syncthreads();
         }
         if (A.nounbind || n == 0) go = false;
         if (!go) {
@@ -1155,30 +1206,12 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
             break;
         }
         // Remove member ib, swapping the last member into its slot
-        // (kd.c:1424-1440).  Warp 0 updates the FP64 centre while warp 1
-        // moves the records; the two-warp barrier orders warp 0's reads of
-        // slot ib before warp 1's writes to it.
+        // (kd.c:1424-1440): thread 0 updates the FP64 centre while thread 32
+        // moves the records, both from records already read.
         const int nn = n - 1;
-        float4 r_ib = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v_ib = r_ib;
-        int id_ib = 0;
-        float4 rl = r_ib, vl = r_ib, wl = r_ib, wb = r_ib, rb = r_ib, vb = r_ib;
-        int il = 0, ir = 0;
-        long long pl = 0, pb = 0;
         if (tid == 0) {
-            r_ib = qr[ib];
-            v_ib = qv[ib];
-            id_ib = qid[ib];
-        } else if (tid == 32 && nn > 0) {
-            rl = qr[nn]; vl = qv[nn]; il = qid[nn]; pl = pot[nn];
-            rb = qr[ib]; vb = qv[ib]; ir = qid[ib]; pb = pot[ib];
-            if (!exact) { wl = qw[nn]; wb = qw[ib]; }
-        }
-        if (w < 2) {
-            __syncwarp();
-            asm volatile("barrier.sync 1, 64;" ::: "memory");
-        }
-        if (tid == 0) {
-            A.grp[id_ib] = 0;
+            const float4 r_ib = S.cr[kw], v_ib = S.cv[kw];
+            A.grp[S.cid[kw]] = 0;
             ++nrem;
             if (nn == 0) {
                 S.d_mass = 0.0;
@@ -1202,11 +1235,11 @@ __device__ void block_group(const RemoveArgs &A, int g, BlockShared<BS> &S)
             }
             S.s_n = nn;
         } else if (tid == 32 && nn > 0) {
-            qr[ib] = rl; qv[ib] = vl; qid[ib] = il; pot[ib] = pl;
-            qr[nn] = rb; qv[nn] = vb; qid[nn] = ir; pot[nn] = pb;
+            qr[ib] = lr; qv[ib] = lv; qid[ib] = lq; pot[ib] = lp;
+            qr[nn] = S.cr[kw]; qv[nn] = S.cv[kw]; qid[nn] = S.cid[kw]; pot[nn] = S.cp[kw];
             if (!exact) {
-                qw[ib] = wl;
-                qw[nn] = wb;
+                qw[ib] = lw;
+                qw[nn] = S.cw[kw];
             }
         }
         __syncthreads();
