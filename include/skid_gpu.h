@@ -383,6 +383,20 @@ int skid_field(skid_ctx *ctx, int nm, const float *mpos, float *acc);
 /* Friends-of-friends of n explicit points (kd.c:802-917). */
 int skid_fof_points(skid_ctx *ctx, int n, const float *pos, float fTau, int *grp, int *nGroup);
 
+/* The float pair factor of the unbinding potentials ("dir" of kdCellPot,
+ * kdSubPot and kdAddScoopPot, grav.c:25-30,50-55,118-124, with SPLINE_POT of
+ * grav.h:11-31) for n pairs of squared distance d2[i] and summed softening
+ * twoh[i] (host arrays), computed on the device into out[n]:
+ *   SKID_PAIR_USED       the form the unbinding kernels use;
+ *   SKID_PAIR_FP64       the reference's FP64 expression, rounded to float;
+ *   SKID_PAIR_SPLINE_FF  the float-float spline alone, NaN where it leaves
+ *                        the value to the FP64 expression.
+ * A numerics check: the first two must agree bit for bit. */
+#define SKID_PAIR_USED 0
+#define SKID_PAIR_FP64 1
+#define SKID_PAIR_SPLINE_FF 2
+int skid_pair_factor(int n, const float *d2, const float *twoh, int plummer, int mode, float *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,6 +33,7 @@
 // or fixed through the context's options.  A per-group mode (one potential
 // and one removal launch per group, the reference's serial loop on the GPU)
 // serves as the unbatched comparison.
+#include <algorithm>
 #include <cfloat>
 #include <vector>
 
@@ -123,13 +124,113 @@ __device__ __forceinline__ float ref_rsqrt(float x)
     return s;
 }
 
+// Float-float numbers (an unevaluated sum h + l, |l| <= ulp(h) / 2) with
+// round-to-nearest intrinsics throughout, so no step is contracted.  Every
+// operation is within about 2^-46 (relative) of the real result.
+struct ffl {
+    float h, l;
+};
+
+__device__ __forceinline__ ffl ff_norm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ ffl ff_add(ffl a, ffl b)
+{
+    const float s = __fadd_rn(a.h, b.h);
+    const float v = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    return ff_norm(s, e);
+}
+
+__device__ __forceinline__ ffl ff_mul(ffl a, ffl b)
+{
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return ff_norm(p, e);
+}
+
+// A double constant as the nearest float pair (within 2^-48 of it).
+#define SKID_FFC(x) ffl{(float)(x), (float)((x) - (double)(float)(x))}
+
+// The spline branch of the reference's pair factor (grav.h:11-31 as
+// grav.c:25-30 evaluates it, r < 2h) without FP64: the same real-number
+// expression in float-float arithmetic, within about 2^-37 (relative) of
+// its real value -- the one polynomial with cancellation has terms up to 16
+// times its value -- while the reference's FP64 evaluation is within about
+// 2^-45.  Both therefore round to the same float unless the value lies
+// within 2^-32 (relative) of a midpoint between floats, or r is that close
+// to 2h or u = 2r/(2h) to 1 (where the reference's own rounding could take
+// the other branch).  Those inputs, tiny ones and powers of two return
+// false, and the caller takes the FP64 expression.
+__device__ __forceinline__ bool ref_spline_ff(float d2, float twoh, float &out)
+{
+    if (!(d2 >= 1e-30f && twoh >= 1e-30f && twoh <= 1e30f)) return false;
+    // r = sqrt(d2): the correctly rounded root plus one Newton correction
+    // (d2 - s^2 is exact by a fused multiply-add)
+    const float s = __fsqrt_rn(d2);
+    const ffl r = ff_norm(s, __fdiv_rn(__fmaf_rn(-s, s, d2), __fmul_rn(2.0f, s)));
+    // the branch r < 2h, decided only when r is clear of 2h
+    const float dr = ff_add(r, ffl{-twoh, 0.0f}).h;
+    if (fabsf(dr) <= 0x1p-40f * twoh) return false;
+    if (dr >= 0.0f) return false;   // 1/r beyond the softening: not this branch
+    // dih = 2/(2h), the quotient plus its remainder (exact by a fused multiply-add)
+    const float q = __fdiv_rn(2.0f, twoh);
+    const ffl dih = ff_norm(q, __fdiv_rn(__fmaf_rn(-q, twoh, 2.0f), twoh));
+    const ffl u = ff_mul(r, dih);
+    const float du = __fadd_rn(__fsub_rn(u.h, 1.0f), u.l);
+    if (fabsf(du) <= 0x1p-38f) return false;
+    const ffl u2 = ff_mul(u, u);
+    const ffl u4 = ff_mul(u2, u2);
+    const ffl u5 = ff_mul(u4, u);
+    ffl v;
+    if (du < 0.0f) {
+        // dih*(7/5 - 2/3 u^2 + 3/10 u^4 - 1/10 u^5)
+        ffl p = ff_add(SKID_FFC(7.0 / 5.0), ff_mul(SKID_FFC(-2.0 / 3.0), u2));
+        p = ff_add(p, ff_mul(SKID_FFC(3.0 / 10.0), u4));
+        p = ff_add(p, ff_mul(SKID_FFC(-1.0 / 10.0), u5));
+        v = ff_mul(dih, p);
+    } else {
+        // -1/15 / r + dih*(8/5 - 4/3 u^2 + u^3 - 3/10 u^4 + 1/30 u^5)
+        const ffl u3 = ff_mul(u2, u);
+        ffl p = ff_add(SKID_FFC(8.0 / 5.0), ff_mul(SKID_FFC(-4.0 / 3.0), u2));
+        p = ff_add(p, u3);
+        p = ff_add(p, ff_mul(SKID_FFC(-3.0 / 10.0), u4));
+        p = ff_add(p, ff_mul(SKID_FFC(1.0 / 30.0), u5));
+        // 1/r: the rounded reciprocal and its residual 1 - r y
+        const float y = __frcp_rn(r.h);
+        const float t = __fmaf_rn(-r.l, y, __fmaf_rn(-r.h, y, 1.0f));
+        const ffl dir = ff_norm(y, __fmul_rn(y, t));
+        v = ff_add(ff_mul(dih, p), ff_mul(SKID_FFC(-1.0 / 15.0), dir));
+    }
+    // the float nearest v, kept unless v is within 2^-9 ulp of a midpoint
+    const float f = __fadd_rn(v.h, v.l);
+    const float e = __fadd_rn(__fsub_rn(v.h, f), v.l);
+    const unsigned fb = __float_as_uint(f);
+    if (!(f >= 1e-30f && f <= 1e30f) || (fb & 0x7fffffu) == 0u) return false;
+    // (1/2 - 2^-9) ulp(f): exponent of ulp/4, mantissa 2 - 2^-7
+    const float near = __uint_as_float(((fb & 0x7f800000u) - (25u << 23)) | 0x7f0000u);
+    if (fabsf(e) >= near) return false;
+    out = f;
+    return true;
+}
+#undef SKID_FFC
+
 // The pair factor of every potential term, added (potentials, scoop) and
 // subtracted (removal) alike, equal to the reference's float dir.  Beyond
 // the softening (r >= 2h, certain once d2 clears (2h)^2 by the margin below)
-// it is ref_rsqrt; inside, and for Plummer softening, the FP64 form.
+// it is ref_rsqrt; inside, the float-float spline where it decides the
+// rounding, else (and for Plummer softening) the FP64 form.
 __device__ __forceinline__ float pair_dir(float d2, float twoh, int plummer)
 {
     if (!plummer && d2 >= twoh * twoh * 1.000001f) return ref_rsqrt(d2);
+    float v;
+    if (!plummer && ref_spline_ff(d2, twoh, v)) return v;
     return ref_dir_fp64(d2, twoh, plummer);
 }
 
@@ -1942,3 +2043,57 @@ cudaError_t unbind_run(GroupState &G, const int *gof, int nslots, const float4 *
 }
 
 }  // namespace skid
+
+// ---- numerics check of the pair factor ----
+
+namespace {
+
+__global__ void pair_factor_kernel(const float *__restrict__ d2, const float *__restrict__ twoh, int n,
+                                   int plummer, int mode, float *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float v = __int_as_float(0x7fc00000);   // NaN: the float-float form declined
+        if (mode == SKID_PAIR_FP64) v = skid::ref_dir_fp64(d2[i], twoh[i], plummer);
+        else if (mode == SKID_PAIR_SPLINE_FF) skid::ref_spline_ff(d2[i], twoh[i], v);
+        else v = skid::pair_dir(d2[i], twoh[i], plummer);
+        out[i] = v;
+    }
+}
+
+}  // namespace
+
+extern "C" int skid_pair_factor(int n, const float *d2, const float *twoh, int plummer, int mode,
+                                float *out)
+{
+    if (n < 0 || (n > 0 && (!d2 || !twoh || !out))) return SKID_EINVAL;
+    if (mode != SKID_PAIR_USED && mode != SKID_PAIR_FP64 && mode != SKID_PAIR_SPLINE_FF)
+        return SKID_EINVAL;
+    if (n == 0) return 0;
+    float *dv = nullptr;
+    const size_t bytes = (size_t)n * sizeof(float);
+    {
+        std::lock_guard<std::recursive_mutex> lk(skid::device_mutex());
+        if (cudaMalloc((void **)&dv, 3 * bytes)) {
+            cudaGetLastError();
+            return SKID_ENOMEM;
+        }
+    }
+    cudaError_t e = cudaMemcpy(dv, d2, bytes, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(dv + n, twoh, bytes, cudaMemcpyHostToDevice);
+    if (!e) {
+        const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, 65536);
+        pair_factor_kernel<<<blocks, 256>>>(dv, dv + n, n, plummer, mode, dv + 2 * (size_t)n);
+        skid::note_launch();
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpy(out, dv + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+    {
+        std::lock_guard<std::recursive_mutex> lk(skid::device_mutex());
+        cudaFree(dv);
+    }
+    if (e) {
+        cudaGetLastError();
+        return SKID_ECUDA;
+    }
+    return 0;
+}

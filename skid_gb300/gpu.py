@@ -121,7 +121,12 @@ SIGNATURES = {
     "skid_field_adjoint": [_V, C.c_int, _F, _F, _F],
     "skid_potential_adjoint": [_V, C.c_int, C.c_float, C.c_int, _I, _F, _D, _F],
     "skid_batch_run": [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int],
+    "skid_pair_factor": [C.c_int, _F, _F, C.c_int, C.c_int, _F],
 }
+
+PAIR_USED = 0
+PAIR_FP64 = 1
+PAIR_SPLINE_FF = 2
 
 ADJ_RECOMPUTE = 0
 ADJ_STORED = 1
@@ -401,6 +406,21 @@ class Context:
         ng = C.c_int()
         self._call("skid_fof_points", self.h, len(pos), _f(pos), tau, _i(grp), C.byref(ng))
         return grp, ng.value
+
+
+def pair_factor(d2, twoh, plummer=False, mode=PAIR_USED):
+    """The unbinding potentials' float pair factor for squared distances d2
+    and summed softenings twoh, computed on the device (skid_pair_factor)."""
+    lib = load()
+    d2 = _c32(d2)
+    twoh = _c32(twoh)
+    if d2.shape != twoh.shape:
+        raise ValueError("d2 and twoh differ in length")
+    out = np.empty(len(d2), np.float32)
+    rc = lib.skid_pair_factor(len(d2), _f(d2), _f(twoh), int(plummer), int(mode), _f(out))
+    if rc:
+        raise SkidError(rc, "skid_pair_factor")
+    return out
 
 
 def batch_run(volumes, opts, n_workers=8, device=0, group_cap=None):
