@@ -311,6 +311,16 @@ def cli_process_wall(snap, repeats=3):
             if r.returncode:
                 raise RuntimeError(f"skid CLI failed: {r.stderr[-400:]}")
             out = r.stdout
+        # one more run for the wall-clock phases the tool reports on request
+        # (with a CUDA start-up probe first, so start-up and reading separate)
+        phases = {}
+        with open(inp, "rb") as f:
+            r = subprocess.run(cmd, stdin=f, cwd=tmp, capture_output=True, text=True,
+                               env=dict(os.environ, SKID_WALL_TIMES="2"))
+        for line in r.stderr.splitlines():
+            parts = line.split()
+            if len(parts) == 3 and parts[0] == "wall_ms":
+                phases[parts[1]] = round(float(parts[2]), 3)
         files = sorted(f for f in os.listdir(tmp) if f.startswith("out."))
     device = {}
     for line in out.splitlines():
@@ -321,6 +331,7 @@ def cli_process_wall(snap, repeats=3):
     best = min(walls)
     return {"value": snap.n / best, "unit": UNIT, "wall_s": best, "walls_s": walls,
             "n_particles": snap.n, "files": files, "device_stage_ms": device,
+            "host_phases_ms": phases,
             "command": "skid_gb300/bin/skid " + " ".join(flags()) + " -o out < input.bin"}
 
 

@@ -16,6 +16,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "skid_gpu.h"
 #include "tipsy_io.h"
@@ -251,10 +252,42 @@ static int read_unbind_inputs(const options *o, const snapshot *s, int **grp, in
     return 0;
 }
 
+/* Wall-clock phases of the process, printed to stderr when SKID_WALL_TIMES
+ * is set (1: the phases as they run; 2: also a CUDA start-up probe before
+ * the input is read, which separates driver start-up from reading). */
+static double wall_ms(void)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return 1e3 * (double)t.tv_sec + 1e-6 * (double)t.tv_nsec;
+}
+
+static int g_wall = 0;
+static double g_wall_t = 0.0;
+
+static void wall_mark(const char *phase)
+{
+    if (!g_wall) return;
+    const double t = wall_ms();
+    fprintf(stderr, "wall_ms %s %.3f\n", phase, t - g_wall_t);
+    g_wall_t = t;
+}
+
 int main(int argc, char **argv)
 {
     options o;
+    {
+        const char *w = getenv("SKID_WALL_TIMES");
+        g_wall = w ? atoi(w) : 0;
+        g_wall_t = wall_ms();
+        if (g_wall) fprintf(stderr, "wall_abs_ms main %.3f\n", g_wall_t);
+    }
     parse(argc, argv, &o);
+    if (g_wall >= 2) {
+        void *probe = NULL;
+        if (skid_host_alloc(16, &probe) == SKID_OK) skid_host_free(probe);
+        wall_mark("cuda_start");
+    }
     printf("SKID v1.4.1 (GB300)\n");
     /* the particle records as they lie in the file, in page-locked memory;
      * they are unpacked on the device (skid_set_tipsy) */
@@ -273,6 +306,7 @@ int main(int argc, char **argv)
     s.n = raw.n;
     printf("nDark:%d nGas:%d nStar:%d\n", s.nDark, s.nGas, s.nStar);
     fflush(stdout);
+    wall_mark("read");
 
     skid_params par;
     memset(&par, 0, sizeof(par));
@@ -285,6 +319,7 @@ int main(int argc, char **argv)
     par.device = 0;
     die_on(skid_create(&g_ctx, &par), "skid_create");
     skid_ctx *ctx = g_ctx;
+    wall_mark("create");
     /* One run per process: timing the 18 candidate removal schedules would
      * cost more than it saves, so the tool takes the schedule the tuner
      * picks on clustered snapshots (a warp per group of up to 1024 members,
@@ -304,6 +339,7 @@ int main(int argc, char **argv)
         tipsy_raw_positions(&raw, o.bStandard, s.pos);
     }
     tipsy_raw_free(&raw);
+    wall_mark("upload");
 
     int nFoF = 0;
     int inType = (s.nDark ? T_DARK : 0) | (s.nGas ? T_GAS : 0) | (s.nStar ? T_STAR : 0);
@@ -369,6 +405,7 @@ int main(int argc, char **argv)
     die_on(skid_too_small(ctx, o.nMembers, &nGroup), "skid_too_small");
     printf("Number of Groups:%d\n", nGroup);
     fflush(stdout);
+    wall_mark("pipeline");
 
     int *grp = malloc((size_t)(s.n > 0 ? s.n : 1) * sizeof(int));
     skid_group *gr = malloc(((size_t)nGroup + 1) * sizeof(skid_group));
@@ -411,6 +448,7 @@ int main(int argc, char **argv)
         snprintf(path, sizeof(path), "%s.stat", o.achName);
         if (write_stats(path, &o, ctx, gr, nGroup)) fprintf(stderr, "skid: cannot write %s\n", path);
     }
+    wall_mark("outputs");
     skid_timings t;
     die_on(skid_get_timings(ctx, &t), "skid_get_timings");
     printf("SKID GPU Time (device ms):\n");
@@ -427,5 +465,7 @@ int main(int argc, char **argv)
     free(moved);
     skid_destroy(ctx);
     tipsy_free(&s);
+    wall_mark("teardown");
+    if (g_wall) fprintf(stderr, "wall_abs_ms end %.3f\n", wall_ms());
     return 0;
 }
