@@ -551,7 +551,8 @@ def run_gpu(args):
     cli = None if args.no_cli else cli_process_wall(snap)
     extra = None
     if not args.no_extra and world == 1 and CONFIG == 1:
-        extra = {"adjoint_2e20": adjoint_workload(3), "mixed_2e24": mixed_workload(2)}
+        extra = {"adjoint_2e20": adjoint_workload(3), "mixed_2e24": mixed_workload(2),
+                 "batch_96": batch_workload(96, 12, 1)}
     tm = res.timings
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -742,7 +743,7 @@ def mixed_workload(steps=2):
             "generation_s": round(gen_s, 1)}
 
 
-def run_batch(args):
+def batch_workload(n_vol=96, workers=12, steps=1):
     """Config 2: independent periodic subvolumes of uneven sizes (N log-uniform
     in [2^14, 2^20], halos proportional to N, nSmooth from {32, 64, 128},
     tau = 0.5 N^(-1/3)) through skid_batch_run, host buffers in and out
@@ -750,39 +751,44 @@ def run_batch(args):
     from skid_gb300 import build, gpu, synth
     from skid_gb300.options import Options
     build.build_lib()
-    specs = synth.subvolume_specs(args.n_vol)
+    specs = synth.subvolume_specs(n_vol)
     t0 = time.perf_counter()
     vols = [(synth.make_snapshot(spec), k, tau) for spec, k, tau in specs]
     gen_s = time.perf_counter() - t0
     ntot = sum(v[0].n for v in vols)
     base = Options.parse(["-tau", "0.01", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
                           "-H", f"{synth.hubble_for(0.3):.6g}"])
-    gpu.batch_run(vols[:4], base, n_workers=min(4, args.workers))     # warm-up
+    gpu.batch_run(vols[:4], base, n_workers=min(4, workers))     # warm-up
     out = {}
-    for w in (args.workers, 1):
+    for w in (workers, 1):
         best = None
-        for _ in range(max(1, args.steps)):
+        for _ in range(max(1, steps)):
             t = time.perf_counter()
             res = gpu.batch_run(vols, base, n_workers=w)
             dt = time.perf_counter() - t
             best = dt if best is None else min(best, dt)
         out[w] = (best, res)
-    wbest, res = out[args.workers]
+    wbest, res = out[workers]
     sbest, sres = out[1]
     same = all(np.array_equal(a["grp"], b["grp"]) for a, b in zip(res, sres))
     line = {"metric": "particles/s end-to-end SKID, batched subvolumes", "value": ntot / wbest,
-            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 1,
+            "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 1,
             "ms_per_step": 1000 * wbest, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{len(vols)} periodic subvolumes, N log-uniform in [2^14, 2^20] "
                                    f"({ntot} particles), halos proportional to N, nSmooth in "
                                    f"{{32, 64, 128}}, tau = 0.5 N^(-1/3)",
-                       "workers": args.workers, "sequential_value": ntot / sbest,
+                       "workers": workers, "sequential_value": ntot / sbest,
                        "sequential_ms": 1000 * sbest, "identical_to_sequential": bool(same),
                        "groups": int(sum(r["nGroup"] for r in res)),
                        "device_ms_sum": float(sum(r["device_ms"] for r in res)),
                        "generation_s": gen_s}}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_batch(args):
+    """Config 2 alone: prints batch_workload's line."""
+    print(json.dumps(batch_workload(args.n_vol, args.workers, args.steps)), flush=True)
     return 0
 
 
@@ -797,7 +803,8 @@ def main():
     ap.add_argument("--no-cli", action="store_true",
                     help="skip the skid command-line process wall-time runs")
     ap.add_argument("--no-extra", action="store_true",
-                    help="skip the adjoint (2^20) and mixed-species (2^24) workload runs")
+                    help="skip the adjoint (2^20), mixed-species (2^24) and batched-subvolume "
+                         "workload runs")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain-form and -nsp comparison runs")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "mixed", "adjoint"],
