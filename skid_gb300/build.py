@@ -96,7 +96,7 @@ def build_cli(force: bool = False) -> str | None:
         tmp = CLI + f".tmp{os.getpid()}"
         cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-Wall",
                "-I" + os.path.join(ROOT, "include"), "-o", tmp, *srcs, "-L" + LIBDIR, "-lskidgpu",
-               "-Wl,-rpath,$ORIGIN/../lib", "-lm"]
+               "-Wl,-rpath,$ORIGIN/../lib", "-lm", "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
             raise RuntimeError(f"CLI build failed:\n{r.stderr}")

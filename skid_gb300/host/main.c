@@ -410,9 +410,11 @@ int main(int argc, char **argv)
     int *grp = malloc((size_t)(s.n > 0 ? s.n : 1) * sizeof(int));
     skid_group *gr = malloc(((size_t)nGroup + 1) * sizeof(skid_group));
     die_on(skid_get_groups(ctx, grp, gr), "skid_get_groups");
+    wall_mark("fetch");
     char path[300];
     snprintf(path, sizeof(path), "%s.grp", o.achName);
     if (write_grp(path, s.n, grp)) fprintf(stderr, "skid: cannot write %s\n", path);
+    wall_mark("grp");
     {
         float *gm = malloc(((size_t)nGroup + 1) * sizeof(float));
         float *gp = malloc(3 * ((size_t)nGroup + 1) * sizeof(float));

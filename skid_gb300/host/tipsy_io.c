@@ -6,9 +6,11 @@
 #include "skid_gpu.h"
 
 #include <errno.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #define GAS_FLOATS 12
 #define DARK_FLOATS 9
@@ -244,30 +246,118 @@ static char *put_int(char *p, int v)
     return p;
 }
 
+/* One line per value, formatted in parallel chunks on the host's cores and
+ * written in order: the same bytes as formatting the lines one after
+ * another.  fmt writes line i at p (at most maxlen bytes, plus a NUL it may
+ * leave after them) and returns its length. */
+typedef size_t (*line_fmt)(char *p, const void *data, size_t i);
+
+typedef struct {
+    line_fmt fmt;
+    const void *data;
+    size_t lo, hi, len;
+    char *buf;
+} line_job;
+
+static void *format_lines(void *arg)
+{
+    line_job *j = (line_job *)arg;
+    char *p = j->buf;
+    for (size_t i = j->lo; i < j->hi; ++i) p += j->fmt(p, j->data, i);
+    j->len = (size_t)(p - j->buf);
+    return NULL;
+}
+
+enum { LINE_THREADS_MAX = 16 };
+
+static int write_lines(FILE *fp, size_t n, line_fmt fmt, const void *data, size_t maxlen)
+{
+    int nt = 1;
+    if (n >= 65536) {
+        long c = sysconf(_SC_NPROCESSORS_ONLN);
+        nt = c < 1 ? 1 : c > LINE_THREADS_MAX ? LINE_THREADS_MAX : (int)c;
+    }
+    line_job job[LINE_THREADS_MAX];
+    pthread_t th[LINE_THREADS_MAX];
+    int started[LINE_THREADS_MAX] = {0};
+    const size_t per = (n + (size_t)nt - 1) / (size_t)nt;
+    int rc = 0;
+    for (int t = 0; t < nt; ++t) {
+        job[t].fmt = fmt;
+        job[t].data = data;
+        job[t].lo = (size_t)t * per < n ? (size_t)t * per : n;
+        job[t].hi = (size_t)(t + 1) * per < n ? (size_t)(t + 1) * per : n;
+        job[t].len = 0;
+        job[t].buf = malloc((job[t].hi - job[t].lo) * maxlen + 1);
+        if (!job[t].buf) rc = -1;
+    }
+    if (!rc) {
+        for (int t = 1; t < nt; ++t)
+            started[t] = pthread_create(&th[t], NULL, format_lines, &job[t]) == 0;
+        format_lines(&job[0]);
+        for (int t = 1; t < nt; ++t) {
+            if (started[t]) pthread_join(th[t], NULL);
+            else format_lines(&job[t]);   /* no thread: this one formats the chunk */
+        }
+        for (int t = 0; t < nt && !rc; ++t)
+            if (fwrite(job[t].buf, 1, job[t].len, fp) != job[t].len) rc = -1;
+    }
+    for (int t = 0; t < nt; ++t) free(job[t].buf);
+    return rc;
+}
+
+static size_t grp_line(char *p, const void *data, size_t i)
+{
+    return (size_t)(put_int(p, ((const int *)data)[i]) - p);
+}
+
 int write_grp(const char *path, int n, const int *grp)
 {
     FILE *fp = fopen(path, "w");
     if (!fp) return -1;
-    size_t cap = 1 << 20;
-    char *buf = malloc(cap + 32);
-    char *p = buf;
-    p = put_int(p, n);
-    for (int i = 0; i < n; ++i) {
-        p = put_int(p, grp[i]);
-        if ((size_t)(p - buf) > cap) { fwrite(buf, 1, (size_t)(p - buf), fp); p = buf; }
-    }
-    fwrite(buf, 1, (size_t)(p - buf), fp);
-    free(buf);
-    return fclose(fp) ? -1 : 0;
+    char head[16];
+    int rc = fwrite(head, 1, (size_t)(put_int(head, n) - head), fp) ? 0 : -1;
+    if (!rc && n > 0) rc = write_lines(fp, (size_t)n, grp_line, grp, 12);
+    return fclose(fp) || rc ? -1 : 0;
+}
+
+static size_t den_line(char *p, const void *data, size_t i)
+{
+    return (size_t)snprintf(p, 32, "%.10g\n", ((const float *)data)[i]);
 }
 
 int write_den(const char *path, int n, const float *rho)
 {
     FILE *fp = fopen(path, "w");
     if (!fp) return -1;
-    fprintf(fp, "%d\n", n);
-    for (int i = 0; i < n; ++i) fprintf(fp, "%.10g\n", rho[i]);
-    return fclose(fp) ? -1 : 0;
+    int rc = fprintf(fp, "%d\n", n) < 0 ? -1 : 0;
+    if (!rc && n > 0) rc = write_lines(fp, (size_t)n, den_line, rho, 31);
+    return fclose(fp) || rc ? -1 : 0;
+}
+
+typedef struct {
+    const snapshot *s;
+    const float *moved;
+    const int *flag;
+    float h[3];
+} ray_data;
+
+/* Line d*n + i: the wrapped displacement of particle i along axis d. */
+static size_t ray_line(char *p, const void *data, size_t k)
+{
+    const ray_data *r = (const ray_data *)data;
+    const size_t n = (size_t)r->s->n, i = k % n;
+    const int d = (int)(k / n);
+    if (!r->flag[i]) {
+        p[0] = '0';
+        p[1] = '\n';
+        return 2;
+    }
+    float dx = r->moved[3 * i + d] - r->s->pos[3 * i + d];
+    const float h = r->h[d];
+    if (dx > h) dx -= 2 * h;
+    if (dx <= -h) dx += 2 * h;
+    return (size_t)snprintf(p, 32, "%g\n", dx);
 }
 
 int write_ray(const char *path, const snapshot *s, const float *moved, const int *moved_flag,
@@ -275,21 +365,11 @@ int write_ray(const char *path, const snapshot *s, const float *moved, const int
 {
     FILE *fp = fopen(path, "w");
     if (!fp) return -1;
-    fprintf(fp, "%d\n", s->n);
-    for (int d = 0; d < 3; ++d) {
-        float h = (float)(0.5 * (double)period[d]);
-        for (int i = 0; i < s->n; ++i) {
-            if (!moved_flag[i]) {
-                fprintf(fp, "0\n");
-                continue;
-            }
-            float dx = moved[3 * (size_t)i + d] - s->pos[3 * (size_t)i + d];
-            if (dx > h) dx -= 2 * h;
-            if (dx <= -h) dx += 2 * h;
-            fprintf(fp, "%g\n", dx);
-        }
-    }
-    return fclose(fp) ? -1 : 0;
+    int rc = fprintf(fp, "%d\n", s->n) < 0 ? -1 : 0;
+    ray_data r = {s, moved, moved_flag, {0.0f, 0.0f, 0.0f}};
+    for (int d = 0; d < 3; ++d) r.h[d] = (float)(0.5 * (double)period[d]);
+    if (!rc && s->n > 0) rc = write_lines(fp, 3 * (size_t)s->n, ray_line, &r, 31);
+    return fclose(fp) || rc ? -1 : 0;
 }
 
 int read_grp(const char *path, int **grp, char *err, size_t errlen)
