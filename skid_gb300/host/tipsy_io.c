@@ -269,24 +269,23 @@ static void *format_lines(void *arg)
 }
 
 enum { LINE_THREADS_MAX = 16 };
+/* Lines formatted per block (bounds the text held at once). */
+#define LINE_BLOCK ((size_t)1 << 22)
 
-static int write_lines(FILE *fp, size_t n, line_fmt fmt, const void *data, size_t maxlen)
+/* Lines [lo, hi) in nt chunks, then written in order. */
+static int write_block(FILE *fp, size_t lo, size_t hi, int nt, line_fmt fmt, const void *data,
+                       size_t maxlen)
 {
-    int nt = 1;
-    if (n >= 65536) {
-        long c = sysconf(_SC_NPROCESSORS_ONLN);
-        nt = c < 1 ? 1 : c > LINE_THREADS_MAX ? LINE_THREADS_MAX : (int)c;
-    }
     line_job job[LINE_THREADS_MAX];
     pthread_t th[LINE_THREADS_MAX];
     int started[LINE_THREADS_MAX] = {0};
-    const size_t per = (n + (size_t)nt - 1) / (size_t)nt;
+    const size_t n = hi - lo, per = (n + (size_t)nt - 1) / (size_t)nt;
     int rc = 0;
     for (int t = 0; t < nt; ++t) {
         job[t].fmt = fmt;
         job[t].data = data;
-        job[t].lo = (size_t)t * per < n ? (size_t)t * per : n;
-        job[t].hi = (size_t)(t + 1) * per < n ? (size_t)(t + 1) * per : n;
+        job[t].lo = lo + ((size_t)t * per < n ? (size_t)t * per : n);
+        job[t].hi = lo + ((size_t)(t + 1) * per < n ? (size_t)(t + 1) * per : n);
         job[t].len = 0;
         job[t].buf = malloc((job[t].hi - job[t].lo) * maxlen + 1);
         if (!job[t].buf) rc = -1;
@@ -303,6 +302,19 @@ static int write_lines(FILE *fp, size_t n, line_fmt fmt, const void *data, size_
             if (fwrite(job[t].buf, 1, job[t].len, fp) != job[t].len) rc = -1;
     }
     for (int t = 0; t < nt; ++t) free(job[t].buf);
+    return rc;
+}
+
+static int write_lines(FILE *fp, size_t n, line_fmt fmt, const void *data, size_t maxlen)
+{
+    int nt = 1;
+    if (n >= 65536) {
+        long c = sysconf(_SC_NPROCESSORS_ONLN);
+        nt = c < 1 ? 1 : c > LINE_THREADS_MAX ? LINE_THREADS_MAX : (int)c;
+    }
+    int rc = 0;
+    for (size_t lo = 0; lo < n && !rc; lo += LINE_BLOCK)
+        rc = write_block(fp, lo, lo + LINE_BLOCK < n ? lo + LINE_BLOCK : n, nt, fmt, data, maxlen);
     return rc;
 }
 
