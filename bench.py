@@ -552,7 +552,7 @@ def run_gpu(args):
     extra = None
     if not args.no_extra and world == 1 and CONFIG == 1:
         extra = {"adjoint_2e20": adjoint_workload(3), "mixed_2e24": mixed_workload(2),
-                 "batch_96": batch_workload(96, 12, 1)}
+                 "batch_96": batch_workload(96, 12, 1, cpu=not args.no_cpu_baseline)}
     tm = res.timings
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -743,7 +743,39 @@ def mixed_workload(steps=2):
             "generation_s": round(gen_s, 1)}
 
 
-def batch_workload(n_vol=96, workers=12, steps=1):
+def batch_cpu_baseline(vols, rest):
+    """Reference skid on the host cores over the 16 volumes of the batch
+    nearest its median size (each single-threaded, 16 processes at a time:
+    the batch's largest volumes would take a minute each on one core)."""
+    import tempfile
+    from skid_gb300 import synth
+    exe, why = reference_binary()
+    cores = os.cpu_count() or 1
+    ln = np.log2([v[0].n for v in vols])
+    pick = sorted(np.argsort(np.abs(ln - np.median(ln)), kind="stable")[:16])
+    workers = min(cores, len(pick))
+    with tempfile.TemporaryDirectory() as tmp:
+        inputs = []
+        for i in pick:
+            snap, k, tau = vols[i]
+            path = os.path.join(tmp, f"vol{i:02d}.bin")
+            synth.write_snapshot(path, snap)
+            inputs.append((path, ["-tau", repr(float(np.float32(tau))), "-s", str(k)] + rest))
+        wall, per_run, counts = reference_step(exe, inputs, workers, tmp)
+    ns = [vols[i][0].n for i in pick]
+    kind = "reference" if exe else "port"
+    what = ("reference skid v1.4.1 built from its own sources on this host (gcc -O2 "
+            "-ffp-contract=off)" if kind == "reference" else
+            f"the oracle's C restatement of skid ({why})")
+    return {"value": sum(ns) / wall, "unit": UNIT, "cores": workers, "kind": kind,
+            "per_core_value": sum(ns) / sum(per_run), "n_particles": int(sum(ns)),
+            "sample": f"{what}: the {len(pick)} volumes of the batch nearest its median size "
+                      f"(N {min(ns)}-{max(ns)}, each with its own nSmooth and tau), {workers} "
+                      f"processes at a time, each single-threaded; {wall:.1f} s wall",
+            "catalogue": counts}
+
+
+def batch_workload(n_vol=96, workers=12, steps=1, cpu=False):
     """Config 2: independent periodic subvolumes of uneven sizes (N log-uniform
     in [2^14, 2^20], halos proportional to N, nSmooth from {32, 64, 128},
     tau = 0.5 N^(-1/3)) through skid_batch_run, host buffers in and out
@@ -756,8 +788,8 @@ def batch_workload(n_vol=96, workers=12, steps=1):
     vols = [(synth.make_snapshot(spec), k, tau) for spec, k, tau in specs]
     gen_s = time.perf_counter() - t0
     ntot = sum(v[0].n for v in vols)
-    base = Options.parse(["-tau", "0.01", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
-                          "-H", f"{synth.hubble_for(0.3):.6g}"])
+    rest = ["-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7", "-H", f"{synth.hubble_for(0.3):.6g}"]
+    base = Options.parse(["-tau", "0.01"] + rest)
     gpu.batch_run(vols[:4], base, n_workers=min(4, workers))     # warm-up
     out = {}
     for w in (workers, 1):
@@ -783,6 +815,8 @@ def batch_workload(n_vol=96, workers=12, steps=1):
                        "groups": int(sum(r["nGroup"] for r in res)),
                        "device_ms_sum": float(sum(r["device_ms"] for r in res)),
                        "generation_s": gen_s}}
+    if cpu:
+        line["cpu_baseline"] = batch_cpu_baseline(vols, rest)
     return line
 
 
