@@ -551,7 +551,8 @@ def run_gpu(args):
     cli = None if args.no_cli else cli_process_wall(snap)
     extra = None
     if not args.no_extra and world == 1 and CONFIG == 1:
-        extra = {"adjoint_2e20": adjoint_workload(3), "mixed_2e24": mixed_workload(2),
+        extra = {"adjoint_2e20": adjoint_workload(3),
+                 "mixed_2e24": mixed_workload(2, cpu=not args.no_cpu_baseline),
                  "batch_96": batch_workload(96, 12, 1, cpu=not args.no_cpu_baseline)}
     tm = res.timings
     line = {
@@ -691,7 +692,32 @@ def adjoint_workload(steps, check_fd=False):
     return line
 
 
-def mixed_workload(steps=2):
+def mixed_cpu_baseline():
+    """Reference skid on one host core over the 32768-particle slice of the
+    mixed-species generator (the 2^24 run itself would take it the better part
+    of an hour)."""
+    import tempfile
+    from skid_gb300 import synth
+    exe, why = reference_binary()
+    snap = synth.make_snapshot(synth.CONFIG4_SLICE)
+    fl = synth.config4_slice_flags()
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "slice.bin")
+        synth.write_snapshot(path, snap)
+        _, per_run, counts = reference_step(exe, [(path, fl)], 1, tmp)
+    kind = "reference" if exe else "port"
+    what = ("reference skid v1.4.1 built from its own sources on this host (gcc -O2 "
+            "-ffp-contract=off)" if kind == "reference" else
+            f"the oracle's C restatement of skid ({why})")
+    return {"value": snap.n / per_run[0], "unit": UNIT, "cores": 1, "kind": kind,
+            "per_core_value": snap.n / per_run[0], "n_particles": snap.n,
+            "sample": f"{what}: the {snap.n}-particle slice of the mixed-species generator "
+                      f"(12 halos, 50 % gas, Gaussian-random-field background; "
+                      f"{' '.join(fl)}), one single-threaded process, {per_run[0]:.2f} s",
+            "catalogue": counts}
+
+
+def mixed_workload(steps=2, cpu=False):
     """Config 4 at full size: 2^24 gas + dark particles (-gd, z = 0.5,
     Zel'dovich k^-2 background), resident and end-to-end particles/s over
     `steps` runs after one warm-up (whose first unbinding tunes the schedule).
@@ -730,7 +756,7 @@ def mixed_workload(steps=2):
     e_ms, _ = timed(True)
     ctx.close()
     tm = res.timings
-    return {"workload": "config 4: N=2^24 (50% gas of mass 0.2, 50% dark), 6000 NFW halos "
+    line = {"workload": "config 4: N=2^24 (50% gas of mass 0.2, 50% dark), 6000 NFW halos "
                         "(3.5 dex, c 4-20, 50%) + Zel'dovich-displaced k^-2 Gaussian random "
                         "field background, z = 0.5, -gd",
             "flags": " ".join(synth.WORKLOAD_FLAGS[4]), "n_particles": snap.n,
@@ -741,6 +767,9 @@ def mixed_workload(steps=2):
             "stage_ms": {k: round(float(tm[k]), 3) for k in
                          ("density_ms", "moving_ms", "fof_ms", "micro_ms", "unbind_ms")},
             "generation_s": round(gen_s, 1)}
+    if cpu:
+        line["cpu_baseline"] = mixed_cpu_baseline()
+    return line
 
 
 def batch_cpu_baseline(vols, rest):

@@ -60,6 +60,19 @@ def config1_spec(n: int) -> HaloSpec:
                     SEED_BASE + 1)
 
 
+# A 32768-particle slice of the mixed-species generator (12 halos, the same
+# species mix, mass range, concentrations and background as the 2^24
+# workload, largest r200 0.05) and its flags (tau scaled to the slice's
+# spacing): a case small enough for reference skid on one core.
+CONFIG4_SLICE = HaloSpec(1 << 15, 12, 3.5, (4.0, 20.0), 0.05, 0.50, SEED_BASE + 4, gas_frac=0.5,
+                         background="grf")
+
+
+def config4_slice_flags() -> list:
+    return ["-tau", "0.016", "-s", "64", "-m", "16", "-p", "1", "-O", "0.3", "-Lambda", "0.7",
+            "-z", "0.5", "-gd", "-H", f"{hubble_for(0.3):.6g}"]
+
+
 def hubble_for(omega0: float) -> float:
     """Self-consistent H0 for G=1, mean density 1: H0 = sqrt(8 pi / (3 Omega0))."""
     return math.sqrt(8.0 * math.pi / (3.0 * omega0))

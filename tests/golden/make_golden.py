@@ -125,8 +125,7 @@ def make_input(name):
 # Workload-scale cases.  "spec": a generator spec (synth.HaloSpec) or
 # "dark.std" (the reference's own demo fixture, XDR); "store": "gz" keeps the
 # input compressed beside the outputs, "regen" keeps only its SHA-256.
-C4_SLICE = synth.HaloSpec(1 << 15, 12, 3.5, (4.0, 20.0), 0.05, 0.50, synth.SEED_BASE + 4,
-                          gas_frac=0.5, background="grf")
+C4_SLICE = synth.CONFIG4_SLICE
 LARGE_CASES = {
     "config0_32k": dict(spec=synth.CONFIGS[0], store="gz",
                         flags=synth.WORKLOAD_FLAGS[0] + ["-den", "-stats"]),
@@ -134,9 +133,7 @@ LARGE_CASES = {
                           flags=["-std", "-tau", "9e-4", "-s", "64", "-d", "170", "-m", "8",
                                  "-H", "2.8944", "-p", "1", "-ray", "-den", "-stats"]),
     "config4_slice_32k": dict(spec=C4_SLICE, store="gz",
-                              flags=["-tau", "0.016", "-s", "64", "-m", "16", "-p", "1", "-O",
-                                     "0.3", "-Lambda", "0.7", "-z", "0.5", "-gd", "-H", H3,
-                                     "-stats"]),
+                              flags=synth.config4_slice_flags() + ["-stats"]),
     "config1_2e18": dict(spec=synth.config1_spec(1 << 18), store="regen",
                          flags=synth.WORKLOAD_FLAGS[1]),
     "config1_2e21": dict(spec=synth.CONFIGS[1], store="regen", flags=synth.WORKLOAD_FLAGS[1]),
