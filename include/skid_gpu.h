@@ -303,8 +303,10 @@ typedef struct skid_batch_flags {
 /* Run the whole pipeline on nVol independent volumes of uneven sizes on one
  * GPU.  nWorkers host workers (each with its own context and CUDA stream)
  * take volumes largest first from a shared queue, so the pipelines of many
- * volumes run on the GPU at once; each worker's contexts reuse their device
- * memory, captured graphs and autotuned unbinding schedule across volumes.
+ * volumes run on the GPU at once; each worker's context reuses its device
+ * memory across volumes (its move-iteration graphs are captured again for
+ * every volume, whose period and step length they carry), and every volume
+ * takes the usual fixed removal schedule rather than tuning one.
  * Results per volume are those of the single-volume sequence.  Returns 0 if
  * every volume succeeded, else the first failing volume's status. */
 int skid_batch_run(skid_volume *vols, int nVol, const skid_batch_flags *flags, int nWorkers,
