@@ -106,6 +106,24 @@ def field_issue():
         return None
 
 
+def roofline_e2e(counts, n, field_bytes, ms, peak, peak_kind):
+    """The whole run against the HBM roofline: its algorithmic bytes (the
+    compulsory traffic of each stage, per unit: tree build 40 B and density
+    24 B per scatterer; every move step the field kernel's 24 B per active
+    mover and 20 B per live scatterer copy, as the library counts them;
+    friends-of-friends 24 B per mover; group reductions 48 B, unbinding 36 B
+    and outputs 4 B per particle) over the run's time."""
+    ns = counts.get("nScatter", n)
+    nm = counts.get("nMove", n)
+    parts = {"tree_and_density": 64.0 * ns, "move_steps": float(field_bytes),
+             "fof": 24.0 * nm, "groups_unbinding_outputs": 88.0 * n}
+    tot = sum(parts.values())
+    achieved = tot / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes_per_step": tot,
+            "components": {k: round(v) for k, v in parts.items()}}
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -472,10 +490,12 @@ def run_gpu(args):
     tot_ms = reduce_max(sum(step_ms), world, "cuda")
     value = job_value(world, n, args.steps, tot_ms)
 
-    # roofline of the dominant kernel (move field): algorithmic bytes / event time
-    f_ms = t_after["field_ms"] - t_before["field_ms"]
-    f_bytes = t_after["field_bytes"] - t_before["field_bytes"]
-    f_launch = t_after["gather_launches"] - t_before["gather_launches"]
+    # roofline of the dominant kernel (move field): algorithmic bytes / event
+    # time, from the library's figures, which restart with every run: those
+    # of the last timed run (the launch count above is cumulative)
+    f_ms = t_after["field_ms"]
+    f_bytes = t_after["field_bytes"]
+    f_launch = t_after["gather_launches"]
     peak, peak_kind = measured_peak()
     achieved = (f_bytes / f_launch) / (f_ms / f_launch / 1000.0) / 1e9 if f_ms > 0 else 0.0
 
@@ -591,6 +611,7 @@ def run_gpu(args):
                      "issue": {"frac": field_issue(), "unit": "fraction of peak issue slots",
                                "source": "static: ncu issue active of one launch at full "
                                          "activity (profiles/field_kernel_skid_config1_2e21.md)"}},
+        "roofline_e2e": roofline_e2e(res.counts, n, f_bytes, tot_ms / args.steps, peak, peak_kind),
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

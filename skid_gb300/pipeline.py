@@ -74,8 +74,9 @@ def run(snap: tipsy.Snapshot, opts: Options, ctx: gpu.Context | None = None, log
             ctx.set_groups(grp_in, centers)
             n_fof = int(grp_in.max(initial=0))
         else:
-            ctx.scatter_active(opts.bGasAndDark, opts.bGasOnly)
+            counts["nScatter"] = ctx.scatter_active(opts.bGasAndDark, opts.bGasOnly)
             nextra = ctx.density()
+            counts["nExtraScat"] = nextra
             if opts.periodic:
                 say(f"nExtraScat:{nextra}")
             if want_density:
