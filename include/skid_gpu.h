@@ -95,7 +95,8 @@ const char *skid_last_cuda_error(const skid_ctx *ctx);
 
 /* kdReadTipsy (kd.c:122-222), data part: copies particles to the device.
  * pos/vel are float[3n], mass/soft/temp float[n]; temp may be NULL (0).
- * soft is hsmooth for gas and eps for dark and star. */
+ * soft is hsmooth for gas and eps for dark and star.  n = nGas + nDark +
+ * nStar must be 1 .. 2^28 with no negative count (else SKID_EINVAL). */
 int skid_set_particles(skid_ctx *ctx, int nGas, int nDark, int nStar, double time,
                        const float *pos, const float *vel, const float *mass,
                        const float *soft, const float *temp);

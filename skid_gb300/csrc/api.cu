@@ -503,7 +503,9 @@ namespace {
 int load_begin(skid_ctx *ctx, int nGas, int nDark, int nStar, double time)
 {
     long long nn = (long long)nGas + nDark + nStar;
-    if (nn > (1ll << 28)) return ctx->fail(SKID_EINVAL);
+    // no particles, a negative count or more than 2^28: nothing to run
+    if (nGas < 0 || nDark < 0 || nStar < 0 || nn <= 0 || nn > (1ll << 28))
+        return ctx->fail(SKID_EINVAL);
     int n = (int)nn;
     cudaSetDevice(ctx->par.device);
     ctx->reset_pipeline();
