@@ -78,7 +78,8 @@ typedef struct skid_timings {
                                    scatterer (position, mass, fBall2) */
 } skid_timings;
 
-/* kdInit (kd.c:46-82) + smInit (smooth1.c:8-29). */
+/* kdInit (kd.c:46-82) + smInit (smooth1.c:8-29).  nSmooth >= 1 and every
+ * period > 0 (FLT_MAX: no period), else SKID_EINVAL before any device work. */
 int skid_create(skid_ctx **pctx, const skid_params *par);
 
 /* kdFinish (kd.c:1842-1850) + smFinish (smooth1.c:32-38). */
@@ -214,6 +215,9 @@ int skid_get_moved(skid_ctx *ctx, float *pos);
  * (smooth1.c:463-470); kdOutStats reads these (kd.c:1790). */
 int skid_get_final_density(skid_ctx *ctx, float *rho);
 
+/* The stage times and the move-field figures of the current run (they
+ * restart with skid_set_particles, skid_set_tipsy and skid_restart);
+ * kernel_launches counts from process start. */
 int skid_get_timings(skid_ctx *ctx, skid_timings *t);
 
 /* Work counters of the move-field kernel (no reference counterpart): with

@@ -394,6 +394,9 @@ int skid_create(skid_ctx **pctx, const skid_params *par)
     if (!pctx || !par) return SKID_EINVAL;
     *pctx = nullptr;
     if (par->nSmooth < 1) return SKID_EINVAL;
+    // a period is positive (FLT_MAX: no period along that axis); NaN fails too
+    for (int d = 0; d < 3; ++d)
+        if (!(par->period[d] > 0.0f)) return SKID_EINVAL;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= par->device || par->device < 0) {
         cudaGetLastError();

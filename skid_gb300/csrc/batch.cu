@@ -105,6 +105,8 @@ extern "C" int skid_batch_run(skid_volume *vols, int nVol, const skid_batch_flag
     for (int i = 0; i < nVol; ++i) {
         vols[i].status = SKID_ENODEV;   // until a worker runs it
         vols[i].message[0] = 0;
+        for (int d = 0; d < 3; ++d)
+            if (!(vols[i].period[d] > 0.0f) || vols[i].nSmooth < 1) return SKID_EINVAL;
     }
     // largest volumes first
     std::vector<int> order(nVol);

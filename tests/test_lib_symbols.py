@@ -39,3 +39,21 @@ def test_no_device_is_an_error_not_a_crash():
     with pytest.raises(gpu.SkidError) as e:
         gpu.Context(period=1.0, nSmooth=32)
     assert e.value.code == -6
+
+
+def test_bad_parameters_are_refused_before_any_device_work():
+    """A smoothing count below 1 or a period that is not positive (NaN
+    included) is SKID_EINVAL from skid_create, checked before the device is
+    looked at, here or on a GPU host."""
+    from skid_gb300 import gpu
+    lib = gpu.load()
+    for period, k in (((1.0, 1.0, 1.0), 0), ((0.0, 0.0, 0.0), 32), ((1.0, -1.0, 1.0), 32),
+                      ((float("nan"),) * 3, 32)):
+        p = gpu.Params()
+        for d in range(3):
+            p.period[d] = period[d]
+        p.periodic = 1
+        p.nSmooth = k
+        h = ctypes.c_void_p()
+        assert lib.skid_create(ctypes.byref(h), ctypes.byref(p)) == -1, (period, k)
+        assert not h.value
