@@ -313,7 +313,9 @@ typedef struct skid_batch_flags {
  * every volume, whose period and step length they carry), and every volume
  * takes the usual fixed removal schedule rather than tuning one.
  * Results per volume are those of the single-volume sequence.  Returns 0 if
- * every volume succeeded, else the first failing volume's status. */
+ * every volume succeeded, else the first failing volume's status; a volume
+ * with a period that is not positive or nSmooth below 1 makes the call
+ * return SKID_EINVAL before any work. */
 int skid_batch_run(skid_volume *vols, int nVol, const skid_batch_flags *flags, int nWorkers,
                    int device);
 
